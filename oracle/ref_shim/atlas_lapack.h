@@ -1,0 +1,25 @@
+/* LAPACK-layer names used by the extracted routines.  TEST INFRASTRUCTURE ONLY. */
+#ifndef REFSHIM_LAPACK_H
+#define REFSHIM_LAPACK_H
+#include "atlas_misc.h"
+#define ATL_getrfC Mjoin(PATL,getrfC)
+#define ATL_getrfR Mjoin(PATL,getrfR)
+#define ATL_getrs  Mjoin(PATL,getrs)
+#define ATL_laswp  Mjoin(PATL,laswp)
+int  ATL_dgetrfC(const int, const int, double*, const int, int*);
+int  ATL_sgetrfC(const int, const int, float*, const int, int*);
+int  ATL_dgetrfR(const int, const int, double*, const int, int*);
+int  ATL_sgetrfR(const int, const int, float*, const int, int*);
+int  ATL_dgetf2(const int, const int, double*, const int, int*);
+int  ATL_sgetf2(const int, const int, float*, const int, int*);
+void ATL_dlaswp(const int, double*, const int, const int, const int, const int*, const int);
+void ATL_slaswp(const int, float*, const int, const int, const int, const int*, const int);
+void ATL_dgetrs(const enum CBLAS_ORDER, const enum CBLAS_TRANSPOSE, const int, const int,
+                const double*, const int, const int*, double*, const int);
+void ATL_sgetrs(const enum CBLAS_ORDER, const enum CBLAS_TRANSPOSE, const int, const int,
+                const float*, const int, const int*, float*, const int);
+void ATL_dger(const int, const int, const double, const double*, const int, const double*,
+              const int, double*, const int);
+void ATL_sger(const int, const int, const float, const float*, const int, const float*,
+              const int, float*, const int);
+#endif

@@ -1,0 +1,158 @@
+"""Generates tests/golden/atlas_ref_fixtures.npz from the reference's own
+routines (oracle/_ref/libatlref.so, built by oracle/ref_build.sh from the
+reference basefiles).  Run once where the reference source tree is present:
+
+    sh oracle/ref_build.sh && python tests/golden/make_golden.py
+
+The fixtures pin the oracle and the GPU library to the reference:
+  * ATL_rand streams and ATL_gegen matrices (bit-exact),
+  * ATL_getrfC / ATL_getrfR pivots and info (bit-exact) and LU factors,
+  * ATL_laswp permutations (bit-exact),
+  * ATL_getrs solutions, reference-BLAS gemm and trsm results (tolerance).
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+REFLIB = os.path.join(ROOT, "oracle", "_ref", "libatlref.so")
+OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "atlas_ref_fixtures.npz")
+
+dp = np.ctypeslib.ndpointer(np.float64, flags="F_CONTIGUOUS")
+sp = np.ctypeslib.ndpointer(np.float32, flags="F_CONTIGUOUS")
+ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+I, D, F = C.c_int, C.c_double, C.c_float
+
+
+def load():
+    R = C.CDLL(REFLIB)
+    R.atlref_srand.argtypes = [I]
+    R.atlref_rand.restype = I
+    R.atlref_dgegen.argtypes = [I, I, dp, I, I]
+    R.atlref_sgegen.argtypes = [I, I, sp, I, I]
+    R.atlref_dgetrf.argtypes = [I, I, I, dp, I, ip]
+    R.atlref_dgetrf.restype = I
+    R.atlref_sgetrf.argtypes = [I, I, I, sp, I, ip]
+    R.atlref_sgetrf.restype = I
+    R.atlref_dgetrs.argtypes = [I, I, I, I, dp, I, ip, dp, I]
+    R.atlref_dlaswp.argtypes = [I, dp, I, I, I, ip, I]
+    R.atlref_dgemm.argtypes = [I, I, I, I, I, I, D, dp, I, dp, I, D, dp, I]
+    R.atlref_dtrsm.argtypes = [I, I, I, I, I, I, I, D, dp, I, dp, I]
+    return R
+
+
+def gegen(R, M, N, lda, seed, dtype=np.float64):
+    A = np.zeros((lda, N), dtype=dtype, order="F")
+    (R.atlref_dgegen if dtype == np.float64 else R.atlref_sgegen)(M, N, A, lda, seed)
+    return A
+
+
+# (M, N, lda) cases of the LU fixtures; seeds follow xdlutst (M*N+lda)
+LU_CASES = [(1, 1, 1), (2, 2, 2), (3, 5, 4), (5, 3, 7), (17, 17, 17), (64, 64, 64),
+            (100, 100, 103), (37, 80, 40), (80, 37, 80), (129, 129, 130), (200, 200, 200),
+            (257, 513, 260)]
+GEMM_CASES = [(111, 111, 37, 29, 41, 1.0, 0.0), (111, 112, 64, 64, 64, 1.0, 0.0),
+              (112, 111, 33, 65, 17, -1.5, 0.5), (112, 112, 50, 20, 70, 0.75, -2.0),
+              (111, 111, 128, 96, 1, 1.0, 1.0)]
+
+
+def main():
+    if not os.path.exists(REFLIB):
+        sys.exit("build the reference routines first: sh oracle/ref_build.sh")
+    R = load()
+    out = {}
+    seeds = np.array([0, 1, 7, 513 * 7 + 90, 12345, 65536 + 3, 8192 * 8192 + 8192, -5, 2**31 - 1],
+                     dtype=np.int64)
+    streams = []
+    for s in seeds:
+        R.atlref_srand(int(s))
+        streams.append([R.atlref_rand() for _ in range(256)])
+    out["rand_seeds"] = seeds
+    out["rand_streams"] = np.array(streams, dtype=np.int64)
+    out["gegen_7x3_lda9"] = gegen(R, 7, 3, 9, 7 * 3 + 9)
+    out["sgegen_7x3_lda9"] = gegen(R, 7, 3, 9, 7 * 3 + 9, np.float32)
+
+    out["lu_cases"] = np.array(LU_CASES, dtype=np.int64)
+    for (M, N, lda) in LU_CASES:
+        for order, tag in ((102, "C"), (101, "R")):
+            rows = M if order == 102 else N
+            cols = N if order == 102 else M
+            ld = max(lda, rows)
+            A = gegen(R, rows, cols, ld, M * N + lda)
+            piv = np.zeros(max(min(M, N), 1), dtype=np.int32)
+            info = R.atlref_dgetrf(order, M, N, A, ld, piv)
+            key = f"lu{tag}_{M}x{N}_{lda}"
+            out[key + "_ipiv"] = piv[: min(M, N)].copy()
+            out[key + "_info"] = np.array(info)
+            if rows * cols <= 130 * 130:
+                out[key + "_lu"] = A[:rows, :cols].copy()
+        As = gegen(R, M, N, max(lda, M), M * N + lda, np.float32)
+        piv = np.zeros(max(min(M, N), 1), dtype=np.int32)
+        info = R.atlref_sgetrf(102, M, N, As, max(lda, M), piv)
+        out[f"sluC_{M}x{N}_{lda}_ipiv"] = piv[: min(M, N)].copy()
+        out[f"sluC_{M}x{N}_{lda}_info"] = np.array(info)
+
+    # singular matrices: a zero column (info = first zero pivot, 1-based)
+    for (n, zc) in ((8, 3), (50, 0), (64, 63), (100, 70)):
+        A = gegen(R, n, n, n, n * n + n)
+        A[:, zc] = 0.0
+        A0 = A.copy(order="F")
+        piv = np.zeros(n, dtype=np.int32)
+        info = R.atlref_dgetrf(102, n, n, A, n, piv)
+        out[f"sing_{n}_{zc}_a"] = A0
+        out[f"sing_{n}_{zc}_ipiv"] = piv
+        out[f"sing_{n}_{zc}_info"] = np.array(info)
+        out[f"sing_{n}_{zc}_lu"] = A.copy()
+
+    # laswp forward and backward with a random pivot vector (ipiv[i] >= i)
+    rng = np.random.default_rng(20260)
+    for (m, n, k1, k2) in ((40, 70, 0, 40), (100, 33, 5, 77), (64, 64, 0, 64)):
+        piv = np.array([rng.integers(i, m) for i in range(m)], dtype=np.int32)
+        A = gegen(R, m, n, m, m * n)
+        for inci in (1, -1):
+            B = A.copy(order="F")
+            R.atlref_dlaswp(n, B, m, k1, k2, piv, inci)
+            out[f"laswp_{m}_{n}_{k1}_{k2}_{inci}"] = B
+        out[f"laswp_{m}_{n}_{k1}_{k2}_piv"] = piv
+
+    # getrs NoTrans / Trans on the factor of a 60x60 and a 129x129 matrix
+    for n, nrhs in ((60, 3), (129, 5)):
+        A = gegen(R, n, n, n, n * n + n)
+        piv = np.zeros(n, dtype=np.int32)
+        R.atlref_dgetrf(102, n, n, A, n, piv)
+        for trans in (111, 112):
+            B = gegen(R, n, nrhs, n, 77 + n)
+            R.atlref_dgetrs(102, trans, n, nrhs, A, n, piv, B, n)
+            out[f"getrs_{n}_{nrhs}_{trans}"] = B
+
+    # reference-BLAS gemm (gemmtst seeds)
+    out["gemm_cases"] = np.array(GEMM_CASES, dtype=np.float64)
+    for (ta, tb, M, N, K, al, be) in GEMM_CASES:
+        mA, nA = (M, K) if ta == 111 else (K, M)
+        mB, nB = (K, N) if tb == 111 else (N, K)
+        A = gegen(R, mA, nA, mA, mA * nA + 513 * 7 + 90)
+        B = gegen(R, mB, nB, mB, mB * nB + 127 * 50 + 77)
+        Cm = gegen(R, M, N, M, M * N + 101 * 2 + 53)
+        R.atlref_dgemm(102, ta, tb, M, N, K, al, A, mA, B, mB, be, Cm, M)
+        out[f"gemm_{ta}_{tb}_{M}_{N}_{K}"] = Cm
+
+    # reference trsm, all 16 Side/Uplo/Trans/Diag cases, diagonally dominant A
+    for side in (141, 142):
+        for uplo in (121, 122):
+            for ta in (111, 112):
+                for diag in (131, 132):
+                    M, N = 45, 38
+                    na = M if side == 141 else N
+                    A = gegen(R, na, na, na, na * na + 11)
+                    A += np.eye(na) * na
+                    B = gegen(R, M, N, M, M * N + 3)
+                    R.atlref_dtrsm(102, side, uplo, ta, diag, M, N, 1.5, A, na, B, M)
+                    out[f"trsm_{side}_{uplo}_{ta}_{diag}"] = B
+    np.savez_compressed(OUT, **out)
+    print("wrote", OUT, os.path.getsize(OUT), "bytes")
+
+
+if __name__ == "__main__":
+    main()
