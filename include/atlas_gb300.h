@@ -1,0 +1,109 @@
+/*
+ * atlas_gb300.h -- C ABI of the GB300 (sm_103a) implementation of ATLAS's
+ * Level-3 / LU path.
+ *
+ * The cblas_* and clapack_* entry points have the reference's names,
+ * prototypes, enum values, argument checks and return conventions, so a
+ * program built against ATLAS's cblas.h / clapack.h links against
+ * libatlas_gb300.so unchanged.  Each declaration cites the reference
+ * interface it replaces (paths inside the ATLAS source tree).
+ *
+ * Conventions (as in the reference):
+ *  - the caller owns every array; A and B are overwritten in place;
+ *  - ipiv is caller allocated, min(M,N) ints, 0-based row indices;
+ *  - an invalid argument prints "Parameter %d to routine %s was incorrect"
+ *    on stderr and exits with status -1 (cblas_xerbla);
+ *  - clapack_*getrf returns i > 0 when U(i-1,i-1) is exactly zero (the
+ *    factorization is completed);
+ *  - every host-pointer call is synchronous and must be made from one host
+ *    thread at a time.
+ * The atlg_*_dev variants take device pointers and a CUDA stream (NULL:
+ * the library's stream), are asynchronous, and return 0 or -1 for a bad size.
+ */
+#ifndef ATLAS_GB300_H
+#define ATLAS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* AtlasBase/Clint/atlas.base:19800-19806 (cblas.h enums) */
+#ifndef CBLAS_ENUM_DEFINED_H
+#define CBLAS_ENUM_DEFINED_H
+enum CBLAS_ORDER {CblasRowMajor=101, CblasColMajor=102};
+enum CBLAS_TRANSPOSE {CblasNoTrans=111, CblasTrans=112, CblasConjTrans=113, AtlasConj=114};
+enum CBLAS_UPLO {CblasUpper=121, CblasLower=122};
+enum CBLAS_DIAG {CblasNonUnit=131, CblasUnit=132};
+enum CBLAS_SIDE {CblasLeft=141, CblasRight=142};
+#endif
+
+/* ---- error reporting: AtlasBase/Clint/cblas.base:14 (cblas_errprn), :42 (cblas_xerbla) */
+int  cblas_errprn(int ierr, int info, const char *form, ...);
+void cblas_xerbla(int p, const char *rout, const char *form, ...);
+
+/* ---- Level 3: AtlasBase/Clint/cblas.base:110-236 (GEMM template, d and s) */
+void cblas_dgemm(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TA,
+                 const enum CBLAS_TRANSPOSE TB, const int M, const int N, const int K,
+                 const double alpha, const double *A, const int lda, const double *B,
+                 const int ldb, const double beta, double *C, const int ldc);
+void cblas_sgemm(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TA,
+                 const enum CBLAS_TRANSPOSE TB, const int M, const int N, const int K,
+                 const float alpha, const float *A, const int lda, const float *B,
+                 const int ldb, const float beta, float *C, const int ldc);
+
+/* ---- Level 3: AtlasBase/Clint/cblas.base:600-692 (TRSM template, d and s) */
+void cblas_dtrsm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side,
+                 const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TA,
+                 const enum CBLAS_DIAG Diag, const int M, const int N, const double alpha,
+                 const double *A, const int lda, double *B, const int ldb);
+void cblas_strsm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side,
+                 const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TA,
+                 const enum CBLAS_DIAG Diag, const int M, const int N, const float alpha,
+                 const float *A, const int lda, float *B, const int ldb);
+
+/* ---- LAPACK: AtlasBase/Clint/atlas-clp.base:140 (clapack_getrf, d and s) */
+int clapack_dgetrf(const enum CBLAS_ORDER Order, const int M, const int N, double *A,
+                   const int lda, int *ipiv);
+int clapack_sgetrf(const enum CBLAS_ORDER Order, const int M, const int N, float *A,
+                   const int lda, int *ipiv);
+/* ---- LAPACK: AtlasBase/Clint/atlas-clp.base:218 (clapack_getrs, d and s) */
+int clapack_dgetrs(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE Trans, const int N,
+                   const int NRHS, const double *A, const int lda, const int *ipiv, double *B,
+                   const int ldb);
+int clapack_sgetrs(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE Trans, const int N,
+                   const int NRHS, const float *A, const int lda, const int *ipiv, float *B,
+                   const int ldb);
+/* ---- LAPACK: AtlasBase/Clint/atlas-clp.base:62 (clapack_gesv, d and s) */
+int clapack_dgesv(const enum CBLAS_ORDER Order, const int N, const int NRHS, double *A,
+                  const int lda, int *ipiv, double *B, const int ldb);
+int clapack_sgesv(const enum CBLAS_ORDER Order, const int N, const int NRHS, float *A,
+                  const int lda, int *ipiv, float *B, const int ldb);
+
+/* ---- device-pointer variants (no reference counterpart: the reference has
+ *      no device memory; these are the same operations on GPU-resident data,
+ *      column-major, used by callers that keep matrices in HBM) */
+int      atlg_num_sms(void);
+void    *atlg_stream(void);
+unsigned atlg_status(void);   /* device wait-timeout flags since the last call, cleared */
+int atlg_dgemm_dev(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda,
+                   const double *B, int ldb, double beta, double *C, int ldc, void *stream);
+int atlg_dgemm_dev_opts(int TA, int TB, int M, int N, int K, double alpha, const double *A,
+                        int lda, const double *B, int ldb, double beta, double *C, int ldc,
+                        int allow_tma, void *stream);
+int atlg_sgemm_dev(int TA, int TB, int M, int N, int K, float alpha, const float *A, int lda,
+                   const float *B, int ldb, float beta, float *C, int ldc, void *stream);
+int atlg_dtrsm_dev(int Side, int Uplo, int TA, int Diag, int M, int N, double alpha,
+                   const double *A, int lda, double *B, int ldb, void *stream);
+/* ATL_laswp semantics (AtlasBase/Clint/atlas-lp.base:1053); rows [0,nrows) may move */
+int atlg_dlaswp_dev(int N, double *A, int lda, int K1, int K2, const int *ipiv, int inci,
+                    int nrows, void *stream);
+/* column-major LU; info written to device memory */
+int atlg_dgetrf_dev(int M, int N, double *A, int lda, int *ipiv, int *info, void *stream);
+int atlg_sgetrf_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void *stream);
+int atlg_dgetrs_dev(int Order, int Trans, int N, int NRHS, const double *A, int lda,
+                    const int *ipiv, double *B, int ldb, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

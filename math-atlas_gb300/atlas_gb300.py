@@ -1,0 +1,152 @@
+"""ctypes binding of libatlas_gb300.so (the C ABI declared in include/atlas_gb300.h).
+
+The host-pointer functions mirror the reference's cblas_* / clapack_* calls on
+numpy arrays; the ``*_dev`` functions take device pointers (e.g. torch CUDA
+tensors' ``data_ptr()``) and a CUDA stream handle.  There is no fallback: if
+the shared library is missing or fails to load, every call raises.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libatlas_gb300.so")
+
+RowMajor, ColMajor = 101, 102
+NoTrans, Trans, ConjTrans = 111, 112, 113
+Upper, Lower = 121, 122
+NonUnit, Unit = 131, 132
+Left, Right = 141, 142
+
+# every exported symbol of include/atlas_gb300.h
+EXPORTS = [
+    "cblas_errprn", "cblas_xerbla", "cblas_dgemm", "cblas_sgemm", "cblas_dtrsm", "cblas_strsm",
+    "clapack_dgetrf", "clapack_sgetrf", "clapack_dgetrs", "clapack_sgetrs", "clapack_dgesv",
+    "clapack_sgesv", "atlg_num_sms", "atlg_stream", "atlg_status", "atlg_dgemm_dev",
+    "atlg_dgemm_dev_opts", "atlg_sgemm_dev", "atlg_dtrsm_dev", "atlg_dlaswp_dev", "atlg_dgetrf_dev",
+    "atlg_sgetrf_dev", "atlg_dgetrs_dev",
+]
+
+_lib = None
+
+
+def build(jobs=8):
+    subprocess.check_call(["make", "-s", "-j%d" % jobs, "-C", HERE, "libatlas_gb300.so"])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libatlas_gb300.so is not built (run __graft_entry__.build())")
+        _lib = C.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="F_CONTIGUOUS")
+_sp = np.ctypeslib.ndpointer(dtype=np.float32, flags="F_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_i, _d, _f, _v, _u = C.c_int, C.c_double, C.c_float, C.c_void_p, C.c_uint
+
+
+def _declare(L):
+    sig = {
+        "cblas_dgemm": (None, [_i, _i, _i, _i, _i, _i, _d, _dp, _i, _dp, _i, _d, _dp, _i]),
+        "cblas_sgemm": (None, [_i, _i, _i, _i, _i, _i, _f, _sp, _i, _sp, _i, _f, _sp, _i]),
+        "cblas_dtrsm": (None, [_i, _i, _i, _i, _i, _i, _i, _d, _dp, _i, _dp, _i]),
+        "cblas_strsm": (None, [_i, _i, _i, _i, _i, _i, _i, _f, _sp, _i, _sp, _i]),
+        "clapack_dgetrf": (_i, [_i, _i, _i, _dp, _i, _ip]),
+        "clapack_sgetrf": (_i, [_i, _i, _i, _sp, _i, _ip]),
+        "clapack_dgetrs": (_i, [_i, _i, _i, _i, _dp, _i, _ip, _dp, _i]),
+        "clapack_sgetrs": (_i, [_i, _i, _i, _i, _sp, _i, _ip, _sp, _i]),
+        "clapack_dgesv": (_i, [_i, _i, _i, _dp, _i, _ip, _dp, _i]),
+        "clapack_sgesv": (_i, [_i, _i, _i, _sp, _i, _ip, _sp, _i]),
+        "atlg_num_sms": (_i, []),
+        "atlg_stream": (_v, []),
+        "atlg_status": (_u, []),
+        "atlg_dgemm_dev": (_i, [_i, _i, _i, _i, _i, _d, _v, _i, _v, _i, _d, _v, _i, _v]),
+        "atlg_dgemm_dev_opts": (_i, [_i, _i, _i, _i, _i, _d, _v, _i, _v, _i, _d, _v, _i, _i, _v]),
+        "atlg_sgemm_dev": (_i, [_i, _i, _i, _i, _i, _f, _v, _i, _v, _i, _f, _v, _i, _v]),
+        "atlg_dtrsm_dev": (_i, [_i, _i, _i, _i, _i, _i, _d, _v, _i, _v, _i, _v]),
+        "atlg_dlaswp_dev": (_i, [_i, _v, _i, _i, _i, _v, _i, _i, _v]),
+        "atlg_dgetrf_dev": (_i, [_i, _i, _v, _i, _v, _v, _v]),
+        "atlg_sgetrf_dev": (_i, [_i, _i, _v, _i, _v, _v, _v]),
+        "atlg_dgetrs_dev": (_i, [_i, _i, _i, _i, _v, _i, _v, _v, _i, _v]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def _f64(a):
+    if not (a.dtype == np.float64 and a.flags.f_contiguous):
+        raise TypeError("expected a Fortran-ordered float64 array")
+    return a
+
+
+# ------------------------------------------------------------ host-pointer API
+def cblas_dgemm(order, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, Cm, ldc):
+    lib().cblas_dgemm(order, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, Cm, ldc)
+
+
+def cblas_sgemm(order, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, Cm, ldc):
+    lib().cblas_sgemm(order, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, Cm, ldc)
+
+
+def cblas_dtrsm(order, side, uplo, ta, diag, M, N, alpha, A, lda, B, ldb):
+    lib().cblas_dtrsm(order, side, uplo, ta, diag, M, N, alpha, A, lda, B, ldb)
+
+
+def cblas_strsm(order, side, uplo, ta, diag, M, N, alpha, A, lda, B, ldb):
+    lib().cblas_strsm(order, side, uplo, ta, diag, M, N, alpha, A, lda, B, ldb)
+
+
+def clapack_dgetrf(order, M, N, A, lda, ipiv):
+    return lib().clapack_dgetrf(order, M, N, A, lda, ipiv)
+
+
+def clapack_sgetrf(order, M, N, A, lda, ipiv):
+    return lib().clapack_sgetrf(order, M, N, A, lda, ipiv)
+
+
+def clapack_dgetrs(order, trans, N, NRHS, A, lda, ipiv, B, ldb):
+    return lib().clapack_dgetrs(order, trans, N, NRHS, A, lda, ipiv, B, ldb)
+
+
+def clapack_dgesv(order, N, NRHS, A, lda, ipiv, B, ldb):
+    return lib().clapack_dgesv(order, N, NRHS, A, lda, ipiv, B, ldb)
+
+
+def clapack_sgesv(order, N, NRHS, A, lda, ipiv, B, ldb):
+    return lib().clapack_sgesv(order, N, NRHS, A, lda, ipiv, B, ldb)
+
+
+# convenience wrappers on whole arrays (column-major)
+def dgemm(ta, tb, alpha, A, B, beta, Cm):
+    M, N = Cm.shape
+    K = A.shape[1] if ta == NoTrans else A.shape[0]
+    f = cblas_dgemm if Cm.dtype == np.float64 else cblas_sgemm
+    f(ColMajor, ta, tb, M, N, K, alpha, A, A.shape[0], B, B.shape[0], beta, Cm, Cm.shape[0])
+    return Cm
+
+
+def getrf(A, order=ColMajor, M=None, N=None):
+    M = A.shape[0] if M is None else M
+    N = A.shape[1] if N is None else N
+    ipiv = np.zeros(max(min(M, N), 1), dtype=np.int32)
+    f = clapack_dgetrf if A.dtype == np.float64 else clapack_sgetrf
+    info = f(order, M, N, A, A.shape[0], ipiv)
+    return info, ipiv[: min(M, N)]
+
+
+# ---------------------------------------------------------- device-pointer API
+def status():
+    return lib().atlg_status()
+
+
+def num_sms():
+    return lib().atlg_num_sms()

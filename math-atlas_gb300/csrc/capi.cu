@@ -1,0 +1,459 @@
+// capi.cu -- the drop-in C ABI: cblas_* / clapack_* with the reference's
+// prototypes, argument checks, error messages and return conventions, plus
+// device-pointer variants (atlg_*_dev) for callers whose data already lives
+// in GPU memory.
+//
+// Host-pointer entry points are synchronous like the reference's: they copy
+// the operands to cached device buffers (packed, leading dimension rounded
+// up to an even count so TMA can address them), run on the library's stream
+// and copy the results back before returning.
+//
+// Argument checking follows AtlasBase/Clint/cblas.base (cblas_errprn :14,
+// cblas_xerbla :42 -- message to stderr and exit(-1); GEMM checks :119-216,
+// TRSM checks :611-677) and AtlasBase/Clint/atlas-clp.base (clapack_gesv :62,
+// clapack_getrf :140, clapack_getrs :218).
+#include <stdarg.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../../include/atlas_gb300.h"
+#include "common.cuh"
+#include "context.cuh"
+#include "gemm.cuh"
+#include "lu.cuh"
+#include "trsm.cuh"
+
+using namespace atlg;
+
+// ------------------------------------------------------------ error reporting
+extern "C" int cblas_errprn(int ierr, int info, const char *form, ...) {
+  va_list ap;
+  va_start(ap, form);
+  vfprintf(stderr, form, ap);
+  va_end(ap);
+  return ierr < info ? ierr : info;
+}
+
+extern "C" void cblas_xerbla(int p, const char *rout, const char *form, ...) {
+  va_list ap;
+  va_start(ap, form);
+  if (p) fprintf(stderr, "Parameter %d to routine %s was incorrect\n", p, rout);
+  vfprintf(stderr, form, ap);
+  va_end(ap);
+  fflush(stderr);
+  exit(-1);
+}
+
+namespace {
+
+void check_status(const char *rout) {
+  const unsigned s = gemm_status_read_and_clear() | lu_status_read_and_clear();
+  if (s) {
+    fprintf(stderr, "atlas_gb300: %s: device wait gave up (status 0x%x)\n", rout, s);
+    fflush(stderr);
+    abort();
+  }
+}
+
+inline int even_up(int n) { return n < 2 ? 2 : (n + 1) & ~1; }
+
+template <typename T>
+T *to_dev(int slot, const T *h, int rows, int cols, int ldh, int *ldd, cudaStream_t st) {
+  *ldd = even_up(rows);
+  T *d = static_cast<T *>(ctx().buffer(slot, sizeof(T) * (size_t)(*ldd) * (cols > 0 ? cols : 1)));
+  if (rows > 0 && cols > 0)
+    ATLG_CHECK(cudaMemcpy2DAsync(d, sizeof(T) * (*ldd), h, sizeof(T) * ldh, sizeof(T) * rows, cols,
+                                 cudaMemcpyHostToDevice, st));
+  return d;
+}
+
+template <typename T>
+void to_host(T *h, int ldh, const T *d, int ldd, int rows, int cols, cudaStream_t st) {
+  if (rows > 0 && cols > 0)
+    ATLG_CHECK(cudaMemcpy2DAsync(h, sizeof(T) * ldh, d, sizeof(T) * ldd, sizeof(T) * rows, cols,
+                                 cudaMemcpyDeviceToHost, st));
+}
+
+cudaStream_t stream_of(void *s) { return s ? static_cast<cudaStream_t>(s) : ctx().stream; }
+
+// ---------------------------------------------------------------------- GEMM
+template <typename T>
+int gemm_check(const char *rout, int Order, int TA, int TB, int M, int N, int K, int lda, int ldb, int ldc) {
+  int info = 2000;
+  if (M < 0) info = cblas_errprn(4, info, "M cannot be less than zero 0,; is set to %d.", M);
+  if (N < 0) info = cblas_errprn(5, info, "N cannot be less than zero 0,; is set to %d.", N);
+  if (K < 0) info = cblas_errprn(6, info, "K cannot be less than zero 0,; is set to %d.", K);
+  if (Order == CblasRowMajor) {
+    if (TA == CblasNoTrans) {
+      if (lda < K || lda < 1) info = cblas_errprn(9, info, "lda must be >= MAX(K,1): lda=%d K=%d", lda, K);
+    } else {
+      if (TA != CblasConjTrans && TA != CblasTrans)
+        info = cblas_errprn(2, info, "TransA must be %d, %d or %d, but is set to %d", CblasNoTrans, CblasTrans,
+                            CblasConjTrans, TA);
+      if (lda < M || lda < 1) info = cblas_errprn(9, info, "lda must be >= MAX(M,1): lda=%d M=%d", lda, M);
+    }
+    if (TB == CblasNoTrans) {
+      if (ldb < N || ldb < 1) info = cblas_errprn(11, info, "ldb must be >= MAX(N,1): ldb=%d N=%d", ldb, N);
+    } else {
+      if (TB != CblasConjTrans && TB != CblasTrans)
+        info = cblas_errprn(3, info, "TransB must be %d, %d or %d, but is set to %d", CblasNoTrans, CblasTrans,
+                            CblasConjTrans, TB);
+      if (ldb < K || ldb < 1) info = cblas_errprn(11, info, "ldb must be >= MAX(K,1): ldb=%d K=%d", ldb, K);
+    }
+    if (ldc < N || ldc < 1) info = cblas_errprn(14, info, "ldc must be >= MAX(N,1): ldc=%d N=%d", ldc, N);
+  } else if (Order == CblasColMajor) {
+    if (TA == CblasNoTrans) {
+      if (lda < M || lda < 1) info = cblas_errprn(9, info, "lda must be >= MAX(M,1): lda=%d M=%d", lda, M);
+    } else {
+      if (TA != CblasConjTrans && TA != CblasTrans)
+        info = cblas_errprn(2, info, "TransA must be %d, %d or %d, but is set to %d", CblasNoTrans, CblasTrans,
+                            CblasConjTrans, TA);
+      if (lda < K || lda < 1) info = cblas_errprn(9, info, "lda must be >= MAX(K,1): lda=%d K=%d", lda, K);
+    }
+    if (TB == CblasNoTrans) {
+      if (ldb < K || ldb < 1) info = cblas_errprn(11, info, "ldb must be >= MAX(K,1): ldb=%d K=%d", ldb, K);
+    } else {
+      if (TB != CblasConjTrans && TB != CblasTrans)
+        info = cblas_errprn(3, info, "TransB must be %d, %d or %d, but is set to %d", CblasNoTrans, CblasTrans,
+                            CblasConjTrans, TB);
+      if (ldb < N || ldb < 1) info = cblas_errprn(11, info, "ldb must be >= MAX(N,1): ldb=%d N=%d", ldb, N);
+    }
+    if (ldc < M || ldc < 1) info = cblas_errprn(14, info, "ldc must be >= MAX(M,1): ldc=%d M=%d", ldc, M);
+  } else {
+    info = cblas_errprn(1, info, "Order must be %d or %d, but is set to %d", CblasRowMajor, CblasColMajor, Order);
+  }
+  if (info != 2000) {
+    cblas_xerbla(info, rout, "");
+    return info;
+  }
+  return 0;
+}
+
+template <typename T>
+void dev_gemm_any(int TA, int TB, int M, int N, int K, T alpha, const T *A, int lda, const T *B, int ldb, T beta,
+                  T *C, int ldc, cudaStream_t st);
+template <>
+void dev_gemm_any<double>(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda,
+                          const double *B, int ldb, double beta, double *C, int ldc, cudaStream_t st) {
+  dev_dgemm(TA, TB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st);
+}
+template <>
+void dev_gemm_any<float>(int TA, int TB, int M, int N, int K, float alpha, const float *A, int lda, const float *B,
+                         int ldb, float beta, float *C, int ldc, cudaStream_t st) {
+  dev_sgemm(TA, TB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st);
+}
+
+template <typename T>
+void host_gemm(const char *rout, int Order, int TA, int TB, int M, int N, int K, T alpha, const T *A, int lda,
+               const T *B, int ldb, T beta, T *C, int ldc) {
+  if (gemm_check<T>(rout, Order, TA, TB, M, N, K, lda, ldb, ldc)) return;
+  if (M == 0 || N == 0) return;
+  if (Order == CblasRowMajor) {   // C^T = op(B)^T op(A)^T in column-major terms
+    const T *t = A; A = B; B = t;
+    int ti = lda; lda = ldb; ldb = ti;
+    ti = TA; TA = TB; TB = ti;
+    ti = M; M = N; N = ti;
+  }
+  cudaStream_t st = ctx().stream;
+  int ldd_c;
+  const bool need_c = (beta != T(0));
+  T *dC;
+  if (need_c) dC = to_dev<T>(kBufC, C, M, N, ldc, &ldd_c, st);
+  else {
+    ldd_c = even_up(M);
+    dC = static_cast<T *>(ctx().buffer(kBufC, sizeof(T) * (size_t)ldd_c * N));
+  }
+  if (alpha != T(0) && K > 0) {
+    const int ra = (TA == CblasNoTrans) ? M : K, ca = (TA == CblasNoTrans) ? K : M;
+    const int rb = (TB == CblasNoTrans) ? K : N, cb = (TB == CblasNoTrans) ? N : K;
+    int ldd_a, ldd_b;
+    const T *dA = to_dev<T>(kBufA, A, ra, ca, lda, &ldd_a, st);
+    const T *dB = to_dev<T>(kBufB, B, rb, cb, ldb, &ldd_b, st);
+    dev_gemm_any<T>(TA, TB, M, N, K, alpha, dA, ldd_a, dB, ldd_b, beta, dC, ldd_c, st);
+  } else {
+    dev_gescal(M, N, beta, dC, ldd_c, st);
+  }
+  to_host<T>(C, ldc, dC, ldd_c, M, N, st);
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  check_status(rout);
+}
+
+// ---------------------------------------------------------------------- TRSM
+int trsm_check(const char *rout, int Order, int Side, int Uplo, int TA, int Diag, int M, int N, int lda, int ldb) {
+  int info = 2000;
+  if (Order == CblasColMajor) {
+    if (Side == CblasLeft) {
+      if (lda < M || lda < 1) info = cblas_errprn(10, info, "lda must be >= MAX(M,1): lda=%d M=%d", lda, M);
+    } else if (Side == CblasRight) {
+      if (lda < N || lda < 1) info = cblas_errprn(10, info, "lda must be >= MAX(N,1): lda=%d N=%d", lda, N);
+    } else
+      info = cblas_errprn(2, info, "SIDE must be %d or %d, but is set to %d", CblasRight, CblasLeft, Side);
+    if (ldb < M || ldb < 1) info = cblas_errprn(12, info, "ldb must be >= MAX(M,1): ldb=%d M=%d", ldb, M);
+  } else if (Order == CblasRowMajor) {
+    if (Side == CblasLeft) {
+      if (lda < M || lda < 1) info = cblas_errprn(10, info, "lda must be >= MAX(M,1): lda=%d M=%d", lda, M);
+    } else if (Side == CblasRight) {
+      if (lda < N || lda < 1) info = cblas_errprn(10, info, "lda must be >= MAX(N,1): lda=%d N=%d", lda, N);
+    } else
+      info = cblas_errprn(2, info, "SIDE must be %d or %d, but is set to %d", CblasRight, CblasLeft, Side);
+    if (ldb < N || ldb < 1) info = cblas_errprn(12, info, "ldb must be >= MAX(N,1): ldb=%d N=%d", ldb, N);
+  } else
+    info = cblas_errprn(1, info, "Order must be %d or %d, but is set to %d", CblasRowMajor, CblasColMajor, Order);
+  if (Uplo != CblasUpper && Uplo != CblasLower)
+    info = cblas_errprn(3, info, "UPLO must be %d or %d, but is set to %d", CblasUpper, CblasLower, Uplo);
+  if (TA != CblasNoTrans && TA != CblasTrans && TA != CblasConjTrans)
+    info = cblas_errprn(4, info, "TransA must be %d, %d or %d, but is set to %d", CblasNoTrans, CblasTrans,
+                        CblasConjTrans, TA);
+  if (Diag != CblasUnit && Diag != CblasNonUnit)
+    info = cblas_errprn(5, info, "UPLO must be %d or %d, but is set to %d", CblasUnit, CblasNonUnit, Diag);
+  if (M < 0) info = cblas_errprn(6, info, "M cannot be less than zero; it is set to %d.", M);
+  if (N < 0) info = cblas_errprn(7, info, "N cannot be less than zero; it is set to %d.", N);
+  if (info != 2000) {
+    cblas_xerbla(info, rout, "");
+    return info;
+  }
+  return 0;
+}
+
+template <typename T>
+void dev_trsm_any(int side, int uplo, int ta, int diag, int M, int N, T alpha, const T *A, int lda, T *B, int ldb,
+                  cudaStream_t st) {
+  if (sizeof(T) == 8)
+    dev_dtrsm(side, uplo, ta, diag, M, N, (double)alpha, (const double *)A, lda, (double *)B, ldb, st);
+  else
+    dev_strsm(side, uplo, ta, diag, M, N, (float)alpha, (const float *)A, lda, (float *)B, ldb, st);
+}
+
+template <typename T>
+void host_trsm(const char *rout, int Order, int Side, int Uplo, int TA, int Diag, int M, int N, T alpha, const T *A,
+               int lda, T *B, int ldb) {
+  if (trsm_check(rout, Order, Side, Uplo, TA, Diag, M, N, lda, ldb)) return;
+  if (Order == CblasRowMajor) {
+    Side = (Side == CblasLeft) ? CblasRight : CblasLeft;
+    Uplo = (Uplo == CblasUpper) ? CblasLower : CblasUpper;
+    const int t = M; M = N; N = t;
+  }
+  if (M == 0 || N == 0) return;
+  cudaStream_t st = ctx().stream;
+  const int na = (Side == CblasLeft) ? M : N;
+  int ldd_a, ldd_b;
+  const T *dA = to_dev<T>(kBufA, A, na, na, lda, &ldd_a, st);
+  T *dB = to_dev<T>(kBufB, B, M, N, ldb, &ldd_b, st);
+  dev_trsm_any<T>(Side, Uplo, TA, Diag, M, N, alpha, dA, ldd_a, dB, ldd_b, st);
+  to_host<T>(B, ldb, dB, ldd_b, M, N, st);
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  check_status(rout);
+}
+
+// ---------------------------------------------------------------- LAPACK LU
+template <typename T>
+void dev_getrf_any(int M, int N, T *A, int lda, int *ipiv, int *info, cudaStream_t st) {
+  if (sizeof(T) == 8) dev_dgetrf(M, N, (double *)A, lda, ipiv, info, st);
+  else dev_sgetrf(M, N, (float *)A, lda, ipiv, info, st);
+}
+template <typename T>
+void dev_getrs_any(int order, int trans, int N, int NRHS, const T *A, int lda, const int *ipiv, T *B, int ldb,
+                   cudaStream_t st) {
+  if (sizeof(T) == 8) dev_dgetrs(order, trans, N, NRHS, (const double *)A, lda, ipiv, (double *)B, ldb, st);
+  else dev_sgetrs(order, trans, N, NRHS, (const float *)A, lda, ipiv, (float *)B, ldb, st);
+}
+
+// getrf on host data; the factor stays on the device (kBufA, ld *ldd) for gesv.
+template <typename T>
+int host_getrf_keep(int Order, int M, int N, T *A, int lda, int *ipiv, T **dA_out, int *ldd_out, int **dpiv_out) {
+  cudaStream_t st = ctx().stream;
+  // RowMajor M x N is the column-major N x M matrix; ATL_getrfR is the
+  // column-pivoted LU of it, i.e. the row-pivoted LU of the transpose.
+  const int rows = (Order == CblasColMajor) ? M : N, cols = (Order == CblasColMajor) ? N : M;
+  const int MN = M < N ? M : N;
+  int ldd;
+  T *dA = to_dev<T>(kBufA, A, rows, cols, lda, &ldd, st);
+  int *dpiv = static_cast<int *>(ctx().buffer(kBufPiv, sizeof(int) * (size_t)(MN > 0 ? MN : 1)));
+  int *dinfo = static_cast<int *>(ctx().buffer(kBufInfo, sizeof(int) * 4));
+  dev_getrf_any<T>(rows, cols, dA, ldd, dpiv, dinfo, st);
+  int info = 0;
+  to_host<T>(A, lda, dA, ldd, rows, cols, st);
+  if (MN > 0) ATLG_CHECK(cudaMemcpyAsync(ipiv, dpiv, sizeof(int) * MN, cudaMemcpyDeviceToHost, st));
+  ATLG_CHECK(cudaMemcpyAsync(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  if (dA_out) *dA_out = dA;
+  if (ldd_out) *ldd_out = ldd;
+  if (dpiv_out) *dpiv_out = dpiv;
+  return info;
+}
+
+template <typename T>
+int host_getrf(const char *rout, int Order, int M, int N, T *A, int lda, int *ipiv) {
+  if (Order != CblasRowMajor && Order != CblasColMajor)
+    cblas_xerbla(1, rout, "Order must be %d or %d, but is set to %d\n", CblasRowMajor, CblasColMajor, Order);
+  if (M < 0) cblas_xerbla(2, rout, "M cannot be less than zero 0,; is set to %d.\n", M);
+  if (N < 0) cblas_xerbla(3, rout, "N cannot be less than zero 0,; is set to %d.\n", N);
+  if (Order == CblasColMajor) {
+    if (lda < M || lda < 1) cblas_xerbla(6, rout, "lda must be >= MAX(M,1): lda=%d M=%d\n", lda, M);
+  } else {
+    if (lda < N || lda < 1) cblas_xerbla(6, rout, "lda must be >= MAX(N,1): lda=%d N=%d\n", lda, N);
+  }
+  if (M == 0 || N == 0) return 0;
+  const int info = host_getrf_keep<T>(Order, M, N, A, lda, ipiv, nullptr, nullptr, nullptr);
+  check_status(rout);
+  return info;
+}
+
+template <typename T>
+int host_getrs(const char *rout, int Order, int Trans, int N, int NRHS, const T *A, int lda, const int *ipiv, T *B,
+               int ldb) {
+  if (Order != CblasRowMajor && Order != CblasColMajor)
+    cblas_xerbla(1, rout, "Order must be %d or %d, but is set to %d\n", CblasRowMajor, CblasColMajor, Order);
+  if (Trans != CblasNoTrans && Trans != CblasTrans && Trans != CblasConjTrans)
+    cblas_xerbla(2, rout, "Trans must be %d, %d, or %d, but is set to %d\n", CblasNoTrans, CblasTrans,
+                 CblasConjTrans, Trans);
+  if (N < 0) cblas_xerbla(3, rout, "N cannot be less than zero 0,; is set to %d.\n", N);
+  if (NRHS < 0) cblas_xerbla(4, rout, "NRHS cannot be less than zero 0,; is set to %d.\n", NRHS);
+  if (lda < N || lda < 1) cblas_xerbla(6, rout, "lda must be >= MAX(N,1): lda=%d N=%d\n", lda, N);
+  if (ldb < N || ldb < 1) cblas_xerbla(9, rout, "ldb must be >= MAX(N,1): lda=%d N=%d\n", lda, N);
+  if (N == 0 || NRHS == 0) return 0;
+  cudaStream_t st = ctx().stream;
+  int ldd_a, ldd_b;
+  const T *dA = to_dev<T>(kBufA, A, N, N, lda, &ldd_a, st);
+  int *dpiv = static_cast<int *>(ctx().buffer(kBufPiv, sizeof(int) * (size_t)N));
+  ATLG_CHECK(cudaMemcpyAsync(dpiv, ipiv, sizeof(int) * N, cudaMemcpyHostToDevice, st));
+  T *dB = to_dev<T>(kBufB, B, N, NRHS, ldb, &ldd_b, st);
+  dev_getrs_any<T>(Order, Trans, N, NRHS, dA, ldd_a, dpiv, dB, ldd_b, st);
+  to_host<T>(B, ldb, dB, ldd_b, N, NRHS, st);
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  check_status(rout);
+  return 0;
+}
+
+template <typename T>
+int host_gesv(const char *rout, int Order, int N, int NRHS, T *A, int lda, int *ipiv, T *B, int ldb) {
+  if (Order != CblasRowMajor && Order != CblasColMajor)
+    cblas_xerbla(1, rout, "Order must be %d or %d, but is set to %d.\n", CblasRowMajor, CblasColMajor, Order);
+  if (N < 0) cblas_xerbla(2, rout, "N cannot be less than zero 0,; is set to %d.\n", N);
+  if (NRHS < 0) cblas_xerbla(3, rout, "NRHS cannot be less than zero 0,; is set to %d.\n", NRHS);
+  if (lda < N || lda < 1) cblas_xerbla(5, rout, "lda must be >= MAX(N,1): lda=%d N=%d\n", lda, N);
+  if (ldb < N || ldb < 1) cblas_xerbla(8, rout, "ldb must be >= MAX(N,1): ldb=%d N=%d\n", ldb, N);
+  if (N == 0) return 0;
+  T *dA;
+  int ldd_a;
+  int *dpiv;
+  const int info = host_getrf_keep<T>(Order, N, N, A, lda, ipiv, &dA, &ldd_a, &dpiv);
+  if (info == 0 && NRHS > 0) {
+    cudaStream_t st = ctx().stream;
+    int ldd_b;
+    T *dB = to_dev<T>(kBufB, B, N, NRHS, ldb, &ldd_b, st);
+    dev_getrs_any<T>(Order, CblasNoTrans, N, NRHS, dA, ldd_a, dpiv, dB, ldd_b, st);
+    to_host<T>(B, ldb, dB, ldd_b, N, NRHS, st);
+    ATLG_CHECK(cudaStreamSynchronize(st));
+  }
+  check_status(rout);
+  return info;
+}
+
+}  // namespace
+
+// ============================================================== C ABI: host
+extern "C" {
+
+void cblas_dgemm(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TA, const enum CBLAS_TRANSPOSE TB,
+                 const int M, const int N, const int K, const double alpha, const double *A, const int lda,
+                 const double *B, const int ldb, const double beta, double *C, const int ldc) {
+  host_gemm<double>("cblas_dgemm", Order, TA, TB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+
+void cblas_sgemm(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TA, const enum CBLAS_TRANSPOSE TB,
+                 const int M, const int N, const int K, const float alpha, const float *A, const int lda,
+                 const float *B, const int ldb, const float beta, float *C, const int ldc) {
+  host_gemm<float>("cblas_sgemm", Order, TA, TB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+
+void cblas_dtrsm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side, const enum CBLAS_UPLO Uplo,
+                 const enum CBLAS_TRANSPOSE TA, const enum CBLAS_DIAG Diag, const int M, const int N,
+                 const double alpha, const double *A, const int lda, double *B, const int ldb) {
+  host_trsm<double>("cblas_dtrsm", Order, Side, Uplo, TA, Diag, M, N, alpha, A, lda, B, ldb);
+}
+
+void cblas_strsm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side, const enum CBLAS_UPLO Uplo,
+                 const enum CBLAS_TRANSPOSE TA, const enum CBLAS_DIAG Diag, const int M, const int N,
+                 const float alpha, const float *A, const int lda, float *B, const int ldb) {
+  host_trsm<float>("cblas_strsm", Order, Side, Uplo, TA, Diag, M, N, alpha, A, lda, B, ldb);
+}
+
+int clapack_dgetrf(const enum CBLAS_ORDER Order, const int M, const int N, double *A, const int lda, int *ipiv) {
+  return host_getrf<double>("clapack_dgetrf", Order, M, N, A, lda, ipiv);
+}
+int clapack_sgetrf(const enum CBLAS_ORDER Order, const int M, const int N, float *A, const int lda, int *ipiv) {
+  return host_getrf<float>("clapack_sgetrf", Order, M, N, A, lda, ipiv);
+}
+int clapack_dgetrs(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE Trans, const int N, const int NRHS,
+                   const double *A, const int lda, const int *ipiv, double *B, const int ldb) {
+  return host_getrs<double>("clapack_dgetrs", Order, Trans, N, NRHS, A, lda, ipiv, B, ldb);
+}
+int clapack_sgetrs(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE Trans, const int N, const int NRHS,
+                   const float *A, const int lda, const int *ipiv, float *B, const int ldb) {
+  return host_getrs<float>("clapack_sgetrs", Order, Trans, N, NRHS, A, lda, ipiv, B, ldb);
+}
+int clapack_dgesv(const enum CBLAS_ORDER Order, const int N, const int NRHS, double *A, const int lda, int *ipiv,
+                  double *B, const int ldb) {
+  return host_gesv<double>("clapack_dgesv", Order, N, NRHS, A, lda, ipiv, B, ldb);
+}
+int clapack_sgesv(const enum CBLAS_ORDER Order, const int N, const int NRHS, float *A, const int lda, int *ipiv,
+                  float *B, const int ldb) {
+  return host_gesv<float>("clapack_sgesv", Order, N, NRHS, A, lda, ipiv, B, ldb);
+}
+
+// ============================================================ C ABI: device
+int atlg_num_sms(void) { return ctx().num_sms; }
+
+void *atlg_stream(void) { return ctx().stream; }
+
+unsigned atlg_status(void) { return gemm_status_read_and_clear() | lu_status_read_and_clear(); }
+
+int atlg_dgemm_dev(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda, const double *B,
+                   int ldb, double beta, double *C, int ldc, void *stream) {
+  if (M < 0 || N < 0 || K < 0) return -1;
+  dev_dgemm(TA, TB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, stream_of(stream));
+  return 0;
+}
+int atlg_dgemm_dev_opts(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda,
+                        const double *B, int ldb, double beta, double *C, int ldc, int allow_tma, void *stream) {
+  if (M < 0 || N < 0 || K < 0) return -1;
+  GemmOpts o;
+  o.allow_tma = allow_tma != 0;
+  dev_dgemm(TA, TB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, stream_of(stream), o);
+  return 0;
+}
+int atlg_sgemm_dev(int TA, int TB, int M, int N, int K, float alpha, const float *A, int lda, const float *B,
+                   int ldb, float beta, float *C, int ldc, void *stream) {
+  if (M < 0 || N < 0 || K < 0) return -1;
+  dev_sgemm(TA, TB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, stream_of(stream));
+  return 0;
+}
+int atlg_dtrsm_dev(int Side, int Uplo, int TA, int Diag, int M, int N, double alpha, const double *A, int lda,
+                   double *B, int ldb, void *stream) {
+  if (M < 0 || N < 0) return -1;
+  dev_dtrsm(Side, Uplo, TA, Diag, M, N, alpha, A, lda, B, ldb, stream_of(stream));
+  return 0;
+}
+int atlg_dlaswp_dev(int N, double *A, int lda, int K1, int K2, const int *ipiv, int inci, int nrows, void *stream) {
+  dev_dlaswp(N, A, lda, K1, K2, ipiv, inci, nrows, stream_of(stream));
+  return 0;
+}
+int atlg_dgetrf_dev(int M, int N, double *A, int lda, int *ipiv, int *info, void *stream) {
+  if (M < 0 || N < 0 || lda < (M > 1 ? M : 1)) return -1;
+  dev_dgetrf(M, N, A, lda, ipiv, info, stream_of(stream));
+  return 0;
+}
+int atlg_sgetrf_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void *stream) {
+  if (M < 0 || N < 0 || lda < (M > 1 ? M : 1)) return -1;
+  dev_sgetrf(M, N, A, lda, ipiv, info, stream_of(stream));
+  return 0;
+}
+int atlg_dgetrs_dev(int Order, int Trans, int N, int NRHS, const double *A, int lda, const int *ipiv, double *B,
+                    int ldb, void *stream) {
+  if (N < 0 || NRHS < 0) return -1;
+  dev_dgetrs(Order, Trans, N, NRHS, A, lda, ipiv, B, ldb, stream_of(stream));
+  return 0;
+}
+
+}  // extern "C"

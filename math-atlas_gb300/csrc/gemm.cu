@@ -1,0 +1,307 @@
+// gemm.cu -- C = alpha*op(A)*op(B) + beta*C for FP64 (DGEMM) and FP32 (SGEMM)
+// on GB300, column-major, any op/shape/leading dimension.
+//
+// Replaces the reference's AMM GEMM stack: ATL_dammm recursion and shape
+// dispatch (AtlasBase/Clint/atlas-ammm.base:15624, 17707-17811), the
+// access-major copy/pack routines with alpha/beta (Students/trmm-micro-cpg.base:
+// 15-120, Clint/atlas-mmcpy.base) and the register-blocked ammkern_t kernels
+// (AtlasBase/kernel/ClintWhaley/*.S).
+//
+// GB300 design.  FP64 on GB300 runs on the CUDA-core DFMA pipe (measured
+// 1.19 TFLOP/s for DFMA against 1.05 TFLOP/s for FP64 mma.sync), so the FP64
+// kernel is a register-tiled DFMA kernel; the same template with FFMA serves
+// FP32.  Operand tiles are staged global -> shared by TMA tensor loads
+// (cp.async.bulk.tensor.2d, zero fill at the matrix edges) into a STAGES-deep
+// ring completed on mbarriers; a matrix TMA cannot address (base not 16-byte
+// aligned, leading dimension not a multiple of 16 bytes) takes a cp.async
+// zero-fill pipeline with the same shared-memory layout.  alpha/beta are
+// fused into the epilogue (beta == 0 never reads C).  The tile shape is picked
+// per call to balance the CTAs over the 152 SMs.
+#include "common.cuh"
+#include "gemm.cuh"
+
+namespace atlg {
+
+__device__ unsigned g_gemm_status;
+
+template <typename T, int BM, int BN, int BK, int TM, int TN, int NT, int STAGES, int TA, int TB,
+          bool USE_TMA>
+struct GemmKernel {
+  static constexpr int A_ELEMS = BM * BK;
+  static constexpr int B_ELEMS = BK * BN;
+  static constexpr int STAGE_ELEMS = A_ELEMS + B_ELEMS;
+  static constexpr int SMEM_BYTES = STAGES * STAGE_ELEMS * (int)sizeof(T) + 64;
+  static constexpr int GX = BM / TM;   // threads along m
+  static constexpr int GY = BN / TN;   // threads along n
+  static_assert(GX * GY == NT, "thread grid");
+  static_assert(A_ELEMS % NT == 0 && B_ELEMS % NT == 0, "loader split");
+};
+
+// op(A)(m,k) inside a stage:  TA==N -> [k][m],  TA==T -> [m][k]
+template <int TA, int BM, int BK>
+__device__ __forceinline__ int a_idx(int m, int k) {
+  return TA == kNoTrans ? k * BM + m : m * BK + k;
+}
+// op(B)(k,n) inside a stage:  TB==N -> [n][k],  TB==T -> [k][n]
+template <int TB, int BN, int BK>
+__device__ __forceinline__ int b_idx(int k, int n) {
+  return TB == kNoTrans ? n * BK + k : k * BN + n;
+}
+
+template <typename T, int BM, int BN, int BK, int TM, int TN, int NT, int STAGES, int TA, int TB,
+          bool USE_TMA>
+__global__ void __launch_bounds__(NT)
+    gemm_kernel(int M, int N, int K, T alpha, const T *__restrict__ A, int lda,
+                const T *__restrict__ B, int ldb, T beta, T *__restrict__ C, int ldc,
+                const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB) {
+  using KC = GemmKernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, USE_TMA>;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  T *smem = reinterpret_cast<T *>(smem_raw);
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + STAGES * KC::STAGE_ELEMS * sizeof(T));
+
+  const int tid = threadIdx.x;
+  const int m0 = blockIdx.x * BM;
+  const int n0 = blockIdx.y * BN;
+  const int KT = (K + BK - 1) / BK;
+  const int tx = tid % KC::GX, ty = tid / KC::GX;
+
+  T acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
+
+  auto stageA = [&](int s) { return smem + s * KC::STAGE_ELEMS; };
+  auto stageB = [&](int s) { return smem + s * KC::STAGE_ELEMS + KC::A_ELEMS; };
+
+  // ---- producers ----------------------------------------------------------
+  auto issue_tma = [&](int kt, int s) {
+    const unsigned bytes = KC::STAGE_ELEMS * sizeof(T);
+    mbar_arrive_expect_tx(&full[s], bytes);
+    const int k0 = kt * BK;
+    if (TA == kNoTrans) tma_load_2d(stageA(s), &tmA, &full[s], m0, k0);
+    else                tma_load_2d(stageA(s), &tmA, &full[s], k0, m0);
+    if (TB == kNoTrans) tma_load_2d(stageB(s), &tmB, &full[s], k0, n0);
+    else                tma_load_2d(stageB(s), &tmB, &full[s], n0, k0);
+  };
+  auto issue_cpasync = [&](int kt, int s) {
+    const int k0 = kt * BK;
+    T *sa = stageA(s), *sb = stageB(s);
+#pragma unroll
+    for (int e = tid; e < KC::A_ELEMS; e += NT) {
+      int m, k;
+      if (TA == kNoTrans) { m = e % BM; k = e / BM; } else { k = e % BK; m = e / BK; }
+      const int gm = m0 + m, gk = k0 + k;
+      const bool ok = gm < M && gk < K;
+      const T *src = ok ? (TA == kNoTrans ? A + gm + (size_t)gk * lda : A + gk + (size_t)gm * lda) : A;
+      if (sizeof(T) == 8) cp_async8(sa + e, src, ok); else cp_async4(sa + e, src, ok);
+    }
+#pragma unroll
+    for (int e = tid; e < KC::B_ELEMS; e += NT) {
+      int k, n;
+      if (TB == kNoTrans) { k = e % BK; n = e / BK; } else { n = e % BN; k = e / BN; }
+      const int gn = n0 + n, gk = k0 + k;
+      const bool ok = gn < N && gk < K;
+      const T *src = ok ? (TB == kNoTrans ? B + gk + (size_t)gn * ldb : B + gn + (size_t)gk * ldb) : B;
+      if (sizeof(T) == 8) cp_async8(sb + e, src, ok); else cp_async4(sb + e, src, ok);
+    }
+  };
+
+  if (USE_TMA) {
+    if (tid == 0) {
+      prefetch_tmap(&tmA);
+      prefetch_tmap(&tmB);
+      for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], 1);
+      fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0)
+      for (int s = 0; s < STAGES && s < KT; ++s) issue_tma(s, s);
+  } else {
+#pragma unroll
+    for (int s = 0; s < STAGES - 1; ++s) {
+      if (s < KT) issue_cpasync(s, s);
+      cp_async_commit();
+    }
+  }
+
+  bool failed = false;
+  for (int kt = 0; kt < KT; ++kt) {
+    const int s = kt % STAGES;
+    if (USE_TMA) {
+      if (!mbar_wait(&full[s], (kt / STAGES) & 1, &g_gemm_status)) { failed = true; break; }
+    } else {
+      cp_async_wait<STAGES - 2>();
+      __syncthreads();
+      const int nk = kt + STAGES - 1;
+      if (nk < KT) issue_cpasync(nk, nk % STAGES);
+      cp_async_commit();
+    }
+    const T *sa = stageA(s), *sb = stageB(s);
+#pragma unroll
+    for (int k = 0; k < BK; ++k) {
+      T a[TM], b[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) a[i] = sa[a_idx<TA, BM, BK>(tx + i * KC::GX, k)];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) b[j] = sb[b_idx<TB, BN, BK>(k, ty + j * KC::GY)];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    if (USE_TMA) {
+      __syncthreads();                       // every thread is done with stage s
+      if (tid == 0 && kt + STAGES < KT) issue_tma(kt + STAGES, s);
+    }
+  }
+  if (!USE_TMA) cp_async_wait<0>();
+  if (failed) return;
+
+  // ---- epilogue: C = alpha*acc + beta*C --------------------------------------
+#pragma unroll
+  for (int j = 0; j < TN; ++j) {
+    const int n = n0 + ty + j * KC::GY;
+    if (n >= N) continue;
+    T *c = C + (size_t)n * ldc;
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+      const int m = m0 + tx + i * KC::GX;
+      if (m >= M) continue;
+      const T v = alpha * acc[i][j];
+      c[m] = (beta == T(0)) ? v : fma(beta, c[m], v);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ host side
+template <typename T> struct DT;
+template <> struct DT<double> { static constexpr CUtensorMapDataType v = CU_TENSOR_MAP_DATA_TYPE_FLOAT64; };
+template <> struct DT<float>  { static constexpr CUtensorMapDataType v = CU_TENSOR_MAP_DATA_TYPE_FLOAT32; };
+
+template <typename T, int BM, int BN, int BK, int TM, int TN, int NT, int STAGES, int TA, int TB>
+static void launch_cfg(int M, int N, int K, T alpha, const T *A, int lda, const T *B, int ldb,
+                       T beta, T *C, int ldc, cudaStream_t st, bool allow_tma) {
+  dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN);
+  CUtensorMap tmA, tmB;
+  bool tma = allow_tma;
+  if (tma) {
+    // op(A) is M x K; stored TA==N as M x K (inner M), TA==T as K x M (inner K)
+    if (TA == kNoTrans) tma = encode_tmap_2d(&tmA, A, DT<T>::v, sizeof(T), M, K, lda, BM, BK);
+    else                tma = encode_tmap_2d(&tmA, A, DT<T>::v, sizeof(T), K, M, lda, BK, BM);
+  }
+  if (tma) {
+    if (TB == kNoTrans) tma = encode_tmap_2d(&tmB, B, DT<T>::v, sizeof(T), K, N, ldb, BK, BN);
+    else                tma = encode_tmap_2d(&tmB, B, DT<T>::v, sizeof(T), N, K, ldb, BN, BK);
+  }
+  if (tma) {
+    using KC = GemmKernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, true>;
+    auto k = gemm_kernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, true>;
+    ATLG_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, KC::SMEM_BYTES));
+    k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, tmA, tmB);
+  } else {
+    memset(&tmA, 0, sizeof(tmA));
+    memset(&tmB, 0, sizeof(tmB));
+    using KC = GemmKernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, false>;
+    auto k = gemm_kernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, false>;
+    ATLG_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, KC::SMEM_BYTES));
+    k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, tmA, tmB);
+  }
+  ATLG_CHECK(cudaGetLastError());
+}
+
+// Tile choice: the kernels are bound by the FP64 (or FP32) pipe, so the
+// makespan is ceil(tiles/SMs) * tile area; pick the shape that minimises it
+// (larger tile on ties).
+static int pick_dtile(int M, int N, int nsm) {
+  const int shapes[3][2] = {{64, 64}, {64, 32}, {32, 32}};
+  long best = -1;
+  int bi = 0;
+  for (int i = 0; i < 3; ++i) {
+    const long tiles = (long)((M + shapes[i][0] - 1) / shapes[i][0]) * ((N + shapes[i][1] - 1) / shapes[i][1]);
+    const long span = ((tiles + nsm - 1) / nsm) * shapes[i][0] * shapes[i][1];
+    if (best < 0 || span < best) { best = span; bi = i; }
+  }
+  return bi;
+}
+
+template <int TA, int TB>
+static void dgemm_t(int M, int N, int K, double alpha, const double *A, int lda, const double *B, int ldb,
+                    double beta, double *C, int ldc, cudaStream_t st, bool tma, int nsm) {
+  switch (pick_dtile(M, N, nsm)) {
+    case 0: launch_cfg<double, 64, 64, 16, 8, 4, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma); break;
+    case 1: launch_cfg<double, 64, 32, 16, 4, 4, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma); break;
+    default: launch_cfg<double, 32, 32, 16, 4, 2, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma); break;
+  }
+}
+
+template <int TA, int TB>
+static void sgemm_t(int M, int N, int K, float alpha, const float *A, int lda, const float *B, int ldb,
+                    float beta, float *C, int ldc, cudaStream_t st, bool tma) {
+  launch_cfg<float, 128, 128, 16, 8, 8, 256, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma);
+}
+
+__global__ void scale_kernel_d(int M, int N, double beta, double *C, int ldc) {
+  const size_t total = (size_t)M * N;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int m = (int)(e % M), n = (int)(e / M);
+    double *c = C + m + (size_t)n * ldc;
+    *c = (beta == 0.0) ? 0.0 : beta * *c;
+  }
+}
+__global__ void scale_kernel_s(int M, int N, float beta, float *C, int ldc) {
+  const size_t total = (size_t)M * N;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int m = (int)(e % M), n = (int)(e / M);
+    float *c = C + m + (size_t)n * ldc;
+    *c = (beta == 0.0f) ? 0.0f : beta * *c;
+  }
+}
+
+void dev_gescal(int M, int N, double beta, double *C, int ldc, cudaStream_t st) {
+  if (M <= 0 || N <= 0 || beta == 1.0) return;
+  const size_t total = (size_t)M * N;
+  const int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
+  scale_kernel_d<<<blocks, 256, 0, st>>>(M, N, beta, C, ldc);
+  ATLG_CHECK(cudaGetLastError());
+}
+void dev_gescal(int M, int N, float beta, float *C, int ldc, cudaStream_t st) {
+  if (M <= 0 || N <= 0 || beta == 1.0f) return;
+  const size_t total = (size_t)M * N;
+  const int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
+  scale_kernel_s<<<blocks, 256, 0, st>>>(M, N, beta, C, ldc);
+  ATLG_CHECK(cudaGetLastError());
+}
+
+// ATL_gemm semantics: alpha==0 or K==0 -> C = beta*C (gescal / gezero).
+void dev_dgemm(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda, const double *B,
+               int ldb, double beta, double *C, int ldc, cudaStream_t st, const GemmOpts &o) {
+  if (M <= 0 || N <= 0) return;
+  if (alpha == 0.0 || K <= 0) { dev_gescal(M, N, beta, C, ldc, st); return; }
+  const bool ta = TA != kNoTrans, tb = TB != kNoTrans;
+  const int nsm = o.num_sms > 0 ? o.num_sms : kNumSMs;
+  if (!ta && !tb) dgemm_t<kNoTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm);
+  else if (!ta && tb) dgemm_t<kNoTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm);
+  else if (ta && !tb) dgemm_t<kTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm);
+  else dgemm_t<kTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm);
+}
+
+void dev_sgemm(int TA, int TB, int M, int N, int K, float alpha, const float *A, int lda, const float *B,
+               int ldb, float beta, float *C, int ldc, cudaStream_t st, const GemmOpts &o) {
+  if (M <= 0 || N <= 0) return;
+  if (alpha == 0.0f || K <= 0) { dev_gescal(M, N, beta, C, ldc, st); return; }
+  const bool ta = TA != kNoTrans, tb = TB != kNoTrans;
+  if (!ta && !tb) sgemm_t<kNoTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma);
+  else if (!ta && tb) sgemm_t<kNoTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma);
+  else if (ta && !tb) sgemm_t<kTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma);
+  else sgemm_t<kTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma);
+}
+
+unsigned gemm_status_read_and_clear() {
+  unsigned v = 0, z = 0;
+  ATLG_CHECK(cudaMemcpyFromSymbol(&v, g_gemm_status, sizeof(v)));
+  if (v) ATLG_CHECK(cudaMemcpyToSymbol(g_gemm_status, &z, sizeof(z)));
+  return v;
+}
+
+}  // namespace atlg

@@ -1,0 +1,24 @@
+// gemm.cuh -- device-pointer GEMM entry points used by the C ABI and by the
+// LU / TRSM / refinement drivers.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace atlg {
+
+struct GemmOpts {
+  bool allow_tma = true;   // false forces the cp.async loader (tests cover both)
+  int num_sms = 0;         // 0: the device's SM count
+};
+
+// Column-major C = alpha*op(A)*op(B) + beta*C, all pointers on the device.
+void dev_dgemm(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda,
+               const double *B, int ldb, double beta, double *C, int ldc, cudaStream_t st,
+               const GemmOpts &o = GemmOpts());
+void dev_sgemm(int TA, int TB, int M, int N, int K, float alpha, const float *A, int lda,
+               const float *B, int ldb, float beta, float *C, int ldc, cudaStream_t st,
+               const GemmOpts &o = GemmOpts());
+void dev_gescal(int M, int N, double beta, double *C, int ldc, cudaStream_t st);
+void dev_gescal(int M, int N, float beta, float *C, int ldc, cudaStream_t st);
+unsigned gemm_status_read_and_clear();
+
+}  // namespace atlg

@@ -1,0 +1,479 @@
+// lu.cu -- LU factorization with partial pivoting (getrf), row interchanges
+// (laswp) and the solve with the factors (getrs), FP64 and FP32, on GB300.
+//
+// Reference path replaced: ATL_getrfC / ATL_getrfR, the recursive LU
+// (AtlasBase/Clint/atlas-lp.base:1210-1617) with its base cases LU2 / getf2
+// (:1301-1391, :5204-5360), ATL_laswp (:1053-1166) and ATL_getrs (:1631-1717);
+// the pivot search is cblas_iamax (AtlasBase/Clint/atlas-lvl1.base:1148).
+//
+// GB300 design: right-looking blocked LU, panel width NB=64.  Per panel:
+//  1. panel_kernel: one cooperative grid (one CTA per SM, bounded grid
+//     barrier) factors the (M-k) x NB panel column by column.  Each CTA owns
+//     a contiguous slice of rows.  For column j every CTA finds its local
+//     first-max |a|, stages that candidate row and (owner of row j) row j in
+//     global scratch, one grid barrier, then every CTA picks the same global
+//     winner (largest |a|, lowest row on ties -- the iamax rule), swaps the
+//     two rows and eliminates in its own rows.  One barrier per column.  The
+//     pivot is applied as a reciprocal when |pivot| > SAFMIN and by division
+//     otherwise, as the reference does.  CTA 0 also reduces the panel's NB
+//     interchanges to a row permutation (at most 2*NB rows move).
+//  2. apply_perm: the permutation is applied to every column outside the
+//     panel as a gather (all source rows read, then all destination rows
+//     written) instead of NB dependent swaps -- the laswp of the reference.
+//  3. U12 = L11^-1 A12 (warp-per-column unit-lower solve, trsm.cu).
+//  4. A22 -= L21 * U12 on the DFMA GEMM (gemm.cu).
+// Pivots are bit-identical to the reference whenever no two candidates of a
+// pivot search are within rounding of each other; the factors agree to
+// rounding (different but equally stable summation order).
+#include <float.h>
+#include <vector>
+
+#include "common.cuh"
+#include "context.cuh"
+#include "gemm.cuh"
+#include "lu.cuh"
+#include "trsm.cuh"
+
+namespace atlg {
+
+__device__ unsigned g_lu_status;
+
+constexpr int NB = 64;          // panel width
+constexpr int PT = 256;         // threads per panel CTA
+
+template <typename T> struct Lim;
+template <> struct Lim<double> { __device__ static double safmin() { return DBL_MIN; } };
+template <> struct Lim<float>  { __device__ static float safmin() { return FLT_MIN; } };
+
+template <typename T>
+struct BlockArgmax {
+  T v[PT / 32];
+  int i[PT / 32];
+};
+
+// first-max reduction over the block: (val, idx) with larger val winning,
+// lower idx winning ties; val < 0 marks "no candidate".
+template <typename T>
+__device__ void block_argmax(T &val, int &idx, BlockArgmax<T> &sh) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const T ov = __shfl_down_sync(0xffffffffu, val, o);
+    const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+    if (ov > val || (ov == val && oi < idx && ov >= T(0))) { val = ov; idx = oi; }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) { sh.v[w] = val; sh.i[w] = idx; }
+  __syncthreads();
+  if (w == 0) {
+    val = lane < PT / 32 ? sh.v[lane] : T(-1);
+    idx = lane < PT / 32 ? sh.i[lane] : 0x7fffffff;
+    for (int o = 16; o > 0; o >>= 1) {
+      const T ov = __shfl_down_sync(0xffffffffu, val, o);
+      const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+      if (ov > val || (ov == val && oi < idx && ov >= T(0))) { val = ov; idx = oi; }
+    }
+  }
+  __syncthreads();
+}
+
+// Local candidate for column j among own rows [max(r0,j), r1); stage it.
+template <typename T>
+__device__ void stage_candidate(const T *A, int lda, int j, int jb, int r0, int r1, int par, int G, T *cval,
+                                int *cidx, T *crow, T *jrow, BlockArgmax<T> &sh, int *s_idx) {
+  T best = T(-1);
+  int bi = 0x7fffffff;
+  const int lo = r0 > j ? r0 : j;
+  for (int i = lo + threadIdx.x; i < r1; i += PT) {      // ascending rows per thread
+    T a = A[i + (size_t)j * lda];
+    a = a < T(0) ? -a : a;
+    if (a > best) { best = a; bi = i; }
+  }
+  block_argmax(best, bi, sh);
+  if (threadIdx.x == 0) {
+    cval[par * G + blockIdx.x] = best;
+    cidx[par * G + blockIdx.x] = best >= T(0) ? bi : -1;
+    *s_idx = best >= T(0) ? bi : -1;
+  }
+  __syncthreads();
+  const int ci = *s_idx;
+  if (ci >= 0)
+    for (int c = threadIdx.x; c < jb; c += PT) crow[((size_t)par * G + blockIdx.x) * NB + c] = A[ci + (size_t)c * lda];
+  if (j >= r0 && j < r1)
+    for (int c = threadIdx.x; c < jb; c += PT) jrow[par * NB + c] = A[j + (size_t)c * lda];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PT)
+    panel_kernel(T *A, int lda, int M, int jb, int koff, int *ipiv, int *info, T *cval, int *cidx, T *crow,
+                 T *jrow, unsigned *bar, int *perm) {
+  __shared__ BlockArgmax<T> sh;
+  __shared__ T P[NB], J[NB];
+  __shared__ T lbuf[2048];
+  __shared__ int s_idx, s_p, s_zero;
+  __shared__ T s_piv;
+  __shared__ int piv_local[NB];
+
+  const int G = gridDim.x;
+  const int chunk = (M + G - 1) / G;
+  const int r0 = blockIdx.x * chunk;
+  const int r1 = (r0 + chunk < M) ? r0 + chunk : M;
+  const bool big = (r1 - r0) > 2048;
+
+  stage_candidate(A, lda, 0, jb, r0, r1, 0, G, cval, cidx, crow, jrow, sh, &s_idx);
+  for (int j = 0; j < jb; ++j) {
+    const int par = j & 1;
+    if (!grid_barrier(&bar[0], &bar[1], G, &g_lu_status)) return;
+    // ---- global winner (identical in every CTA) ----
+    if (threadIdx.x < 32) {
+      T best = T(-1);
+      int bb = 0x7fffffff;
+      for (int b = threadIdx.x; b < G; b += 32) {
+        const T v = cval[par * G + b];
+        if (v > best) { best = v; bb = b; }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const T ov = __shfl_down_sync(0xffffffffu, best, o);
+        const int ob = __shfl_down_sync(0xffffffffu, bb, o);
+        if (ov > best || (ov == best && ob < bb)) { best = ov; bb = ob; }
+      }
+      if (threadIdx.x == 0) {
+        const int p = (bb < G && best > T(0)) ? cidx[par * G + bb] : -1;
+        s_zero = (p < 0);
+        s_p = (p < 0) ? j : p;
+        s_piv = best;
+        s_idx = bb;
+      }
+    }
+    __syncthreads();
+    const int p = s_p;
+    const bool zero = s_zero != 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      ipiv[j] = koff + p;
+      piv_local[j] = p;
+      if (zero && *info == 0) *info = koff + j + 1;
+    }
+    if (!zero) {
+      const int wb = s_idx;
+      for (int c = threadIdx.x; c < jb; c += PT) {
+        P[c] = crow[((size_t)par * G + wb) * NB + c];
+        J[c] = jrow[par * NB + c];
+      }
+      __syncthreads();
+      const T pv = P[j];
+      const T apv = pv < T(0) ? -pv : pv;
+      const bool use_rcp = apv > Lim<T>::safmin();
+      const T rcp = T(1) / pv;
+      // pass 1: multipliers (column j) and the two swapped rows' L parts
+      const int lo = r0 > j ? r0 : j;
+      for (int i = lo + threadIdx.x; i < r1; i += PT) {
+        if (i == j) {
+          if (!big) lbuf[i - r0] = T(0);
+          continue;
+        }
+        const T src = (i == p) ? J[j] : A[i + (size_t)j * lda];
+        const T l = use_rcp ? src * rcp : src / pv;
+        A[i + (size_t)j * lda] = l;
+        if (!big) lbuf[i - r0] = l;
+      }
+      // row j <- pivot row (all columns); row p <- old row j in the L part
+      if (j >= r0 && j < r1)
+        for (int c = threadIdx.x; c < jb; c += PT)
+          A[j + (size_t)c * lda] = P[c];
+      if (p != j && p >= r0 && p < r1)
+        for (int c = threadIdx.x; c < j; c += PT) A[p + (size_t)c * lda] = J[c];
+      __syncthreads();
+      // pass 2: rank-1 update of columns j+1..jb-1 in own rows i > j
+      const int ncol = jb - j - 1;
+      const int nrow = r1 - lo;
+      if (ncol > 0 && nrow > 0) {
+        const long tot = (long)ncol * nrow;
+        for (long e = threadIdx.x; e < tot; e += PT) {
+          const int i = lo + (int)(e % nrow);
+          const int c = j + 1 + (int)(e / nrow);
+          if (i == j) continue;
+          const T l = big ? A[i + (size_t)j * lda] : lbuf[i - r0];
+          const T src = (i == p) ? J[c] : A[i + (size_t)c * lda];
+          A[i + (size_t)c * lda] = src - l * P[c];
+        }
+      }
+      __syncthreads();
+    }
+    if (j + 1 < jb)
+      stage_candidate(A, lda, j + 1, jb, r0, r1, (j + 1) & 1, G, cval, cidx, crow, jrow, sh, &s_idx);
+  }
+  // ---- CTA 0: reduce the NB interchanges to a permutation of rows ----
+  if (blockIdx.x == 0 && threadIdx.x < 32) {
+    __shared__ int rows[2 * NB], content[2 * NB];
+    __shared__ int cnt;
+    const int lane = threadIdx.x;
+    for (int t = lane; t < jb; t += 32) { rows[t] = t; content[t] = t; }
+    if (lane == 0) cnt = jb;
+    __syncwarp();
+    for (int j = 0; j < jb; ++j) {
+      const int p = piv_local[j];
+      int slot;
+      if (p < jb) {
+        slot = p;
+      } else {
+        const int n = cnt;
+        int found = -1;
+        for (int base = jb; base < n; base += 32) {
+          const int t = base + lane;
+          const unsigned m = __ballot_sync(0xffffffffu, t < n && rows[t] == p);
+          if (m) { found = base + __ffs(m) - 1; break; }
+        }
+        if (found < 0) {
+          found = n;
+          if (lane == 0) { rows[n] = p; content[n] = p; cnt = n + 1; }
+        }
+        slot = found;
+      }
+      __syncwarp();
+      if (lane == 0 && slot != j) {
+        const int t = content[j];
+        content[j] = content[slot];
+        content[slot] = t;
+      }
+      __syncwarp();
+    }
+    const int n = cnt;
+    for (int t = lane; t < n; t += 32) {
+      perm[1 + t] = rows[t];
+      perm[1 + 2 * NB + t] = content[t];
+    }
+    if (lane == 0) perm[0] = n;
+  }
+}
+
+// Apply a row permutation (perm: count, dst[], src[] relative to row k) to
+// the columns [0, c_split) and [c_from, N) of A: row k+dst[t] <- row k+src[t].
+template <typename T>
+__global__ void __launch_bounds__(256)
+    apply_perm_kernel(T *A, int lda, int k, const int *perm, int c_split, int c_from, int N) {
+  constexpr int CB = 32;
+  __shared__ T v[2 * NB][CB];
+  __shared__ int dst[2 * NB], src[2 * NB];
+  const int n = perm[0];
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    dst[t] = perm[1 + t];
+    src[t] = perm[1 + 2 * NB + t];
+  }
+  __syncthreads();
+  const int nleft_blocks = (c_split + CB - 1) / CB;
+  int c0;
+  if ((int)blockIdx.x < nleft_blocks) c0 = blockIdx.x * CB;
+  else c0 = c_from + (blockIdx.x - nleft_blocks) * CB;
+  const int cend = ((int)blockIdx.x < nleft_blocks) ? c_split : N;
+  const int ncols = (cend - c0 < CB) ? cend - c0 : CB;
+  if (ncols <= 0) return;
+  for (int e = threadIdx.x; e < n * ncols; e += blockDim.x) {
+    const int t = e % n, c = e / n;
+    v[t][c] = A[k + src[t] + (size_t)(c0 + c) * lda];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * ncols; e += blockDim.x) {
+    const int t = e % n, c = e / n;
+    if (dst[t] != src[t]) A[k + dst[t] + (size_t)(c0 + c) * lda] = v[t][c];
+  }
+}
+
+// laswp as one permutation: laswp_perm_kernel runs the interchange sequence
+// K1..K2-1 (reversed when inci < 0) on a row-content table held in shared
+// memory (global memory above kPermSmemRows rows), then the rows are moved
+// with one gather into scratch and one copy back.
+constexpr int kPermSmemRows = 48 * 1024;
+
+__global__ void laswp_perm_kernel(const int *ipiv, int K1, int K2, int inci, int *content_g, int nrows,
+                                  int use_smem) {
+  extern __shared__ int content_s[];
+  int *content = use_smem ? content_s : content_g;
+  for (int i = threadIdx.x; i < nrows; i += blockDim.x) content[i] = i;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int n = K2 - K1;
+    const int step = inci > 0 ? inci : -inci;
+    for (int s = 0; s < n; ++s) {
+      const int i = inci > 0 ? K1 + s : K2 - 1 - s;
+      const int ip = ipiv[(size_t)i * step];
+      if (ip == i || ip < 0 || ip >= nrows) continue;
+      const int t = content[i];
+      content[i] = content[ip];
+      content[ip] = t;
+    }
+  }
+  __syncthreads();
+  if (use_smem)
+    for (int i = threadIdx.x; i < nrows; i += blockDim.x) content_g[i] = content_s[i];
+}
+template <typename T>
+__global__ void gather_rows_kernel(const T *A, int lda, T *W, int ldw, const int *content, int nrows, int N) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < (long)nrows * N; e += (long)gridDim.x * blockDim.x) {
+    const int r = (int)(e % nrows), c = (int)(e / nrows);
+    W[r + (size_t)c * ldw] = A[content[r] + (size_t)c * lda];
+  }
+}
+template <typename T>
+__global__ void copy_rows_kernel(T *A, int lda, const T *W, int ldw, int nrows, int N) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < (long)nrows * N; e += (long)gridDim.x * blockDim.x) {
+    const int r = (int)(e % nrows), c = (int)(e / nrows);
+    A[r + (size_t)c * lda] = W[r + (size_t)c * ldw];
+  }
+}
+
+static int grid_for(long work) {
+  long b = (work + 255) / 256;
+  if (b > 8L * 152) b = 8L * 152;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+// The rows that can move are [0, nrows); nrows must exceed every pivot.
+template <typename T>
+static void laswp_impl(int N, T *A, int lda, int K1, int K2, const int *ipiv, int inci, int nrows,
+                       cudaStream_t st) {
+  if (K2 <= K1 || N <= 0 || nrows <= 0) return;
+  Context &c = ctx();
+  int *content = static_cast<int *>(c.buffer(kBufW3, sizeof(int) * (size_t)nrows));
+  T *W = static_cast<T *>(c.buffer(kBufW4, sizeof(T) * (size_t)nrows * N));
+  const int use_smem = nrows <= kPermSmemRows;
+  const size_t smem = use_smem ? sizeof(int) * (size_t)nrows : 0;
+  ATLG_CHECK(cudaFuncSetAttribute(laswp_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  laswp_perm_kernel<<<1, 1024, smem, st>>>(ipiv, K1, K2, inci, content, nrows, use_smem);
+  gather_rows_kernel<T><<<grid_for((long)nrows * N), 256, 0, st>>>(A, lda, W, nrows, content, nrows, N);
+  copy_rows_kernel<T><<<grid_for((long)nrows * N), 256, 0, st>>>(A, lda, W, nrows, nrows, N);
+  ATLG_CHECK(cudaGetLastError());
+}
+
+void dev_dlaswp(int N, double *A, int lda, int K1, int K2, const int *ipiv, int inci, int nrows, cudaStream_t st) {
+  laswp_impl<double>(N, A, lda, K1, K2, ipiv, inci, nrows, st);
+}
+void dev_slaswp(int N, float *A, int lda, int K1, int K2, const int *ipiv, int inci, int nrows, cudaStream_t st) {
+  laswp_impl<float>(N, A, lda, K1, K2, ipiv, inci, nrows, st);
+}
+
+// ------------------------------------------------------------------ getrf
+template <typename T>
+static void gemm_any(int M, int N, int K, const T *A, int lda, const T *B, int ldb, T *C, int ldc, cudaStream_t st);
+template <>
+void gemm_any<double>(int M, int N, int K, const double *A, int lda, const double *B, int ldb, double *C, int ldc,
+                      cudaStream_t st) {
+  dev_dgemm(kNoTrans, kNoTrans, M, N, K, -1.0, A, lda, B, ldb, 1.0, C, ldc, st);
+}
+template <>
+void gemm_any<float>(int M, int N, int K, const float *A, int lda, const float *B, int ldb, float *C, int ldc,
+                     cudaStream_t st) {
+  dev_sgemm(kNoTrans, kNoTrans, M, N, K, -1.0f, A, lda, B, ldb, 1.0f, C, ldc, st);
+}
+
+template <typename T>
+static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaStream_t st) {
+  ATLG_CHECK(cudaMemsetAsync(info, 0, sizeof(int), st));
+  if (M <= 0 || N <= 0) return;
+  Context &c = ctx();
+  const int MN = M < N ? M : N;
+  int G = c.num_sms;
+  // at least a few rows per CTA for the tallest panel
+  if (G > (M + 7) / 8) G = (M + 7) / 8;
+  if (G < 1) G = 1;
+  // one scratch block: cval[2G] T, crow[2G*NB] T, jrow[2NB] T, cidx[2G] int, bar[2], perm[1+4NB]
+  const size_t tbytes = sizeof(T) * ((size_t)2 * G + (size_t)2 * G * NB + 2 * NB);
+  const size_t ibytes = sizeof(int) * ((size_t)2 * G + 2 + 1 + 4 * NB);
+  unsigned char *scr = static_cast<unsigned char *>(c.buffer(kBufW0, tbytes + ibytes + 64));
+  T *cval = reinterpret_cast<T *>(scr);
+  T *crow = cval + 2 * G;
+  T *jrow = crow + (size_t)2 * G * NB;
+  int *cidx = reinterpret_cast<int *>(scr + ((tbytes + 15) & ~size_t(15)));
+  unsigned *bar = reinterpret_cast<unsigned *>(cidx + 2 * G);
+  int *perm = reinterpret_cast<int *>(bar + 2);
+  ATLG_CHECK(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st));
+
+  for (int k = 0; k < MN; k += NB) {
+    const int jb = (MN - k < NB) ? MN - k : NB;
+    T *Ap = A + k + (size_t)k * lda;
+    int Mp = M - k;
+    int *ipk = ipiv + k;
+    int koff = k;
+    void *args[] = {&Ap, (void *)&lda, &Mp, (void *)&jb, &koff, &ipk, &info, &cval, &cidx, &crow, &jrow, &bar, &perm};
+    ATLG_CHECK(cudaLaunchCooperativeKernel((const void *)panel_kernel<T>, dim3(G), dim3(PT), args, 0, st));
+    const int c_from = k + jb;
+    const int nl = (k + 31) / 32, nr = (N - c_from + 31) / 32;
+    if (nl + nr > 0) {
+      apply_perm_kernel<T><<<nl + nr, 256, 0, st>>>(A, lda, k, perm, k, c_from, N);
+      ATLG_CHECK(cudaGetLastError());
+    }
+    if (c_from < N) {
+      dev_trsm_llnu_block(A, lda, k, jb, A + k + (size_t)c_from * lda, lda, N - c_from, st);
+      if (k + jb < M)
+        gemm_any<T>(M - k - jb, N - c_from, jb, A + (k + jb) + (size_t)k * lda, lda, A + k + (size_t)c_from * lda,
+                    lda, A + (k + jb) + (size_t)c_from * lda, lda, st);
+    }
+  }
+}
+
+void dev_dgetrf(int M, int N, double *A, int lda, int *ipiv, int *info, cudaStream_t st) {
+  getrf_impl<double>(M, N, A, lda, ipiv, info, st);
+}
+void dev_sgetrf(int M, int N, float *A, int lda, int *ipiv, int *info, cudaStream_t st) {
+  getrf_impl<float>(M, N, A, lda, ipiv, info, st);
+}
+
+// ------------------------------------------------------------------ getrs
+template <typename T>
+static void trsm_any(int order, int side, int uplo, int ta, int diag, int M, int N, const T *A, int lda, T *B,
+                     int ldb, cudaStream_t st) {
+  // cblas order handling: RowMajor flips Side and Uplo and swaps M, N
+  if (order == kRowMajor) {
+    side = side == kLeft ? kRight : kLeft;
+    uplo = uplo == kUpper ? kLower : kUpper;
+    const int t = M; M = N; N = t;
+  }
+  if (sizeof(T) == 8)
+    dev_dtrsm(side, uplo, ta, diag, M, N, 1.0, (const double *)A, lda, (double *)B, ldb, st);
+  else
+    dev_strsm(side, uplo, ta, diag, M, N, 1.0f, (const float *)A, lda, (float *)B, ldb, st);
+}
+
+template <typename T>
+static void getrs_impl(int order, int trans, int N, int NRHS, const T *A, int lda, const int *ipiv, T *B, int ldb,
+                       cudaStream_t st) {
+  if (!N || !NRHS) return;
+  // laswp over the N "rows" of B in the column-major sense, as the reference calls it
+  if (order == kColMajor) {
+    if (trans == kNoTrans) {
+      laswp_impl<T>(NRHS, B, ldb, 0, N, ipiv, 1, N, st);
+      trsm_any<T>(order, kLeft, kLower, kNoTrans, kUnit, N, NRHS, A, lda, B, ldb, st);
+      trsm_any<T>(order, kLeft, kUpper, kNoTrans, kNonUnit, N, NRHS, A, lda, B, ldb, st);
+    } else {
+      trsm_any<T>(order, kLeft, kUpper, trans, kNonUnit, N, NRHS, A, lda, B, ldb, st);
+      trsm_any<T>(order, kLeft, kLower, trans, kUnit, N, NRHS, A, lda, B, ldb, st);
+      laswp_impl<T>(NRHS, B, ldb, 0, N, ipiv, -1, N, st);
+    }
+  } else {
+    if (trans == kNoTrans) {
+      trsm_any<T>(order, kRight, kLower, kTrans, kNonUnit, NRHS, N, A, lda, B, ldb, st);
+      trsm_any<T>(order, kRight, kUpper, kTrans, kUnit, NRHS, N, A, lda, B, ldb, st);
+      laswp_impl<T>(NRHS, B, ldb, 0, N, ipiv, -1, N, st);
+    } else {
+      laswp_impl<T>(NRHS, B, ldb, 0, N, ipiv, 1, N, st);
+      trsm_any<T>(order, kRight, kUpper, kNoTrans, kUnit, NRHS, N, A, lda, B, ldb, st);
+      trsm_any<T>(order, kRight, kLower, kNoTrans, kNonUnit, NRHS, N, A, lda, B, ldb, st);
+    }
+  }
+}
+
+void dev_dgetrs(int order, int trans, int N, int NRHS, const double *A, int lda, const int *ipiv, double *B, int ldb,
+                cudaStream_t st) {
+  getrs_impl<double>(order, trans, N, NRHS, A, lda, ipiv, B, ldb, st);
+}
+void dev_sgetrs(int order, int trans, int N, int NRHS, const float *A, int lda, const int *ipiv, float *B, int ldb,
+                cudaStream_t st) {
+  getrs_impl<float>(order, trans, N, NRHS, A, lda, ipiv, B, ldb, st);
+}
+
+unsigned lu_status_read_and_clear() {
+  unsigned v = 0, z = 0;
+  ATLG_CHECK(cudaMemcpyFromSymbol(&v, g_lu_status, sizeof(v)));
+  if (v) ATLG_CHECK(cudaMemcpyToSymbol(g_lu_status, &z, sizeof(z)));
+  return v;
+}
+
+}  // namespace atlg

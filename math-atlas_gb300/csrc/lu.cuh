@@ -1,0 +1,22 @@
+// lu.cuh -- device-pointer LU factorization, interchanges and solve.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace atlg {
+
+// Column-major LU with partial pivoting of the M x N matrix A (device).
+// ipiv (device, min(M,N) ints, 0-based, global row indices) and info
+// (device int: 0, or the 1-based index of the first exactly-zero pivot).
+void dev_dgetrf(int M, int N, double *A, int lda, int *ipiv, int *info, cudaStream_t st);
+void dev_sgetrf(int M, int N, float *A, int lda, int *ipiv, int *info, cudaStream_t st);
+// ATL_laswp semantics on device data; rows [0, nrows) may move (nrows > every pivot).
+void dev_dlaswp(int N, double *A, int lda, int K1, int K2, const int *ipiv, int inci, int nrows, cudaStream_t st);
+void dev_slaswp(int N, float *A, int lda, int K1, int K2, const int *ipiv, int inci, int nrows, cudaStream_t st);
+// ATL_getrs semantics (Order, Trans) on device data.
+void dev_dgetrs(int order, int trans, int N, int NRHS, const double *A, int lda, const int *ipiv, double *B, int ldb,
+                cudaStream_t st);
+void dev_sgetrs(int order, int trans, int N, int NRHS, const float *A, int lda, const int *ipiv, float *B, int ldb,
+                cudaStream_t st);
+unsigned lu_status_read_and_clear();
+
+}  // namespace atlg

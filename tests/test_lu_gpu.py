@@ -1,0 +1,141 @@
+"""LU path through the C ABI: clapack_dgetrf pivots bit-exact with the
+reference (fixtures from its own getrfC/getrfR) and with the oracle, the
+xdlutst residual (AtlasBase/Clint/atlas-tlp.base:1992-2058, threshold 100,
+:2203), zero-pivot info, getrs/gesv against the oracle (xdslvtst residual,
+threshold 100) and the full 8192 factorization."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+LU_THRESH = 100.0
+
+
+@pytest.mark.parametrize("order", ["C", "R"])
+def test_dgetrf_pivots_match_reference_fixtures(gb, ora, golden, order):
+    for (M, N, lda) in golden["lu_cases"]:
+        M, N, lda = int(M), int(N), int(lda)
+        key = f"lu{order}_{M}x{N}_{lda}"
+        rows, cols = (M, N) if order == "C" else (N, M)
+        ld = max(lda, rows)
+        A = ora.gegen(rows, cols, M * N + lda, lda=ld)
+        ipiv = np.zeros(max(min(M, N), 1), dtype=np.int32)
+        info = gb.clapack_dgetrf(102 if order == "C" else 101, M, N, A, ld, ipiv)
+        assert info == int(golden[key + "_info"]), key
+        assert np.array_equal(ipiv[: min(M, N)], golden[key + "_ipiv"]), key
+        if key + "_lu" in golden:
+            assert np.allclose(A[:rows, :cols], golden[key + "_lu"], rtol=0, atol=1e-11 * max(M, N)), key
+        if ld > rows:
+            assert (A[rows:, :] == -2.56e9).all()
+
+
+@pytest.mark.parametrize("M,N,lda", [(500, 500, 500), (1000, 1000, 1001), (1537, 700, 1540), (300, 900, 300),
+                                     (2048, 2048, 2048)])
+def test_dgetrf_matches_oracle_and_residual(gb, ora, M, N, lda):
+    seed = M * N + lda
+    A = ora.gegen(M, N, seed, lda=lda)
+    Ao = A.copy(order="F")
+    ipiv = np.zeros(min(M, N), dtype=np.int32)
+    info = gb.clapack_dgetrf(102, M, N, A, lda, ipiv)
+    oinfo, opiv = ora.getrf(Ao, M, N)
+    assert info == 0 and oinfo == 0
+    assert np.array_equal(ipiv, opiv)
+    r = ora.lu_resid(M, N, A, ipiv, seed)
+    assert r <= LU_THRESH, r
+    assert np.abs(A[:M] - Ao[:M]).max() < 1e-9
+
+
+def test_dgetrf_singular_info(gb, ora, golden):
+    for (n, zc) in ((8, 3), (50, 0), (64, 63), (100, 70)):
+        A = np.asfortranarray(golden[f"sing_{n}_{zc}_a"].copy())
+        ipiv = np.zeros(n, dtype=np.int32)
+        info = gb.clapack_dgetrf(102, n, n, A, n, ipiv)
+        assert info == int(golden[f"sing_{n}_{zc}_info"])
+        assert np.array_equal(ipiv, golden[f"sing_{n}_{zc}_ipiv"])
+
+
+def test_sgetrf_pivots(gb, ora, golden):
+    for (M, N, lda) in golden["lu_cases"]:
+        M, N, lda = int(M), int(N), int(lda)
+        A = ora.gegen(M, N, M * N + lda, lda=max(lda, M), dtype=np.float32)
+        ipiv = np.zeros(max(min(M, N), 1), dtype=np.int32)
+        info = gb.clapack_sgetrf(102, M, N, A, max(lda, M), ipiv)
+        assert info == int(golden[f"sluC_{M}x{N}_{lda}_info"])
+        assert np.array_equal(ipiv[: min(M, N)], golden[f"sluC_{M}x{N}_{lda}_ipiv"])
+
+
+@pytest.mark.parametrize("order", [102, 101])
+@pytest.mark.parametrize("trans", [111, 112])
+def test_dgetrs_matches_oracle(gb, ora, order, trans):
+    n, nrhs = 333, 7
+    A = ora.gegen(n, n, n * n + n)
+    ipiv = np.zeros(n, dtype=np.int32)
+    assert gb.clapack_dgetrf(order, n, n, A, n, ipiv) == 0
+    B0 = ora.gegen(n, nrhs, 99, lda=n + 3)
+    Bg = B0.copy(order="F")
+    gb.clapack_dgetrs(order, trans, n, nrhs, A, n, ipiv, Bg, n + 3)
+    Bo = B0.copy(order="F")
+    ora.lib().ora_dgetrs(order, trans, n, nrhs, A, n, ipiv, Bo, n + 3)
+    assert np.allclose(Bg[:n], Bo[:n], rtol=1e-9, atol=1e-9)
+
+
+def test_dgetrs_reference_fixtures(gb, ora, golden):
+    for n, nrhs in ((60, 3), (129, 5)):
+        A = ora.gegen(n, n, n * n + n)
+        ipiv = np.zeros(n, dtype=np.int32)
+        gb.clapack_dgetrf(102, n, n, A, n, ipiv)
+        for trans in (111, 112):
+            B = ora.gegen(n, nrhs, 77 + n)
+            gb.clapack_dgetrs(102, trans, n, nrhs, A, n, ipiv, B, n)
+            assert np.allclose(B, golden[f"getrs_{n}_{nrhs}_{trans}"], rtol=1e-10, atol=1e-10)
+
+
+def test_dgesv_slvtst_residual(gb, ora):
+    # xdslvtst: X known, B = A X, solve, ||X - Xc||_inf/(N eps ||A||_1 ||Xc||_inf) <= 100
+    n, nrhs = 1000, 3
+    A = ora.gegen(n, n, n * n + n)
+    X = ora.gegen(n, nrhs, 1234)
+    B = np.asfortranarray(A @ X)
+    A0 = A.copy(order="F")
+    ipiv = np.zeros(n, dtype=np.int32)
+    assert gb.clapack_dgesv(102, n, nrhs, A, n, ipiv, B, n) == 0
+    r = ora.lib().ora_dslv_resid(n, nrhs, A0, n, B, n, X, n)
+    assert r <= LU_THRESH, r
+
+
+def test_dgesv_singular_skips_solve(gb, ora):
+    n = 64
+    A = ora.gegen(n, n, 3)
+    A[:, 10] = 0.0
+    B = ora.gegen(n, 2, 4)
+    B0 = B.copy()
+    ipiv = np.zeros(n, dtype=np.int32)
+    assert gb.clapack_dgesv(102, n, 2, A, n, ipiv, B, n) == 11
+    assert np.array_equal(B, B0)
+
+
+def test_dgetrf_full_size_8192(gb, ora):
+    """The headline factorization: n=8192, xdlutst seed; pivots bit-exact with
+    the oracle and the residual (computed with torch fp64 on the GPU as a
+    checker) within the tester threshold."""
+    torch = pytest.importorskip("torch")
+    n = 8192
+    seed = n * n + n
+    A = ora.gegen(n, n, seed)
+    ipiv = np.zeros(n, dtype=np.int32)
+    info = gb.clapack_dgetrf(102, n, n, A, n, ipiv)
+    assert info == 0
+    ora.set_threads(0)
+    Ao = ora.gegen(n, n, seed)
+    oinfo, opiv = ora.getrf(Ao)
+    mism = np.nonzero(ipiv != opiv)[0]
+    assert mism.size == 0, f"pivot mismatch at columns {mism[:10]}"
+    LU = torch.from_numpy(np.ascontiguousarray(A.T)).cuda().T        # column-major view
+    L = torch.tril(LU, -1) + torch.eye(n, dtype=torch.float64, device="cuda")
+    U = torch.triu(LU)
+    A0 = ora.gegen(n, n, seed)
+    ora.laswp(n, A0, 0, n, ipiv, 1)
+    PA = torch.from_numpy(np.ascontiguousarray(A0.T)).cuda().T
+    D = PA - L @ U
+    normA = float(torch.from_numpy(np.ascontiguousarray(ora.gegen(n, n, seed).T)).abs().sum(dim=1).max())
+    resid = float(D.abs().sum(dim=0).max()) / (normA * np.finfo(float).eps * n)
+    assert resid <= LU_THRESH, resid

@@ -1,0 +1,109 @@
+"""The oracle against the fixtures generated from the reference's own
+routines (tests/golden/make_golden.py): generator and pivots bit-exact,
+factors and solutions to rounding."""
+import numpy as np
+import pytest
+
+
+def test_rand_streams_bit_exact(ora, golden):
+    for seed, stream in zip(golden["rand_seeds"], golden["rand_streams"]):
+        got = ora.rand_stream(int(seed), stream.shape[0])
+        assert np.array_equal(got, stream), seed
+
+
+def test_gegen_bit_exact_with_lda_gap(ora, golden):
+    A = ora.gegen(7, 3, 7 * 3 + 9, lda=9)
+    assert np.array_equal(A, golden["gegen_7x3_lda9"])
+    As = ora.gegen(7, 3, 7 * 3 + 9, lda=9, dtype=np.float32)
+    assert np.array_equal(As, golden["sgegen_7x3_lda9"])
+    assert (A[7:, :] == -2.56e9).all()
+
+
+@pytest.mark.parametrize("order", ["C", "R"])
+def test_getrf_pivots_match_reference(ora, golden, order):
+    for (M, N, lda) in golden["lu_cases"]:
+        M, N, lda = int(M), int(N), int(lda)
+        key = f"lu{order}_{M}x{N}_{lda}"
+        rows, cols = (M, N) if order == "C" else (N, M)
+        ld = max(lda, rows)
+        A = ora.gegen(rows, cols, M * N + lda, lda=ld)
+        info, ipiv = ora.getrf(A, M, N, order=ora.ColMajor if order == "C" else ora.RowMajor)
+        assert info == int(golden[key + "_info"])
+        assert np.array_equal(ipiv, golden[key + "_ipiv"]), key
+        if key + "_lu" in golden:
+            ref = golden[key + "_lu"]
+            assert np.allclose(A[:rows, :cols], ref, rtol=0, atol=1e-12 * max(1, M, N)), key
+
+
+def test_sgetrf_pivots_match_reference(ora, golden):
+    for (M, N, lda) in golden["lu_cases"]:
+        M, N, lda = int(M), int(N), int(lda)
+        A = ora.gegen(M, N, M * N + lda, lda=max(lda, M), dtype=np.float32)
+        info, ipiv = ora.getrf(A, M, N)
+        assert info == int(golden[f"sluC_{M}x{N}_{lda}_info"])
+        assert np.array_equal(ipiv, golden[f"sluC_{M}x{N}_{lda}_ipiv"])
+
+
+def test_singular_info_and_pivots(ora, golden):
+    for (n, zc) in ((8, 3), (50, 0), (64, 63), (100, 70)):
+        A = np.asfortranarray(golden[f"sing_{n}_{zc}_a"].copy())
+        info, ipiv = ora.getrf(A)
+        assert info == int(golden[f"sing_{n}_{zc}_info"]) and info > 0
+        assert np.array_equal(ipiv, golden[f"sing_{n}_{zc}_ipiv"])
+        assert np.allclose(A, golden[f"sing_{n}_{zc}_lu"], rtol=0, atol=1e-11)
+
+
+def test_laswp_bit_exact(ora, golden):
+    for (m, n, k1, k2) in ((40, 70, 0, 40), (100, 33, 5, 77), (64, 64, 0, 64)):
+        piv = golden[f"laswp_{m}_{n}_{k1}_{k2}_piv"]
+        for inci in (1, -1):
+            A = ora.gegen(m, n, m * n)
+            ora.laswp(n, A, k1, k2, piv, inci)
+            assert np.array_equal(A, golden[f"laswp_{m}_{n}_{k1}_{k2}_{inci}"])
+
+
+def test_getrs_matches_reference(ora, golden):
+    for n, nrhs in ((60, 3), (129, 5)):
+        A = ora.gegen(n, n, n * n + n)
+        info, ipiv = ora.getrf(A)
+        for trans in (ora.NoTrans, ora.Trans):
+            B = ora.gegen(n, nrhs, 77 + n)
+            ora.getrs(A, ipiv, B, trans=trans)
+            ref = golden[f"getrs_{n}_{nrhs}_{trans}"]
+            assert np.allclose(B, ref, rtol=1e-10, atol=1e-10)
+
+
+def test_gemm_matches_reference_blas(ora, golden):
+    for (ta, tb, M, N, K, al, be) in golden["gemm_cases"]:
+        ta, tb, M, N, K = int(ta), int(tb), int(M), int(N), int(K)
+        mA, nA = (M, K) if ta == 111 else (K, M)
+        mB, nB = (K, N) if tb == 111 else (N, K)
+        A = ora.gegen(mA, nA, mA * nA + 513 * 7 + 90)
+        B = ora.gegen(mB, nB, mB * nB + 127 * 50 + 77)
+        Cm = ora.gegen(M, N, M * N + 101 * 2 + 53)
+        ora.gemm(ta, tb, M, N, K, al, A, B, be, Cm)
+        ref = golden[f"gemm_{ta}_{tb}_{M}_{N}_{K}"]
+        assert np.abs(Cm - ref).max() <= 1e-13 * K * 4
+
+
+def test_trsm_matches_reference_blas(ora, golden):
+    for side in (ora.Left, ora.Right):
+        for uplo in (ora.Upper, ora.Lower):
+            for ta in (ora.NoTrans, ora.Trans):
+                for diag in (ora.NonUnit, ora.Unit):
+                    M, N = 45, 38
+                    na = M if side == ora.Left else N
+                    A = ora.gegen(na, na, na * na + 11)
+                    A += np.eye(na) * na
+                    B = ora.gegen(M, N, M * N + 3)
+                    ora.trsm(side, uplo, ta, diag, M, N, 1.5, A, B)
+                    ref = golden[f"trsm_{side}_{uplo}_{ta}_{diag}"]
+                    assert np.allclose(B, ref, rtol=1e-9, atol=1e-9), (side, uplo, ta, diag)
+
+
+def test_lu_residual_within_tester_threshold(ora):
+    # xdlutst: resid = ||PA-LU||_1/(||A||_1 eps min(M,N)) must be <= 100
+    for (M, N) in ((300, 300), (257, 128), (100, 333)):
+        A = ora.gegen(M, N, M * N + M)
+        info, ipiv = ora.getrf(A)
+        assert ora.lu_resid(M, N, A, ipiv, M * N + M) <= 100.0
