@@ -1,0 +1,322 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 Level-3 / LU path: FP64 dgesv (clapack_dgetrf +
+clapack_dgetrs, nrhs=1) at n=8192, the plain-FP64 configuration of the
+reference's LU tester (xdlutst seeds, uniform (-0.5, 0.5] from ATL_gegen).
+
+One JSON line on stdout (rank 0).  `value` is the device-resident throughput
+(matrix already in HBM, timed with CUDA events on the library stream);
+`e2e` is the same metric through the host-pointer C ABI (clapack_dgesv on
+pinned host arrays, host<->device copies inside the timed region).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+`--impl reference` times the CPU restatement of the reference's algorithm
+(oracle/, OpenMP over all host cores) on the same metric.  With --gpus N > 1
+(under torchrun) every rank runs an independent replica ("replicas only":
+the path has no data-path exchange) and the time is the max over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "math-atlas_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "dgesv/dgemm TFLOP/s on 1 GB300 at FP64 accuracy: mixed-prec vs plain FP64 form"
+UNIT = "TFLOP/s"
+
+
+def dgesv_flops(n, nrhs=1):
+    # xdlutst operation count (AtlasBase/Clint/atlas-tlp.base:2073) + getrs 2 n^2 nrhs
+    return n * n * n - n ** 3 / 3.0 - n * n / 2.0 + 2.0 * n * n * nrhs
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def traffic_from_profiles():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "dgemm_lu_trailing_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get("dram_bytes_per_launch")
+    except Exception:
+        return None
+
+
+# ------------------------------------------------------------------ CPU side
+def cpu_dgesv_seconds(O, n):
+    A = O.gegen(n, n, n * n + n)
+    b = O.gegen(n, 1, n + 1)
+    t0 = time.perf_counter()
+    info, ipiv = O.getrf(A)
+    O.getrs(A, ipiv, b)
+    return time.perf_counter() - t0
+
+
+def cpu_sample(O, budget_s):
+    """Largest n in (8192, 6144, 4096, 2048) whose dgesv fits `budget_s`,
+    estimated from an n=2048 probe (O(n^3))."""
+    t2k = cpu_dgesv_seconds(O, 2048)
+    for n in (8192, 6144, 4096, 2048):
+        if t2k * (n / 2048.0) ** 3 <= budget_s:
+            return n, t2k
+    return 2048, t2k
+
+
+def run_reference(args):
+    import oracle as O
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    threads = O.set_threads(0)
+    steps, warmup = args.steps, args.warmup
+    n, _ = cpu_sample(O, max(2.0, 150.0 / max(1, steps + warmup)))
+    for _ in range(warmup):
+        cpu_dgesv_seconds(O, n)
+    ts = [cpu_dgesv_seconds(O, n) for _ in range(steps)]
+    tot = sum(ts)
+    value = dgesv_flops(n) * steps / tot / 1e12
+    sample = f"dgesv n={n} nrhs=1 per step (full workload n=8192)"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": steps, "warmup": warmup, "ms_per_step": tot / steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (ATL_gegen seeds)",
+        "config": {"workload": "dgesv FP64 plain form, clapack_dgetrf + clapack_dgetrs, n=8192 nrhs=1",
+                   "sample_n": n, "parallelism": "replicas only"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ GPU side
+def run_gpu(args):
+    import torch
+    import atlas_gb300 as G
+    import oracle as O
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    n = args.n
+    nrhs = 1
+    L = G.lib()
+    st = L.atlg_stream()
+    stream = torch.cuda.ExternalStream(st)
+
+    # inputs: xdlutst seeds (gegen(n, n, n*n+lda)), b = gegen(n, 1, n+1)
+    A_h = O.gegen(n, n, n * n + n)
+    b_h = O.gegen(n, nrhs, n + 1)
+    A0 = torch.from_numpy(np.ascontiguousarray(A_h.T)).cuda()     # column-major storage
+    b0 = torch.from_numpy(np.ascontiguousarray(b_h.T)).cuda()
+    A = torch.empty_like(A0)
+    b = torch.empty_like(b0)
+    ipiv = torch.zeros(n, dtype=torch.int32, device="cuda")
+    info = torch.zeros(4, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+
+    def step():
+        with torch.cuda.stream(stream):
+            A.copy_(A0)
+            b.copy_(b0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        L.atlg_dgetrf_dev(n, n, A.data_ptr(), n, ipiv.data_ptr(), info.data_ptr(), st)
+        L.atlg_dgetrs_dev(102, 111, n, nrhs, A.data_ptr(), n, ipiv.data_ptr(), b.data_ptr(), n, st)
+        e1.record(stream)
+        return e0, e1
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    assert int(info[0]) == 0
+    # accuracy of the benchmarked solve (xdlutst-style residual on the device result)
+    x = b.cpu().numpy().reshape(-1)
+
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    launches0 = G.launch_count()
+    G.prof_enable(True)
+    G.prof_collect()
+    evs = [step() for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    G.prof_enable(False)
+    gemm_ms, gemm_flops, gemm_n = G.prof_collect()
+    launches = G.launch_count() - launches0
+    clk = clocks.stop()
+    if dist:
+        dist.barrier()
+    dev_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
+    t_ms = torch.tensor([dev_ms], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t_ms, op=dist.ReduceOp.MAX)
+    dev_ms = float(t_ms[0])
+    flops = dgesv_flops(n, nrhs)
+    value = world * flops * args.steps / (dev_ms * 1e-3) / 1e12
+
+    # ---- e2e through the host C ABI: clapack_dgesv on pinned host arrays ----
+    Ah = torch.empty((n, n), dtype=torch.float64).pin_memory()
+    bh = torch.empty((nrhs, n), dtype=torch.float64).pin_memory()
+    A_pin = Ah.numpy().T          # Fortran-ordered view, column-major n x n
+    b_pin = bh.numpy().T
+    piv_h = np.zeros(n, dtype=np.int32)
+    e2e_steps = max(1, min(args.steps, 5))
+    e2e_t = []
+    for it in range(e2e_steps + 1):
+        np.copyto(A_pin, A_h)
+        np.copyto(b_pin, b_h)
+        t0 = time.perf_counter()
+        rc = G.clapack_dgesv(102, n, nrhs, A_pin, n, piv_h, b_pin, n)
+        t1 = time.perf_counter()
+        assert rc == 0
+        if it > 0:
+            e2e_t.append(t1 - t0)
+    e2e_s = max(e2e_t) if world == 1 else max(e2e_t)
+    e2e_tensor = torch.tensor([sum(e2e_t) / len(e2e_t)], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(e2e_tensor, op=dist.ReduceOp.MAX)
+    e2e_val = world * flops / float(e2e_tensor[0]) / 1e12
+    del e2e_s
+
+    # ---- roofline of the dominant kernel (the trailing-update DGEMM) ----
+    p64, _ = G.probe_peaks()
+    gemm_tflops = gemm_flops / (gemm_ms * 1e-3) / 1e12 if gemm_ms > 0 else None
+    roofline = {
+        "bound": "tensor", "pipe": "FP64 FMA (CUDA-core DFMA; GB300 FP64 mma.sync is slower)",
+        "kernel": "gemm_kernel<double> (LU trailing update)",
+        "achieved": gemm_tflops, "peak": p64, "unit": "TFLOP/s",
+        "frac": (gemm_tflops / p64) if gemm_tflops else None,
+        "peak_source": "FP64 FMA-throughput probe run in this process (MEASURED_PEAKS.json has no FP64 entry)",
+        "traffic": traffic_from_profiles(),
+        "launches_per_step": gemm_n / args.steps, "share_of_step": gemm_ms / dev_ms,
+    }
+
+    if rank == 0:
+        # CPU baseline: the oracle (port of the reference's algorithm) on the host cores
+        cpu = None
+        if not args.skip_cpu:
+            threads = O.set_threads(0)
+            ncpu, _ = cpu_sample(O, 30.0)
+            tc = cpu_dgesv_seconds(O, ncpu)
+            cpu = {"value": dgesv_flops(ncpu) / tc / 1e12, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": f"one dgesv n={ncpu} nrhs=1 (oracle restatement of getrfC/getrs, OpenMP)"}
+        bwd = O.backward_error(np.asfortranarray(A_h), x, b_h.reshape(-1))
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: ATL_gegen uniform(-0.5,0.5], xdlutst seed n*n+lda",
+            "config": {"workload": "dgesv FP64 plain form: clapack_dgetrf + clapack_dgetrs, ColMajor, n=8192, nrhs=1",
+                       "n": n, "nrhs": nrhs, "parallelism": "replicas only" if world > 1 else "1 GPU",
+                       "l2": "inputs larger than L2 (A is 512 MiB); A and b restored by a device copy before "
+                             "each step, outside the event-timed region"},
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs,
+                    "d2h_bytes_per_step": 8 * n * n + 4 * n + 8 * n * nrhs + 4,
+                    "api": "clapack_dgesv on pinned host arrays", "steps": e2e_steps},
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "accuracy": {"backward_error": bwd, "n_eps": n * np.finfo(float).eps},
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=8192)
+    ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

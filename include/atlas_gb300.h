@@ -79,12 +79,37 @@ int clapack_dgesv(const enum CBLAS_ORDER Order, const int N, const int NRHS, dou
 int clapack_sgesv(const enum CBLAS_ORDER Order, const int N, const int NRHS, float *A,
                   const int lda, int *ipiv, float *B, const int ldb);
 
+/* ---- new methods (no reference counterpart: ATLAS has neither a
+ *      mixed-precision solver nor an adjoint).  Column-major. */
+/* FP32 LU + FP64 iterative refinement (LAPACK dsgesv stopping test), with an
+ * FP64-LU fallback.  A is unchanged unless the fallback ran (status 1; A then
+ * holds the FP64 factors); B is unchanged; X receives the solution; berr and
+ * ferr have NRHS entries (normwise backward error, last-correction forward
+ * error estimate); iters = refinement steps.  Returns 0 or i > 0 (zero pivot
+ * in the FP64 factor). */
+int dgesv_mixed(const int N, const int NRHS, double *A, const int lda, int *ipiv,
+                const double *B, const int ldb, double *X, const int ldx, double *berr,
+                double *ferr, int *iters, int *status);
+/* Adjoint of X = A^-1 B on the factors of clapack_dgetrf (ColMajor):
+ * gB = A^-T gX (transposed solve, as ATL_getrs Trans: AtlasBase/Clint/
+ * atlas-lp.base:1675-1682) and gA = -gB X^T (DGEMM). */
+int dgesv_adjoint(const int n, const int nrhs, const double *LU, const int lda,
+                  const int *ipiv, const double *X, const int ldx, const double *gX,
+                  const int ldgx, double *gA, const int ldga, double *gB, const int ldgb);
+
 /* ---- device-pointer variants (no reference counterpart: the reference has
  *      no device memory; these are the same operations on GPU-resident data,
  *      column-major, used by callers that keep matrices in HBM) */
 int      atlg_num_sms(void);
 void    *atlg_stream(void);
 unsigned atlg_status(void);   /* device wait-timeout flags since the last call, cleared */
+/* benchmark support: kernels launched by the library so far; GEMM launch
+ * timing with CUDA events (enable, then collect ms / flops / launches);
+ * FP64 and FP32 FMA-pipe throughput probes in TFLOP/s */
+unsigned long long atlg_launch_count(void);
+void atlg_prof_enable(int on);
+int  atlg_prof_collect(double *ms, double *flops, int *count);
+void atlg_probe_peaks(double *fp64_tflops, double *fp32_tflops);
 int atlg_dgemm_dev(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda,
                    const double *B, int ldb, double beta, double *C, int ldc, void *stream);
 int atlg_dgemm_dev_opts(int TA, int TB, int M, int N, int K, double alpha, const double *A,
@@ -102,6 +127,13 @@ int atlg_dgetrf_dev(int M, int N, double *A, int lda, int *ipiv, int *info, void
 int atlg_sgetrf_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void *stream);
 int atlg_dgetrs_dev(int Order, int Trans, int N, int NRHS, const double *A, int lda,
                     const int *ipiv, double *B, int ldb, void *stream);
+/* berr, ferr (NRHS entries), iters and status are host pointers; synchronizes */
+int atlg_dgesv_mixed_dev(int N, int NRHS, double *A, int lda, int *ipiv, const double *B,
+                         int ldb, double *X, int ldx, double *berr, double *ferr, int *iters,
+                         int *status, void *stream);
+int atlg_dgesv_adjoint_dev(int n, int nrhs, const double *LU, int lda, const int *ipiv,
+                           const double *X, int ldx, const double *gX, int ldgx, double *gA,
+                           int ldga, double *gB, int ldgb, void *stream);
 
 #ifdef __cplusplus
 }

@@ -26,7 +26,8 @@ EXPORTS = [
     "clapack_dgetrf", "clapack_sgetrf", "clapack_dgetrs", "clapack_sgetrs", "clapack_dgesv",
     "clapack_sgesv", "atlg_num_sms", "atlg_stream", "atlg_status", "atlg_dgemm_dev",
     "atlg_dgemm_dev_opts", "atlg_sgemm_dev", "atlg_dtrsm_dev", "atlg_dlaswp_dev", "atlg_dgetrf_dev",
-    "atlg_sgetrf_dev", "atlg_dgetrs_dev",
+    "atlg_sgetrf_dev", "atlg_dgetrs_dev", "atlg_launch_count", "atlg_prof_enable", "atlg_prof_collect",
+    "atlg_probe_peaks", "dgesv_mixed", "dgesv_adjoint", "atlg_dgesv_mixed_dev", "atlg_dgesv_adjoint_dev",
 ]
 
 _lib = None
@@ -75,6 +76,16 @@ def _declare(L):
         "atlg_dgetrf_dev": (_i, [_i, _i, _v, _i, _v, _v, _v]),
         "atlg_sgetrf_dev": (_i, [_i, _i, _v, _i, _v, _v, _v]),
         "atlg_dgetrs_dev": (_i, [_i, _i, _i, _i, _v, _i, _v, _v, _i, _v]),
+        "dgesv_mixed": (_i, [_i, _i, _dp, _i, _ip, _dp, _i, _dp, _i, np.ctypeslib.ndpointer(np.float64),
+                             np.ctypeslib.ndpointer(np.float64), C.POINTER(_i), C.POINTER(_i)]),
+        "dgesv_adjoint": (_i, [_i, _i, _dp, _i, _ip, _dp, _i, _dp, _i, _dp, _i, _dp, _i]),
+        "atlg_dgesv_mixed_dev": (_i, [_i, _i, _v, _i, _v, _v, _i, _v, _i, C.POINTER(_d), C.POINTER(_d),
+                                      C.POINTER(_i), C.POINTER(_i), _v]),
+        "atlg_dgesv_adjoint_dev": (_i, [_i, _i, _v, _i, _v, _v, _i, _v, _i, _v, _i, _v, _i, _v]),
+        "atlg_launch_count": (C.c_ulonglong, []),
+        "atlg_prof_enable": (None, [_i]),
+        "atlg_prof_collect": (_i, [C.POINTER(_d), C.POINTER(_d), C.POINTER(_i)]),
+        "atlg_probe_peaks": (None, [C.POINTER(_d), C.POINTER(_d)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -125,6 +136,25 @@ def clapack_sgesv(order, N, NRHS, A, lda, ipiv, B, ldb):
     return lib().clapack_sgesv(order, N, NRHS, A, lda, ipiv, B, ldb)
 
 
+def dgesv_mixed(A, ipiv, B, X):
+    """Mixed-precision solve on Fortran arrays; returns (info, berr, ferr, iters, status)."""
+    n, nrhs = B.shape
+    berr = np.zeros(max(nrhs, 1))
+    ferr = np.zeros(max(nrhs, 1))
+    it, stt = _i(), _i()
+    info = lib().dgesv_mixed(n, nrhs, A, A.shape[0], ipiv, B, B.shape[0], X, X.shape[0], berr, ferr,
+                             C.byref(it), C.byref(stt))
+    return info, berr[:nrhs], ferr[:nrhs], it.value, stt.value
+
+
+def dgesv_adjoint(LU, ipiv, X, gX):
+    n, nrhs = X.shape
+    gA = np.zeros((n, n), order="F")
+    gB = np.zeros((n, nrhs), order="F")
+    lib().dgesv_adjoint(n, nrhs, LU, LU.shape[0], ipiv, X, X.shape[0], gX, gX.shape[0], gA, n, gB, n)
+    return gA, gB
+
+
 # convenience wrappers on whole arrays (column-major)
 def dgemm(ta, tb, alpha, A, B, beta, Cm):
     M, N = Cm.shape
@@ -150,3 +180,23 @@ def status():
 
 def num_sms():
     return lib().atlg_num_sms()
+
+
+def launch_count():
+    return int(lib().atlg_launch_count())
+
+
+def prof_enable(on=True):
+    lib().atlg_prof_enable(1 if on else 0)
+
+
+def prof_collect():
+    ms, fl, n = _d(), _d(), _i()
+    lib().atlg_prof_collect(C.byref(ms), C.byref(fl), C.byref(n))
+    return ms.value, fl.value, n.value
+
+
+def probe_peaks():
+    a, b = _d(), _d()
+    lib().atlg_probe_peaks(C.byref(a), C.byref(b))
+    return a.value, b.value

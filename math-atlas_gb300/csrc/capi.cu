@@ -21,9 +21,15 @@
 #include "context.cuh"
 #include "gemm.cuh"
 #include "lu.cuh"
+#include "mixed.cuh"
 #include "trsm.cuh"
 
 using namespace atlg;
+
+namespace atlg {
+double probe_fp64_tflops();
+double probe_fp32_tflops();
+}
 
 // ------------------------------------------------------------ error reporting
 extern "C" int cblas_errprn(int ierr, int info, const char *form, ...) {
@@ -350,6 +356,30 @@ int host_gesv(const char *rout, int Order, int N, int NRHS, T *A, int lda, int *
   return info;
 }
 
+// ------------------------------------------------------------- new methods
+int mixed_dev(int N, int NRHS, double *A, int lda, int *ipiv, const double *B, int ldb, double *X, int ldx,
+              double *berr, double *ferr, int *iters, int *status, cudaStream_t st) {
+  MixedResult r;
+  const int info = dev_dgesv_mixed(N, NRHS, A, lda, ipiv, B, ldb, X, ldx, &r, st);
+  for (int j = 0; j < NRHS; ++j) {
+    if (berr) berr[j] = r.berr[j];
+    if (ferr) ferr[j] = r.ferr[j];
+  }
+  if (iters) *iters = r.iters;
+  if (status) *status = r.status;
+  return info;
+}
+
+void adjoint_dev(int n, int nrhs, const double *LU, int lda, const int *ipiv, const double *X, int ldx,
+                 const double *gX, int ldgx, double *gA, int ldga, double *gB, int ldgb, cudaStream_t st) {
+  // gB = A^{-T} gX via the transposed solve on the stored factors (ATL_getrs
+  // Trans: AtlasBase/Clint/atlas-lp.base:1675-1682), then gA = -gB X^T.
+  ATLG_CHECK(cudaMemcpy2DAsync(gB, sizeof(double) * ldgb, gX, sizeof(double) * ldgx, sizeof(double) * n, nrhs,
+                               cudaMemcpyDeviceToDevice, st));
+  dev_dgetrs(kColMajor, kTrans, n, nrhs, LU, lda, ipiv, gB, ldgb, st);
+  dev_dgemm(kNoTrans, kTrans, n, n, nrhs, -1.0, gB, ldgb, X, ldx, 0.0, gA, ldga, st);
+}
+
 }  // namespace
 
 // ============================================================== C ABI: host
@@ -402,12 +432,115 @@ int clapack_sgesv(const enum CBLAS_ORDER Order, const int N, const int NRHS, flo
   return host_gesv<float>("clapack_sgesv", Order, N, NRHS, A, lda, ipiv, B, ldb);
 }
 
+// Mixed-precision solve (no reference counterpart; see mixed.cu).  Column-
+// major.  A is unchanged unless the FP64 fallback ran (status 1: A then
+// holds the FP64 factors, as LAPACK dsgesv leaves them); B is unchanged; X
+// gets the solution; berr/ferr have NRHS entries.  Returns 0, a negative
+// argument index, or i > 0 when the FP64 factor has an exactly zero pivot.
+int dgesv_mixed(const int N, const int NRHS, double *A, const int lda, int *ipiv, const double *B, const int ldb,
+                double *X, const int ldx, double *berr, double *ferr, int *iters, int *status) {
+  const char *rout = "dgesv_mixed";
+  if (N < 0) cblas_xerbla(1, rout, "N cannot be less than zero 0,; is set to %d.\n", N);
+  if (NRHS < 0) cblas_xerbla(2, rout, "NRHS cannot be less than zero 0,; is set to %d.\n", NRHS);
+  if (lda < N || lda < 1) cblas_xerbla(4, rout, "lda must be >= MAX(N,1): lda=%d N=%d\n", lda, N);
+  if (ldb < N || ldb < 1) cblas_xerbla(7, rout, "ldb must be >= MAX(N,1): ldb=%d N=%d\n", ldb, N);
+  if (ldx < N || ldx < 1) cblas_xerbla(9, rout, "ldx must be >= MAX(N,1): ldx=%d N=%d\n", ldx, N);
+  if (iters) *iters = 0;
+  if (status) *status = 0;
+  if (N == 0 || NRHS == 0) return 0;
+  cudaStream_t st = ctx().stream;
+  int lda_d, ldb_d, ldx_d;
+  double *dA = to_dev<double>(kBufA, A, N, N, lda, &lda_d, st);
+  const double *dB = to_dev<double>(kBufB, B, N, NRHS, ldb, &ldb_d, st);
+  ldx_d = lda_d;
+  double *dX = static_cast<double *>(ctx().buffer(kBufC, sizeof(double) * (size_t)ldx_d * NRHS));
+  int *dpiv = static_cast<int *>(ctx().buffer(kBufPiv, sizeof(int) * (size_t)N));
+  int st_out = 0;
+  const int info = mixed_dev(N, NRHS, dA, lda_d, dpiv, dB, ldb_d, dX, ldx_d, berr, ferr, iters, &st_out, st);
+  if (status) *status = st_out;
+  to_host<double>(X, ldx, dX, ldx_d, N, NRHS, st);
+  if (st_out != 0) to_host<double>(A, lda, dA, lda_d, N, N, st);
+  ATLG_CHECK(cudaMemcpyAsync(ipiv, dpiv, sizeof(int) * N, cudaMemcpyDeviceToHost, st));
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  check_status(rout);
+  return info;
+}
+
+// Adjoint of X = A^{-1} B for an upstream gradient gX, on the stored
+// factors (LU, ipiv) of clapack_dgetrf: gB = A^{-T} gX, gA = -gB X^T.
+// No reference counterpart; the transposed solve is ATL_getrs Trans.
+int dgesv_adjoint(const int n, const int nrhs, const double *LU, const int lda, const int *ipiv, const double *X,
+                  const int ldx, const double *gX, const int ldgx, double *gA, const int ldga, double *gB,
+                  const int ldgb) {
+  const char *rout = "dgesv_adjoint";
+  if (n < 0) cblas_xerbla(1, rout, "N cannot be less than zero 0,; is set to %d.\n", n);
+  if (nrhs < 0) cblas_xerbla(2, rout, "NRHS cannot be less than zero 0,; is set to %d.\n", nrhs);
+  if (lda < n || lda < 1) cblas_xerbla(4, rout, "lda must be >= MAX(N,1): lda=%d N=%d\n", lda, n);
+  if (ldx < n || ldx < 1) cblas_xerbla(7, rout, "ldx must be >= MAX(N,1): ldx=%d N=%d\n", ldx, n);
+  if (ldgx < n || ldgx < 1) cblas_xerbla(9, rout, "ldgx must be >= MAX(N,1): ldgx=%d N=%d\n", ldgx, n);
+  if (ldga < n || ldga < 1) cblas_xerbla(11, rout, "ldga must be >= MAX(N,1): ldga=%d N=%d\n", ldga, n);
+  if (ldgb < n || ldgb < 1) cblas_xerbla(13, rout, "ldgb must be >= MAX(N,1): ldgb=%d N=%d\n", ldgb, n);
+  if (n == 0) return 0;
+  cudaStream_t st = ctx().stream;
+  int l_lu, l_x, l_gx;
+  const double *dLU = to_dev<double>(kBufA, LU, n, n, lda, &l_lu, st);
+  const double *dX = to_dev<double>(kBufB, X, n, nrhs, ldx, &l_x, st);
+  const double *dgX = to_dev<double>(kBufW7, gX, n, nrhs, ldgx, &l_gx, st);
+  int *dpiv = static_cast<int *>(ctx().buffer(kBufPiv, sizeof(int) * (size_t)n));
+  ATLG_CHECK(cudaMemcpyAsync(dpiv, ipiv, sizeof(int) * n, cudaMemcpyHostToDevice, st));
+  const int l_ga = l_lu, l_gb = l_lu;
+  double *dgA = static_cast<double *>(ctx().buffer(kBufC, sizeof(double) * (size_t)l_ga * n));
+  double *dgB = static_cast<double *>(ctx().buffer(kBufW6, sizeof(double) * (size_t)l_gb * (nrhs > 0 ? nrhs : 1)));
+  if (nrhs > 0) {
+    adjoint_dev(n, nrhs, dLU, l_lu, dpiv, dX, l_x, dgX, l_gx, dgA, l_ga, dgB, l_gb, st);
+    to_host<double>(gB, ldgb, dgB, l_gb, n, nrhs, st);
+  } else {
+    dev_gescal(n, n, 0.0, dgA, l_ga, st);
+  }
+  to_host<double>(gA, ldga, dgA, l_ga, n, n, st);
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  check_status(rout);
+  return 0;
+}
+
 // ============================================================ C ABI: device
 int atlg_num_sms(void) { return ctx().num_sms; }
 
 void *atlg_stream(void) { return ctx().stream; }
 
 unsigned atlg_status(void) { return gemm_status_read_and_clear() | lu_status_read_and_clear(); }
+
+unsigned long long atlg_launch_count(void) { return ctx().launches; }
+
+void atlg_prof_enable(int on) { ctx().prof = on != 0; }
+
+// Sum of the recorded GEMM launches since the last collect: total device
+// milliseconds, algorithmic flops and launch count.  Synchronizes.
+int atlg_prof_collect(double *ms, double *flops, int *count) {
+  Context &c = ctx();
+  double t = 0.0, f = 0.0;
+  int n = 0;
+  for (auto &r : c.recs) {
+    ATLG_CHECK(cudaEventSynchronize(r.end));
+    float x = 0.f;
+    ATLG_CHECK(cudaEventElapsedTime(&x, r.beg, r.end));
+    t += x;
+    f += r.flops;
+    ++n;
+    c.pool.push_back(r.beg);
+    c.pool.push_back(r.end);
+  }
+  c.recs.clear();
+  if (ms) *ms = t;
+  if (flops) *flops = f;
+  if (count) *count = n;
+  return 0;
+}
+
+void atlg_probe_peaks(double *fp64_tflops, double *fp32_tflops) {
+  if (fp64_tflops) *fp64_tflops = probe_fp64_tflops();
+  if (fp32_tflops) *fp32_tflops = probe_fp32_tflops();
+}
 
 int atlg_dgemm_dev(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda, const double *B,
                    int ldb, double beta, double *C, int ldc, void *stream) {
@@ -447,6 +580,17 @@ int atlg_dgetrf_dev(int M, int N, double *A, int lda, int *ipiv, int *info, void
 int atlg_sgetrf_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void *stream) {
   if (M < 0 || N < 0 || lda < (M > 1 ? M : 1)) return -1;
   dev_sgetrf(M, N, A, lda, ipiv, info, stream_of(stream));
+  return 0;
+}
+int atlg_dgesv_mixed_dev(int N, int NRHS, double *A, int lda, int *ipiv, const double *B, int ldb, double *X,
+                         int ldx, double *berr, double *ferr, int *iters, int *status, void *stream) {
+  if (N < 0 || NRHS < 0) return -1;
+  return mixed_dev(N, NRHS, A, lda, ipiv, B, ldb, X, ldx, berr, ferr, iters, status, stream_of(stream));
+}
+int atlg_dgesv_adjoint_dev(int n, int nrhs, const double *LU, int lda, const int *ipiv, const double *X, int ldx,
+                           const double *gX, int ldgx, double *gA, int ldga, double *gB, int ldgb, void *stream) {
+  if (n < 0 || nrhs < 0) return -1;
+  adjoint_dev(n, nrhs, LU, lda, ipiv, X, ldx, gX, ldgx, gA, ldga, gB, ldgb, stream_of(stream));
   return 0;
 }
 int atlg_dgetrs_dev(int Order, int Trans, int N, int NRHS, const double *A, int lda, const int *ipiv, double *B,

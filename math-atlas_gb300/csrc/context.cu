@@ -61,6 +61,17 @@ void *Context::buffer(int slot, size_t bytes) {
   return buf[slot];
 }
 
+cudaEvent_t Context::event() {
+  if (!pool.empty()) {
+    cudaEvent_t e = pool.back();
+    pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  ATLG_CHECK(cudaEventCreate(&e));
+  return e;
+}
+
 bool encode_tmap_2d(CUtensorMap *map, const void *base, CUtensorMapDataType dtype, int elem_bytes,
                     uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box_rows, uint32_t box_cols,
                     CUtensorMapSwizzle swz) {

@@ -2,13 +2,22 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stddef.h>
+#include <vector>
 
 namespace atlg {
 
 // Device buffer slots reused across calls (grown on demand, never shrunk).
 enum BufSlot {
-  kBufA = 0, kBufB, kBufC, kBufPiv, kBufInfo, kBufW0, kBufW1, kBufW2, kBufW3, kBufW4, kBufW5,
+  kBufA = 0, kBufB, kBufC, kBufPiv, kBufInfo, kBufW0, kBufW1, kBufW2, kBufW3, kBufW4, kBufW5, kBufW6, kBufW7,
   kNumSlots
+};
+
+// Launch accounting and per-kernel timing used by the benchmark: every kernel
+// launch of the library bumps `launches`; when `prof` is on, the GEMM driver
+// brackets each launch with CUDA events on its stream.
+struct ProfRec {
+  cudaEvent_t beg, end;
+  double flops;
 };
 
 struct Context {
@@ -19,6 +28,16 @@ struct Context {
   void *buf[kNumSlots] = {};
   size_t cap[kNumSlots] = {};
   void *buffer(int slot, size_t bytes);
+  unsigned long long launches = 0;
+  bool prof = false;
+  std::vector<ProfRec> recs;
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t event();
 };
+
+inline void note_launch(unsigned n = 1);
+
+Context &ctx();
+inline void note_launch(unsigned n) { ctx().launches += n; }
 
 }  // namespace atlg

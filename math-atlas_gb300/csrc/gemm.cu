@@ -18,6 +18,7 @@
 // fused into the epilogue (beta == 0 never reads C).  The tile shape is picked
 // per call to balance the CTAs over the 152 SMs.
 #include "common.cuh"
+#include "context.cuh"
 #include "gemm.cuh"
 
 namespace atlg {
@@ -199,6 +200,7 @@ static void launch_cfg(int M, int N, int K, T alpha, const T *A, int lda, const 
     auto k = gemm_kernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, true>;
     ATLG_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, KC::SMEM_BYTES));
     k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, tmA, tmB);
+    note_launch();
   } else {
     memset(&tmA, 0, sizeof(tmA));
     memset(&tmB, 0, sizeof(tmB));
@@ -206,6 +208,7 @@ static void launch_cfg(int M, int N, int K, T alpha, const T *A, int lda, const 
     auto k = gemm_kernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, false>;
     ATLG_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, KC::SMEM_BYTES));
     k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, tmA, tmB);
+    note_launch();
   }
   ATLG_CHECK(cudaGetLastError());
 }
@@ -263,6 +266,7 @@ void dev_gescal(int M, int N, double beta, double *C, int ldc, cudaStream_t st) 
   const size_t total = (size_t)M * N;
   const int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
   scale_kernel_d<<<blocks, 256, 0, st>>>(M, N, beta, C, ldc);
+  note_launch();
   ATLG_CHECK(cudaGetLastError());
 }
 void dev_gescal(int M, int N, float beta, float *C, int ldc, cudaStream_t st) {
@@ -270,8 +274,99 @@ void dev_gescal(int M, int N, float beta, float *C, int ldc, cudaStream_t st) {
   const size_t total = (size_t)M * N;
   const int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
   scale_kernel_s<<<blocks, 256, 0, st>>>(M, N, beta, C, ldc);
+  note_launch();
   ATLG_CHECK(cudaGetLastError());
 }
+
+
+// ------------------------------------------------------------------ GEMV
+// y = alpha*op(A)*x + beta*y for the N == 1 products of TRSM, getrs and the
+// refinement residual (a 64x64 GEMM tile would waste 63/64 of its work).
+// op(A) = A (M x K): a CTA owns 32 rows; its 8 warps stride over the K
+// columns (lanes read 32 consecutive rows, 256 B per column), and the 8
+// per-warp partial sums are added in a fixed order, so the result is
+// deterministic.  op(A) = A^T: a warp per output, lanes stride over the
+// contiguous column, shuffle reduction in a fixed order.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    gemv_n_kernel(int M, int K, T alpha, const T *__restrict__ A, int lda, const T *__restrict__ x, int incx,
+                  T beta, T *__restrict__ y) {
+  __shared__ T part[8][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * 32 + lane;
+  T acc = T(0);
+  if (i < M) {
+    const T *a = A + i;
+    int k = w;
+    for (; k + 24 < K; k += 32) {
+      const T a0 = a[(size_t)k * lda], a1 = a[(size_t)(k + 8) * lda];
+      const T a2 = a[(size_t)(k + 16) * lda], a3 = a[(size_t)(k + 24) * lda];
+      acc = fma(a0, x[(size_t)k * incx], acc);
+      acc = fma(a1, x[(size_t)(k + 8) * incx], acc);
+      acc = fma(a2, x[(size_t)(k + 16) * incx], acc);
+      acc = fma(a3, x[(size_t)(k + 24) * incx], acc);
+    }
+    for (; k < K; k += 8) acc = fma(a[(size_t)k * lda], x[(size_t)k * incx], acc);
+  }
+  part[w][lane] = acc;
+  __syncthreads();
+  if (w == 0 && i < M) {
+    T s = part[0][lane];
+#pragma unroll
+    for (int q = 1; q < 8; ++q) s += part[q][lane];
+    const T v = alpha * s;
+    y[i] = (beta == T(0)) ? v : fma(beta, y[i], v);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    gemv_t_kernel(int M, int K, T alpha, const T *__restrict__ A, int lda, const T *__restrict__ x, int incx,
+                  T beta, T *__restrict__ y) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * 8 + w;
+  if (i >= M) return;
+  const T *a = A + (size_t)i * lda;
+  T acc = T(0);
+  for (int k = lane; k < K; k += 32) acc = fma(a[k], x[(size_t)k * incx], acc);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) {
+    const T v = alpha * acc;
+    y[i] = (beta == T(0)) ? v : fma(beta, y[i], v);
+  }
+}
+
+template <typename T>
+static void gemv_launch(int TA, int M, int K, T alpha, const T *A, int lda, const T *x, int incx, T beta, T *y,
+                        cudaStream_t st) {
+  if (TA == kNoTrans)
+    gemv_n_kernel<T><<<(M + 31) / 32, 256, 0, st>>>(M, K, alpha, A, lda, x, incx, beta, y);
+  else
+    gemv_t_kernel<T><<<(M + 7) / 8, 256, 0, st>>>(M, K, alpha, A, lda, x, incx, beta, y);
+  note_launch();
+  ATLG_CHECK(cudaGetLastError());
+}
+
+// CUDA-event bracket around one GEMM launch when profiling is on.
+struct ProfScope {
+  cudaStream_t st;
+  double flops;
+  cudaEvent_t b = nullptr;
+  ProfScope(cudaStream_t s, double f) : st(s), flops(f) {
+    if (ctx().prof) {
+      b = ctx().event();
+      ATLG_CHECK(cudaEventRecord(b, st));
+    }
+  }
+  ~ProfScope() {
+    if (b) {
+      cudaEvent_t e = ctx().event();
+      ATLG_CHECK(cudaEventRecord(e, st));
+      ctx().recs.push_back({b, e, flops});
+    }
+  }
+};
 
 // ATL_gemm semantics: alpha==0 or K==0 -> C = beta*C (gescal / gezero).
 void dev_dgemm(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda, const double *B,
@@ -279,7 +374,12 @@ void dev_dgemm(int TA, int TB, int M, int N, int K, double alpha, const double *
   if (M <= 0 || N <= 0) return;
   if (alpha == 0.0 || K <= 0) { dev_gescal(M, N, beta, C, ldc, st); return; }
   const bool ta = TA != kNoTrans, tb = TB != kNoTrans;
-  const int nsm = o.num_sms > 0 ? o.num_sms : kNumSMs;
+  const int nsm = o.num_sms > 0 ? o.num_sms : ctx().num_sms;
+  if (N == 1 && o.allow_gemv) {   // matrix-vector product: x = op(B)(:,0)
+    gemv_launch<double>(TA, M, K, alpha, A, lda, B, tb ? ldb : 1, beta, C, st);
+    return;
+  }
+  ProfScope ps(st, 2.0 * M * N * K);
   if (!ta && !tb) dgemm_t<kNoTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm);
   else if (!ta && tb) dgemm_t<kNoTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm);
   else if (ta && !tb) dgemm_t<kTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm);
@@ -291,6 +391,11 @@ void dev_sgemm(int TA, int TB, int M, int N, int K, float alpha, const float *A,
   if (M <= 0 || N <= 0) return;
   if (alpha == 0.0f || K <= 0) { dev_gescal(M, N, beta, C, ldc, st); return; }
   const bool ta = TA != kNoTrans, tb = TB != kNoTrans;
+  if (N == 1 && o.allow_gemv) {
+    gemv_launch<float>(TA, M, K, alpha, A, lda, B, tb ? ldb : 1, beta, C, st);
+    return;
+  }
+  ProfScope ps(st, 2.0 * M * N * K);
   if (!ta && !tb) sgemm_t<kNoTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma);
   else if (!ta && tb) sgemm_t<kNoTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma);
   else if (ta && !tb) sgemm_t<kTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma);

@@ -340,6 +340,7 @@ static void laswp_impl(int N, T *A, int lda, int K1, int K2, const int *ipiv, in
   laswp_perm_kernel<<<1, 1024, smem, st>>>(ipiv, K1, K2, inci, content, nrows, use_smem);
   gather_rows_kernel<T><<<grid_for((long)nrows * N), 256, 0, st>>>(A, lda, W, nrows, content, nrows, N);
   copy_rows_kernel<T><<<grid_for((long)nrows * N), 256, 0, st>>>(A, lda, W, nrows, nrows, N);
+  note_launch(3);
   ATLG_CHECK(cudaGetLastError());
 }
 
@@ -394,10 +395,12 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     int koff = k;
     void *args[] = {&Ap, (void *)&lda, &Mp, (void *)&jb, &koff, &ipk, &info, &cval, &cidx, &crow, &jrow, &bar, &perm};
     ATLG_CHECK(cudaLaunchCooperativeKernel((const void *)panel_kernel<T>, dim3(G), dim3(PT), args, 0, st));
+    note_launch();
     const int c_from = k + jb;
     const int nl = (k + 31) / 32, nr = (N - c_from + 31) / 32;
     if (nl + nr > 0) {
       apply_perm_kernel<T><<<nl + nr, 256, 0, st>>>(A, lda, k, perm, k, c_from, N);
+      note_launch();
       ATLG_CHECK(cudaGetLastError());
     }
     if (c_from < N) {

@@ -1,0 +1,245 @@
+// mixed.cu -- mixed-precision dgesv: factor in FP32, recover FP64 accuracy by
+// iterative refinement with FP64 residuals; fall back to the FP64 LU when
+// refinement does not converge.
+//
+// No reference counterpart: ATLAS has no mixed-precision solver.  The method
+// is iterative refinement as published by Langou, Luszczek, Kurzak, Buttari
+// and Dongarra ("Exploiting the performance of 32 bit floating point
+// arithmetic in obtaining 64 bit accuracy", SC'06) and used by LAPACK's
+// dsgesv; the stopping test is that of dsgesv:
+//   ||r_j||_inf <= ||x_j||_inf * ||A||_inf * eps * sqrt(n)   for every column j,
+// with eps = 2^-53, at most 30 refinement steps; refinement also stops as
+// stalled when the residual fails to halve twice in a row.
+//
+// GB300 mapping: the FP32 LU is the FFMA path of lu.cu (sgetrf) and the
+// FP32 solves are its sgetrs; the FP64 residual r = b - A x is one DGEMM (or
+// DGEMV for one right-hand side) on the unmodified FP64 A; conversions and
+// norms are elementwise kernels.  All FP64 work on the GPU is the residual,
+// the update x += d and the norms; the O(n^3) work is FP32.
+#include <float.h>
+#include <math.h>
+#include <vector>
+
+#include "common.cuh"
+#include "context.cuh"
+#include "gemm.cuh"
+#include "lu.cuh"
+#include "mixed.cuh"
+
+namespace atlg {
+
+__global__ void d2s_kernel(int M, int N, const double *__restrict__ A, int lda, float *__restrict__ S, int lds,
+                           int *overflow) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < (long)M * N; e += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % M), j = (int)(e / M);
+    const double v = A[i + (size_t)j * lda];
+    if (fabs(v) > (double)FLT_MAX) *overflow = 1;
+    S[i + (size_t)j * lds] = (float)v;
+  }
+}
+__global__ void s2d_kernel(int M, int N, const float *__restrict__ S, int lds, double *__restrict__ A, int lda) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < (long)M * N; e += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % M), j = (int)(e / M);
+    A[i + (size_t)j * lda] = (double)S[i + (size_t)j * lds];
+  }
+}
+__global__ void axpy_s2d_kernel(int M, int N, const float *__restrict__ S, int lds, double *__restrict__ X, int ldx) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < (long)M * N; e += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % M), j = (int)(e / M);
+    X[i + (size_t)j * ldx] += (double)S[i + (size_t)j * lds];
+  }
+}
+__global__ void copy_d_kernel(int M, int N, const double *__restrict__ S, int lds, double *__restrict__ D, int ldd) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < (long)M * N; e += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % M), j = (int)(e / M);
+    D[i + (size_t)j * ldd] = S[i + (size_t)j * lds];
+  }
+}
+
+// column-wise max |v| of an M x N block: out[j] (one CTA per column)
+template <typename T>
+__global__ void __launch_bounds__(256) colmax_kernel(int M, const T *__restrict__ V, int ldv, double *out) {
+  __shared__ double sh[8];
+  const T *v = V + (size_t)blockIdx.x * ldv;
+  double m = 0.0;
+  for (int i = threadIdx.x; i < M; i += 256) {
+    const double a = fabs((double)v[i]);
+    m = a > m ? a : m;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double t = __shfl_down_sync(0xffffffffu, m, o);
+    m = t > m ? t : m;
+  }
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int q = 0; q < 8; ++q) r = sh[q] > r ? sh[q] : r;
+    out[blockIdx.x] = r;
+  }
+}
+
+// row sums of |A| (n x n, column-major): a CTA owns 32 rows, warps stride columns
+__global__ void __launch_bounds__(256) rowabs_kernel(int M, int N, const double *__restrict__ A, int lda,
+                                                     double *rows) {
+  __shared__ double part[8][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * 32 + lane;
+  double acc = 0.0;
+  if (i < M)
+    for (int k = w; k < N; k += 8) acc += fabs(A[i + (size_t)k * lda]);
+  part[w][lane] = acc;
+  __syncthreads();
+  if (w == 0 && i < M) {
+    double s = 0.0;
+    for (int q = 0; q < 8; ++q) s += part[q][lane];
+    rows[i] = s;
+  }
+}
+
+static int grid_for(long work) {
+  long b = (work + 255) / 256;
+  if (b > 16L * 152) b = 16L * 152;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+static std::vector<double> colmax_host(int M, int N, const double *V, int ldv, double *dtmp, cudaStream_t st) {
+  colmax_kernel<double><<<N, 256, 0, st>>>(M, V, ldv, dtmp);
+  note_launch();
+  std::vector<double> h(N);
+  ATLG_CHECK(cudaMemcpyAsync(h.data(), dtmp, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  return h;
+}
+
+int dev_dgesv_mixed(int n, int nrhs, double *A, int lda, int *ipiv, const double *B, int ldb, double *X, int ldx,
+                    MixedResult *res, cudaStream_t st) {
+  Context &c = ctx();
+  res->iters = 0;
+  res->status = 0;
+  res->berr.assign(nrhs, 0.0);
+  res->ferr.assign(nrhs, 0.0);
+  if (n == 0 || nrhs == 0) return 0;
+  const int lds = (n + 3) & ~3;               // 16-byte aligned FP32 columns (TMA)
+  float *S = static_cast<float *>(c.buffer(kBufW1, sizeof(float) * (size_t)lds * n));
+  const int ldr = (n + 1) & ~1;
+  double *R = static_cast<double *>(c.buffer(kBufW2, sizeof(double) * (size_t)ldr * nrhs));
+  float *R32 = static_cast<float *>(c.buffer(kBufW5, sizeof(float) * (size_t)lds * nrhs + 4096));
+  double *small = static_cast<double *>(c.buffer(kBufInfo, sizeof(double) * (size_t)(2 * n + 2 * nrhs + 16)));
+  int *dinfo = reinterpret_cast<int *>(small);
+  int *dovf = dinfo + 1;
+  double *dtmp = small + 2;
+  double *drows = dtmp + nrhs;
+
+  // ||A||_inf and ||b_j||_inf in FP64
+  rowabs_kernel<<<(n + 31) / 32, 256, 0, st>>>(n, n, A, lda, drows);
+  note_launch();
+  const double anrm = colmax_host(n, 1, drows, n, dtmp, st)[0];
+  std::vector<double> bnrm = colmax_host(n, nrhs, B, ldb, dtmp, st);
+  const double eps = ldexp(1.0, -53);
+  const double cte = anrm * eps * sqrt((double)n);
+
+  // FP32 factorization
+  ATLG_CHECK(cudaMemsetAsync(dinfo, 0, 2 * sizeof(int), st));
+  d2s_kernel<<<grid_for((long)n * n), 256, 0, st>>>(n, n, A, lda, S, lds, dovf);
+  note_launch();
+  dev_sgetrf(n, n, S, lds, ipiv, dinfo, st);
+  int hinfo[2] = {0, 0};
+  ATLG_CHECK(cudaMemcpyAsync(hinfo, dinfo, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  bool fallback = hinfo[0] != 0 || hinfo[1] != 0;
+
+  int iter = 0;
+  if (!fallback) {
+    // x0 = (A32)^-1 b in FP32, promoted
+    d2s_kernel<<<grid_for((long)n * nrhs), 256, 0, st>>>(n, nrhs, B, ldb, R32, lds, dovf);
+    note_launch();
+    dev_sgetrs(kColMajor, kNoTrans, n, nrhs, S, lds, ipiv, R32, lds, st);
+    s2d_kernel<<<grid_for((long)n * nrhs), 256, 0, st>>>(n, nrhs, R32, lds, X, ldx);
+    note_launch();
+    double prev = INFINITY;
+    int slow = 0;
+    const int kItMax = 30;
+    bool conv = false;
+    for (iter = 0; iter <= kItMax; ++iter) {
+      // r = b - A x  (FP64)
+      copy_d_kernel<<<grid_for((long)n * nrhs), 256, 0, st>>>(n, nrhs, B, ldb, R, ldr);
+      note_launch();
+      dev_dgemm(kNoTrans, kNoTrans, n, nrhs, n, -1.0, A, lda, X, ldx, 1.0, R, ldr, st);
+      std::vector<double> rn = colmax_host(n, nrhs, R, ldr, dtmp, st);
+      std::vector<double> xn = colmax_host(n, nrhs, X, ldx, dtmp, st);
+      conv = true;
+      double rmax = 0.0;
+      for (int j = 0; j < nrhs; ++j) {
+        if (!(rn[j] <= xn[j] * cte)) conv = false;
+        rmax = rn[j] > rmax ? rn[j] : rmax;
+        const double den = anrm * xn[j] + bnrm[j];
+        res->berr[j] = den > 0 ? rn[j] / den : 0.0;
+      }
+      if (conv || iter == kItMax) break;
+      if (!(rmax < 0.5 * prev)) {
+        if (++slow >= 2) break;   // stalled
+      } else {
+        slow = 0;
+      }
+      prev = rmax;
+      // d = (A32)^-1 r in FP32; x += d
+      d2s_kernel<<<grid_for((long)n * nrhs), 256, 0, st>>>(n, nrhs, R, ldr, R32, lds, dovf);
+      note_launch();
+      dev_sgetrs(kColMajor, kNoTrans, n, nrhs, S, lds, ipiv, R32, lds, st);
+      axpy_s2d_kernel<<<grid_for((long)n * nrhs), 256, 0, st>>>(n, nrhs, R32, lds, X, ldx);
+      note_launch();
+      {
+        // forward-error estimate ||d||/||x|| from the FP32 correction
+        s2d_kernel<<<grid_for((long)n * nrhs), 256, 0, st>>>(n, nrhs, R32, lds, R, ldr);
+        note_launch();
+        std::vector<double> d2 = colmax_host(n, nrhs, R, ldr, dtmp, st);
+        std::vector<double> x2 = colmax_host(n, nrhs, X, ldx, dtmp, st);
+        for (int j = 0; j < nrhs; ++j) res->ferr[j] = x2[j] > 0 ? d2[j] / x2[j] : 0.0;
+      }
+    }
+    res->iters = iter;
+    fallback = !conv;
+  }
+  if (fallback) {
+    // FP64 LU of a copy of A and the FP64 solve; the normwise backward error
+    // is measured against the untouched A, then the factors are returned in A
+    // (LAPACK dsgesv convention for the fallback).
+    res->status = 1;
+    const int ldf = (n + 1) & ~1;
+    double *F = static_cast<double *>(c.buffer(kBufW6, sizeof(double) * (size_t)ldf * n));
+    copy_d_kernel<<<grid_for((long)n * n), 256, 0, st>>>(n, n, A, lda, F, ldf);
+    note_launch();
+    dev_dgetrf(n, n, F, ldf, ipiv, dinfo, st);
+    int i64 = 0;
+    ATLG_CHECK(cudaMemcpyAsync(&i64, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ATLG_CHECK(cudaStreamSynchronize(st));
+    if (i64 != 0) {
+      res->status = 2;
+      copy_d_kernel<<<grid_for((long)n * n), 256, 0, st>>>(n, n, F, ldf, A, lda);
+      note_launch();
+      ATLG_CHECK(cudaStreamSynchronize(st));
+      return i64;
+    }
+    copy_d_kernel<<<grid_for((long)n * nrhs), 256, 0, st>>>(n, nrhs, B, ldb, X, ldx);
+    note_launch();
+    dev_dgetrs(kColMajor, kNoTrans, n, nrhs, F, ldf, ipiv, X, ldx, st);
+    copy_d_kernel<<<grid_for((long)n * nrhs), 256, 0, st>>>(n, nrhs, B, ldb, R, ldr);
+    note_launch();
+    dev_dgemm(kNoTrans, kNoTrans, n, nrhs, n, -1.0, A, lda, X, ldx, 1.0, R, ldr, st);
+    std::vector<double> rn = colmax_host(n, nrhs, R, ldr, dtmp, st);
+    std::vector<double> xn = colmax_host(n, nrhs, X, ldx, dtmp, st);
+    for (int j = 0; j < nrhs; ++j) {
+      const double den = anrm * xn[j] + bnrm[j];
+      res->berr[j] = den > 0 ? rn[j] / den : 0.0;
+      res->ferr[j] = 0.0;
+    }
+    copy_d_kernel<<<grid_for((long)n * n), 256, 0, st>>>(n, n, F, ldf, A, lda);
+    note_launch();
+    ATLG_CHECK(cudaStreamSynchronize(st));
+  }
+  return 0;
+}
+
+}  // namespace atlg

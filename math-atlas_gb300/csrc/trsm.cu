@@ -14,6 +14,7 @@
 // reciprocal as in the reference.  The off-diagonal update is one GEMM per
 // block step on the library's DFMA/FFMA GEMM.
 #include "common.cuh"
+#include "context.cuh"
 #include "gemm.cuh"
 #include "trsm.cuh"
 
@@ -145,6 +146,7 @@ static void trsm_impl(int side, int uplo, int tA, int diag, int M, int N, T alph
       const int b = lower ? s : nb - 1 - s;
       const int r0 = b * TB, n = (M - r0 < TB) ? M - r0 : TB;
       trsm_diag_left<T><<<grid, blk, 0, st>>>(A, lda, ta, lower, unit, r0, n, N, B, ldb);
+      note_launch();
       ATLG_CHECK(cudaGetLastError());
       if (lower && r0 + n < M)
         gemm_any<T>(ta, kNoTrans, M - r0 - n, N, n, T(-1), opblk(A, lda, ta, r0 + n, r0), lda, B + r0, ldb, T(1),
@@ -160,6 +162,7 @@ static void trsm_impl(int side, int uplo, int tA, int diag, int M, int N, T alph
       const int b = upper ? s : nb - 1 - s;
       const int c0 = b * TB, n = (N - c0 < TB) ? N - c0 : TB;
       trsm_diag_right<T><<<grid, blk, 0, st>>>(A, lda, ta, upper, unit, c0, n, M, B, ldb);
+      note_launch();
       ATLG_CHECK(cudaGetLastError());
       if (upper && c0 + n < N)
         gemm_any<T>(kNoTrans, ta, M, N - c0 - n, n, T(-1), B + (size_t)c0 * ldb, ldb, opblk(A, lda, ta, c0, c0 + n),
@@ -188,6 +191,7 @@ void dev_trsm_llnu_block(const double *A, int lda, int k, int n, double *B, int 
   const dim3 grid((ncols + WARPS - 1) / WARPS);
   trsm_diag_left<double><<<grid, WARPS * 32, 0, st>>>(A + k + (size_t)k * lda, lda, kNoTrans, 1, 1, 0, n, ncols,
                                                        B, ldb);
+      note_launch();
   ATLG_CHECK(cudaGetLastError());
 }
 void dev_trsm_llnu_block(const float *A, int lda, int k, int n, float *B, int ldb, int ncols, cudaStream_t st) {
@@ -195,6 +199,7 @@ void dev_trsm_llnu_block(const float *A, int lda, int k, int n, float *B, int ld
   const dim3 grid((ncols + WARPS - 1) / WARPS);
   trsm_diag_left<float><<<grid, WARPS * 32, 0, st>>>(A + k + (size_t)k * lda, lda, kNoTrans, 1, 1, 0, n, ncols, B,
                                                       ldb);
+      note_launch();
   ATLG_CHECK(cudaGetLastError());
 }
 
