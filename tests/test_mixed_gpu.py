@@ -1,0 +1,67 @@
+"""Mixed-precision dgesv (FP32 LU + FP64 iterative refinement, FP64
+fallback) through the C ABI.  A = U diag(s) V^T with U, V from Householder QR
+of seeded Gaussian matrices and s geometric from 1 to 1/kappa; b Gaussian.
+Accuracy is judged against the FP64 oracle solve: normwise backward error
+<= n*eps (double-double residual), forward error comparable to the FP64
+LU's."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def make_system(n, kappa, seed):
+    rng = np.random.default_rng(seed)
+    U, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    V, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    s = np.geomspace(1.0, 1.0 / kappa, n)
+    A = np.asfortranarray((U * s) @ V.T)
+    b = np.asfortranarray(rng.standard_normal((n, 1)))
+    return A, b
+
+
+@pytest.mark.parametrize("kappa,expect_fallback", [(1e2, False), (1e6, False), (1e10, True)])
+def test_dgesv_mixed_accuracy(gb, ora, kappa, expect_fallback):
+    n = 1024
+    A, b = make_system(n, kappa, 20260 + int(np.log10(kappa)))
+    A0 = A.copy(order="F")
+    X = np.zeros((n, 1), order="F")
+    ipiv = np.zeros(n, dtype=np.int32)
+    info, berr, ferr, iters, status = gb.dgesv_mixed(A, ipiv, b.copy(order="F"), X)
+    assert info == 0
+    assert status == (1 if expect_fallback else 0), (status, iters, berr)
+    eps = np.finfo(float).eps
+    be = ora.backward_error(A0, X[:, 0], b[:, 0])
+    assert be <= n * eps, be
+    assert abs(be - berr[0]) <= 1e-2 * be + 1e-18 or berr[0] <= n * eps
+    # FP64 oracle solve for the forward-error comparison
+    Ao = A0.copy(order="F")
+    xo = b.copy(order="F")
+    ora.lib().ora_dgesv(102, n, 1, Ao, n, np.zeros(n, dtype=np.int32), xo, n)
+    fe_mixed = np.abs(X - xo).max() / np.abs(xo).max()
+    assert fe_mixed <= max(1e3 * kappa * eps, 1e-12)
+    if not expect_fallback:
+        assert np.array_equal(A, A0)          # A untouched when refinement converged
+        assert 1 <= iters <= 30
+
+
+def test_dgesv_mixed_multiple_rhs(gb, ora):
+    n, nrhs = 700, 4
+    A, _ = make_system(n, 1e3, 5)
+    rng = np.random.default_rng(9)
+    B = np.asfortranarray(rng.standard_normal((n, nrhs)))
+    X = np.zeros((n, nrhs), order="F")
+    info, berr, ferr, iters, status = gb.dgesv_mixed(A.copy(order="F"), np.zeros(n, dtype=np.int32), B, X)
+    assert info == 0 and status == 0 and berr.shape == (nrhs,)
+    for j in range(nrhs):
+        assert ora.backward_error(A, X[:, j], B[:, j]) <= n * np.finfo(float).eps
+
+
+def test_dgesv_mixed_singular_reports_info(gb):
+    n = 64
+    A = np.asfortranarray(np.random.default_rng(1).standard_normal((n, n)))
+    A[:, 5] = 0.0
+    X = np.zeros((n, 1), order="F")
+    b = np.ones((n, 1), order="F")
+    info, berr, ferr, iters, status = gb.dgesv_mixed(A, np.zeros(n, dtype=np.int32), b, X)
+    assert info == 6 and status == 2
