@@ -122,6 +122,18 @@ int atlg_dtrsm_dev(int Side, int Uplo, int TA, int Diag, int M, int N, double al
 /* ATL_laswp semantics (AtlasBase/Clint/atlas-lp.base:1053); rows [0,nrows) may move */
 int atlg_dlaswp_dev(int N, double *A, int lda, int K1, int K2, const int *ipiv, int inci,
                     int nrows, void *stream);
+/* The same row interchanges as atlg_dlaswp_dev without any device allocation
+ * (no reference counterpart): its scratch is a fixed 16 MiB array that every
+ * GPU loading the library holds until exit.  For callers that cannot let a
+ * library call cudaMalloc/cudaFree (their own pool owns device memory, or
+ * they cannot take the device-wide synchronisation those calls imply).
+ * Returns 0; -1 bad size; -2 when 4*nrows (rounded up to 256) + 8*nrows*N
+ * bytes exceed the 16 MiB scratch; -3 CUDA error.  The first call on a
+ * device looks up the scratch address (cudaGetSymbolAddress): make it before
+ * any stream capture.  Calls that overlap on the GPU share the scratch and
+ * race: serialise them. */
+int atlg_dlaswp_noalloc(int N, double *A, int lda, int K1, int K2, const int *ipiv, int inci,
+                        int nrows, void *stream);
 /* column-major LU; info written to device memory */
 int atlg_dgetrf_dev(int M, int N, double *A, int lda, int *ipiv, int *info, void *stream);
 int atlg_sgetrf_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void *stream);

@@ -28,6 +28,7 @@ EXPORTS = [
     "atlg_dgemm_dev_opts", "atlg_sgemm_dev", "atlg_dtrsm_dev", "atlg_dlaswp_dev", "atlg_dgetrf_dev",
     "atlg_sgetrf_dev", "atlg_dgetrs_dev", "atlg_launch_count", "atlg_prof_enable", "atlg_prof_collect",
     "atlg_probe_peaks", "dgesv_mixed", "dgesv_adjoint", "atlg_dgesv_mixed_dev", "atlg_dgesv_adjoint_dev",
+    "atlg_dlaswp_noalloc",
 ]
 
 _lib = None
@@ -73,6 +74,7 @@ def _declare(L):
         "atlg_sgemm_dev": (_i, [_i, _i, _i, _i, _i, _f, _v, _i, _v, _i, _f, _v, _i, _v]),
         "atlg_dtrsm_dev": (_i, [_i, _i, _i, _i, _i, _i, _d, _v, _i, _v, _i, _v]),
         "atlg_dlaswp_dev": (_i, [_i, _v, _i, _i, _i, _v, _i, _i, _v]),
+        "atlg_dlaswp_noalloc": (_i, [_i, _v, _i, _i, _i, _v, _i, _i, _v]),
         "atlg_dgetrf_dev": (_i, [_i, _i, _v, _i, _v, _v, _v]),
         "atlg_sgetrf_dev": (_i, [_i, _i, _v, _i, _v, _v, _v]),
         "atlg_dgetrs_dev": (_i, [_i, _i, _i, _i, _v, _i, _v, _v, _i, _v]),

@@ -26,6 +26,7 @@
 // pivot search are within rounding of each other; the factors agree to
 // rounding (different but equally stable summation order).
 #include <float.h>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -479,4 +480,78 @@ unsigned lu_status_read_and_clear() {
   return v;
 }
 
+
+// ------------------------------------------------- laswp without allocation
+// Some callers cannot let a library allocate device memory in the middle of
+// their work: programs that hand all device memory to their own pool
+// allocator up front, and programs that cannot accept the device-wide
+// synchronisation that cudaMalloc / cudaFree imply.  atlg_dlaswp_noalloc is
+// the row-interchange operation of atlg_dlaswp_dev for them: its scratch (the
+// row-content table and the gathered rows) lives in the fixed array below,
+// which the CUDA runtime reserves on every GPU that loads this library and
+// keeps until the process exits.
+//
+//  - Limit: 4*nrows bytes (rounded up to 256) + 8*nrows*N bytes must fit in
+//    kNoAllocScratchBytes (16 MiB); larger calls are rejected with a message
+//    on stderr and return -2, before any work is queued.
+//  - Set-up: the first call on each device looks up the array's device
+//    address with cudaGetSymbolAddress while that device is current.  Make
+//    that first call before beginning any stream capture.
+//  - Every call shares the one array, so calls whose work overlaps on the GPU
+//    (different streams, or concurrent host threads) race on it; serialise
+//    them.  Nothing in the array has to start at zero: the permutation kernel
+//    fills its whole table and the gather writes every element the copy back
+//    reads, so the contents left by the previous call are never read.
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+static unsigned char *noalloc_scratch_for_current_device() {
+  static std::mutex mu;
+  static unsigned char *addr[256] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!addr[dev]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+      fprintf(stderr, "atlg_dlaswp_noalloc: cudaGetSymbolAddress failed on device %d: %s\n", dev,
+              cudaGetErrorString(e));
+      return nullptr;
+    }
+    addr[dev] = static_cast<unsigned char *>(p);
+  }
+  return addr[dev];
+}
+
 }  // namespace atlg
+
+extern "C" int atlg_dlaswp_noalloc(int N, double *A, int lda, int K1, int K2, const int *ipiv, int inci, int nrows,
+                                   void *stream) {
+  using namespace atlg;
+  if (N < 0 || nrows < 0 || lda < (nrows > 1 ? nrows : 1)) return -1;
+  if (K2 <= K1 || N == 0 || nrows == 0) return 0;
+  const size_t table = ((size_t)nrows * sizeof(int) + 255) & ~size_t(255);
+  const size_t need = table + (size_t)nrows * (size_t)N * sizeof(double);
+  if (need > kNoAllocScratchBytes) {
+    fprintf(stderr,
+            "atlg_dlaswp_noalloc: %d rows x %d columns need %zu bytes of scratch; the fixed scratch holds %zu "
+            "(4*nrows rounded to 256 + 8*nrows*N must not exceed it)\n",
+            nrows, N, need, kNoAllocScratchBytes);
+    return -2;
+  }
+  unsigned char *base = noalloc_scratch_for_current_device();
+  if (!base) return -3;
+  int *content = reinterpret_cast<int *>(base);
+  double *W = reinterpret_cast<double *>(base + table);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int use_smem = nrows <= kPermSmemRows;
+  const size_t smem = use_smem ? sizeof(int) * (size_t)nrows : 0;
+  if (cudaFuncSetAttribute(laswp_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
+      cudaSuccess)
+    return -3;
+  laswp_perm_kernel<<<1, 1024, smem, st>>>(ipiv, K1, K2, inci, content, nrows, use_smem);
+  gather_rows_kernel<double><<<grid_for((long)nrows * N), 256, 0, st>>>(A, lda, W, nrows, content, nrows, N);
+  copy_rows_kernel<double><<<grid_for((long)nrows * N), 256, 0, st>>>(A, lda, W, nrows, nrows, N);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
