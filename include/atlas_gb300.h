@@ -81,6 +81,14 @@ int clapack_sgesv(const enum CBLAS_ORDER Order, const int N, const int NRHS, flo
 
 /* ---- new methods (no reference counterpart: ATLAS has neither a
  *      mixed-precision solver nor an adjoint).  Column-major. */
+/* Split-precision DGEMM: cblas_dgemm's interface and checks, computed from
+ * `nslices` (1..8) 7-bit integer slices of each operand (per-row / per-column
+ * power-of-two scaling) multiplied exactly on tcgen05 tensor cores and
+ * recombined in FP64 (Ozaki scheme). */
+void dgemm_split(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TA,
+                 const enum CBLAS_TRANSPOSE TB, const int M, const int N, const int K,
+                 const double alpha, const double *A, const int lda, const double *B,
+                 const int ldb, const double beta, double *C, const int ldc, const int nslices);
 /* FP32 LU + FP64 iterative refinement (LAPACK dsgesv stopping test), with an
  * FP64-LU fallback.  A is unchanged unless the fallback ran (status 1; A then
  * holds the FP64 factors); B is unchanged; X receives the solution; berr and
@@ -115,6 +123,9 @@ int atlg_dgemm_dev(int TA, int TB, int M, int N, int K, double alpha, const doub
 int atlg_dgemm_dev_opts(int TA, int TB, int M, int N, int K, double alpha, const double *A,
                         int lda, const double *B, int ldb, double beta, double *C, int ldc,
                         int allow_tma, void *stream);
+int atlg_dgemm_split_dev(int TA, int TB, int M, int N, int K, double alpha, const double *A,
+                         int lda, const double *B, int ldb, double beta, double *C, int ldc,
+                         int nslices, void *stream);
 int atlg_sgemm_dev(int TA, int TB, int M, int N, int K, float alpha, const float *A, int lda,
                    const float *B, int ldb, float beta, float *C, int ldc, void *stream);
 int atlg_dtrsm_dev(int Side, int Uplo, int TA, int Diag, int M, int N, double alpha,

@@ -28,7 +28,7 @@ EXPORTS = [
     "atlg_dgemm_dev_opts", "atlg_sgemm_dev", "atlg_dtrsm_dev", "atlg_dlaswp_dev", "atlg_dgetrf_dev",
     "atlg_sgetrf_dev", "atlg_dgetrs_dev", "atlg_launch_count", "atlg_prof_enable", "atlg_prof_collect",
     "atlg_probe_peaks", "dgesv_mixed", "dgesv_adjoint", "atlg_dgesv_mixed_dev", "atlg_dgesv_adjoint_dev",
-    "atlg_dlaswp_noalloc",
+    "atlg_dlaswp_noalloc", "dgemm_split", "atlg_dgemm_split_dev",
 ]
 
 _lib = None
@@ -84,6 +84,8 @@ def _declare(L):
         "atlg_dgesv_mixed_dev": (_i, [_i, _i, _v, _i, _v, _v, _i, _v, _i, C.POINTER(_d), C.POINTER(_d),
                                       C.POINTER(_i), C.POINTER(_i), _v]),
         "atlg_dgesv_adjoint_dev": (_i, [_i, _i, _v, _i, _v, _v, _i, _v, _i, _v, _i, _v, _i, _v]),
+        "dgemm_split": (None, [_i, _i, _i, _i, _i, _i, _d, _dp, _i, _dp, _i, _d, _dp, _i, _i]),
+        "atlg_dgemm_split_dev": (_i, [_i, _i, _i, _i, _i, _d, _v, _i, _v, _i, _d, _v, _i, _i, _v]),
         "atlg_launch_count": (C.c_ulonglong, []),
         "atlg_prof_enable": (None, [_i]),
         "atlg_prof_collect": (_i, [C.POINTER(_d), C.POINTER(_d), C.POINTER(_i)]),
@@ -136,6 +138,14 @@ def clapack_dgesv(order, N, NRHS, A, lda, ipiv, B, ldb):
 
 def clapack_sgesv(order, N, NRHS, A, lda, ipiv, B, ldb):
     return lib().clapack_sgesv(order, N, NRHS, A, lda, ipiv, B, ldb)
+
+
+def dgemm_split(ta, tb, alpha, A, B, beta, Cm, nslices=7):
+    M, N = Cm.shape
+    K = A.shape[1] if ta == NoTrans else A.shape[0]
+    lib().dgemm_split(ColMajor, ta, tb, M, N, K, alpha, A, A.shape[0], B, B.shape[0], beta, Cm, Cm.shape[0],
+                      nslices)
+    return Cm
 
 
 def dgesv_mixed(A, ipiv, B, X):

@@ -22,6 +22,7 @@
 #include "gemm.cuh"
 #include "lu.cuh"
 #include "mixed.cuh"
+#include "split.cuh"
 #include "trsm.cuh"
 
 using namespace atlg;
@@ -53,7 +54,7 @@ extern "C" void cblas_xerbla(int p, const char *rout, const char *form, ...) {
 namespace {
 
 void check_status(const char *rout) {
-  const unsigned s = gemm_status_read_and_clear() | lu_status_read_and_clear();
+  const unsigned s = gemm_status_read_and_clear() | lu_status_read_and_clear() | split_status_read_and_clear();
   if (s) {
     fprintf(stderr, "atlas_gb300: %s: device wait gave up (status 0x%x)\n", rout, s);
     fflush(stderr);
@@ -432,6 +433,40 @@ int clapack_sgesv(const enum CBLAS_ORDER Order, const int N, const int NRHS, flo
   return host_gesv<float>("clapack_sgesv", Order, N, NRHS, A, lda, ipiv, B, ldb);
 }
 
+// Split-precision DGEMM (no reference counterpart; see split.cu): the
+// cblas_dgemm interface and checks, plus the number of 7-bit slices per
+// operand (1..8; 7 gives about 49 bits of each row/column's largest entry).
+void dgemm_split(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TA, const enum CBLAS_TRANSPOSE TB,
+                 const int M, const int N, const int K, const double alpha, const double *A, const int lda,
+                 const double *B, const int ldb, const double beta, double *C, const int ldc, const int nslices) {
+  const char *rout = "dgemm_split";
+  if (gemm_check<double>(rout, Order, TA, TB, M, N, K, lda, ldb, ldc)) return;
+  if (nslices < 1 || nslices > 8) cblas_xerbla(15, rout, "nslices must be in 1..8: %d\n", nslices);
+  if (M == 0 || N == 0) return;
+  int ta = TA, tb = TB, m = M, n = N, la = lda, lb = ldb;
+  const double *a = A, *b = B;
+  if (Order == CblasRowMajor) {
+    a = B; b = A; la = ldb; lb = lda; ta = TB; tb = TA; m = N; n = M;
+  }
+  cudaStream_t st = ctx().stream;
+  int ldd_c;
+  double *dC;
+  if (beta != 0.0) dC = to_dev<double>(kBufC, C, m, n, ldc, &ldd_c, st);
+  else {
+    ldd_c = even_up(m);
+    dC = static_cast<double *>(ctx().buffer(kBufC, sizeof(double) * (size_t)ldd_c * n));
+  }
+  const int ra = (ta == CblasNoTrans) ? m : K, ca = (ta == CblasNoTrans) ? K : m;
+  const int rb = (tb == CblasNoTrans) ? K : n, cb = (tb == CblasNoTrans) ? n : K;
+  int ldd_a, ldd_b;
+  const double *dA = to_dev<double>(kBufA, a, ra, ca, la, &ldd_a, st);
+  const double *dB = to_dev<double>(kBufB, b, rb, cb, lb, &ldd_b, st);
+  dev_dgemm_split(ta, tb, m, n, K, alpha, dA, ldd_a, dB, ldd_b, beta, dC, ldd_c, nslices, st);
+  to_host<double>(C, ldc, dC, ldd_c, m, n, st);
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  check_status(rout);
+}
+
 // Mixed-precision solve (no reference counterpart; see mixed.cu).  Column-
 // major.  A is unchanged unless the FP64 fallback ran (status 1: A then
 // holds the FP64 factors, as LAPACK dsgesv leaves them); B is unchanged; X
@@ -508,7 +543,16 @@ int atlg_num_sms(void) { return ctx().num_sms; }
 
 void *atlg_stream(void) { return ctx().stream; }
 
-unsigned atlg_status(void) { return gemm_status_read_and_clear() | lu_status_read_and_clear(); }
+unsigned atlg_status(void) {
+  return gemm_status_read_and_clear() | lu_status_read_and_clear() | split_status_read_and_clear();
+}
+
+int atlg_dgemm_split_dev(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda,
+                         const double *B, int ldb, double beta, double *C, int ldc, int nslices, void *stream) {
+  if (M < 0 || N < 0 || K < 0 || nslices < 1 || nslices > 8) return -1;
+  dev_dgemm_split(TA, TB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, nslices, stream_of(stream));
+  return 0;
+}
 
 unsigned long long atlg_launch_count(void) { return ctx().launches; }
 

@@ -1,0 +1,364 @@
+// split.cu -- split-precision DGEMM: C = alpha*op(A)*op(B) + beta*C in FP64
+// computed from 7-bit integer slices of A and B on the fifth-generation
+// tensor cores (tcgen05, kind::f16), accumulated exactly, recombined in FP64.
+//
+// No reference counterpart (ATLAS's GEMM is FP64 throughout).  The method is
+// the Ozaki scheme of error-free splitting (Ozaki, Ogita, Oishi, Rump,
+// Numer. Algorithms 59, 2012) in its integer form (Ootomo, Ozaki, Yokota,
+// IJHPCA 2024: "DGEMM on integer matrix multiplication unit"):
+//   op(A) = diag(2^ea) sum_t 2^(-7(t+1)) A_t,  op(B) = (sum_u 2^(-7(u+1)) B_u) diag(2^eb)
+// with per-row (A) / per-column (B) power-of-two scales and integer digit
+// matrices |A_t|, |B_u| <= 127, and
+//   op(A) op(B) ~= diag(2^ea) [ sum_{t+u<=s-1} 2^(-7(t+u+2)) A_t B_u ] diag(2^eb).
+//
+// GB300 mapping.  sm_103a has no tcgen05 INT8 MMA (kind::i8 does not
+// assemble), so the digits are stored as FP16 -- every integer of magnitude
+// <= 2048 is exact in FP16 -- and multiplied with tcgen05.mma kind::f16 into
+// FP32 tensor memory.  A product of two digits is below 2^14; 1024 of them
+// sum below 2^24, so an FP32 accumulator over a K chunk of 1024 holds the
+// exact integer (the GPU test checks this bit for bit).  After each chunk the
+// epilogue warps move the accumulator out of tensor memory (tcgen05.ld),
+// convert it to int32 and add it to per-thread int32 sums that collect every
+// chunk and every slice pair of one diagonal t+u = d (at most 8 pairs x 16
+// chunks x 2^24 < 2^31 for K <= 16384: exact).  Each diagonal is then added
+// into C in FP64 with one exact power-of-two scaling, smallest diagonal
+// first.  K > 16384 is split into pieces accumulated through beta = 1.
+//
+// Kernel structure (one 128 x 128 tile of C per CTA, 6 warps):
+//   warp 0   TMA producer: 128 x 64 FP16 tiles of A_t and B_u (K-major,
+//            128-byte swizzle) into a 5-stage shared-memory ring;
+//   warp 1   allocates 256 tensor-memory columns (two 128-column FP32
+//            accumulators) and issues the MMAs (one thread), committing to
+//            the ring's empty barriers and the accumulator-full barriers;
+//   warps 2-9 epilogue: warp w reads tensor-memory lane quarter w % 4;
+//            each thread owns one row of the tile and 64 of its columns
+//            (int32 sums).
+// Every wait is bounded; a timeout sets the status word and an abort flag
+// that every role polls, so the CTA drains, frees its tensor memory and exits.
+#include <cuda_fp16.h>
+#include <math.h>
+
+#include "common.cuh"
+#include "context.cuh"
+#include "gemm.cuh"
+#include "split.cuh"
+#include "tc.cuh"
+
+namespace atlg {
+
+__device__ unsigned g_split_status;
+
+constexpr int kSliceBits = 7;
+constexpr int TM = 128, TN = 128, KB = 64, KCHUNK_BLOCKS = 16;   // 16 x 64 = 1024 = exact FP32 chunk
+constexpr int STAGES = 5;
+constexpr int STAGE_BYTES = (TM + TN) * KB * 2;                  // 32 KB
+constexpr int SPLIT_THREADS = 320;                             // 2 + 8 warps
+constexpr int EPI_COLS = 64;                                   // columns per epilogue thread
+constexpr int SPLIT_SMEM = STAGES * STAGE_BYTES + 1024 + 256;
+
+// --------------------------------------------------------------- scaling
+// ex[r] = exponent e with max_k |In(r,k)| < 2^e (0 for an all-zero vector);
+// In(r,k) = In[r*rs + k*ks].  Contiguous-in-k vectors: a warp per vector;
+// otherwise 32 consecutive vectors per CTA, 8 warps striding over k.
+__global__ void __launch_bounds__(256) vec_exp_kernel(int R, int Kd, const double *__restrict__ In, long rs, long ks,
+                                                      int *__restrict__ ex) {
+  __shared__ double part[8][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double m = 0.0;
+  int r;
+  if (ks == 1) {
+    r = blockIdx.x * 8 + w;
+    if (r < R)
+      for (int k = lane; k < Kd; k += 32) m = fmax(m, fabs(In[(size_t)r * rs + k]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    if (lane == 0 && r < R) {
+      int e = 0;
+      if (m > 0.0) frexp(m, &e);
+      ex[r] = e;
+    }
+  } else {
+    r = blockIdx.x * 32 + lane;
+    if (r < R)
+      for (int k = w; k < Kd; k += 8) m = fmax(m, fabs(In[(size_t)r * rs + (size_t)k * ks]));
+    part[w][lane] = m;
+    __syncthreads();
+    if (w == 0 && r < R) {
+      double mm = 0.0;
+      for (int q = 0; q < 8; ++q) mm = fmax(mm, part[q][lane]);
+      int e = 0;
+      if (mm > 0.0) frexp(mm, &e);
+      ex[r] = e;
+    }
+  }
+}
+
+// Digit split of In (R x Kd, strides rs/ks) into s FP16 slices
+// Out[(t*Rp + r)*Kp + k], zero outside R x Kd.  x = In * 2^-e in (-1, 1);
+// digit t = trunc(128 * remainder), exact in binary64.
+__global__ void __launch_bounds__(256) slice_kernel(int R, int Kd, int Rp, int Kp, int s, const double *__restrict__ In,
+                                                    long rs, long ks, const int *__restrict__ ex,
+                                                    __half *__restrict__ Out) {
+  __shared__ double tile[32][33];
+  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
+  // load: coalesce along whichever dimension is contiguous
+  for (int q = ty; q < 32; q += 8) {
+    int r, k;
+    if (ks == 1) { r = r0 + q; k = k0 + tx; } else { r = r0 + tx; k = k0 + q; }
+    double v = 0.0;
+    if (r < R && k < Kd) v = ldexp(In[(size_t)r * rs + (size_t)k * ks], -ex[r]);
+    if (ks == 1) tile[q][tx] = v; else tile[tx][q] = v;
+  }
+  __syncthreads();
+  // store: consecutive threads -> consecutive k
+  for (int q = ty; q < 32; q += 8) {
+    const int r = r0 + q, k = k0 + tx;
+    if (r >= Rp || k >= Kp) continue;
+    double x = tile[q][tx];
+    for (int t = 0; t < s; ++t) {
+      x *= 128.0;
+      const double dg = trunc(x);
+      x -= dg;
+      Out[((size_t)t * Rp + r) * Kp + k] = __double2half((float)dg);
+    }
+  }
+}
+
+// ------------------------------------------------------------ tensor cores
+struct SplitArgs {
+  int M, N, Mp, Np, Kp, s;
+  double alpha, beta;
+  double *C;
+  int ldc;
+  const int *exA, *exB;
+};
+
+__device__ __forceinline__ bool wait_or_abort(uint64_t *bar, unsigned parity, volatile int *abort_flag) {
+  for (unsigned i = 0; i < kMbarPollLimit; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 255u) == 255u && *abort_flag) return false;
+  }
+  atomicOr(&g_split_status, kErrMbarTimeout);
+  *abort_flag = 1;
+  return false;
+}
+
+__global__ void __launch_bounds__(SPLIT_THREADS, 1)
+    ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, SplitArgs p) {
+  extern __shared__ unsigned char smem_dyn[];
+  const uint32_t raw = smem_u32(smem_dyn);
+  const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
+  unsigned char *base = smem_dyn + pad;                           // 1024-byte aligned stage ring
+  uint64_t *full = reinterpret_cast<uint64_t *>(base + STAGES * STAGE_BYTES);
+  uint64_t *empty = full + STAGES;
+  uint64_t *acc_full = empty + STAGES;
+  uint64_t *acc_empty = acc_full + 2;
+  uint64_t *done = acc_empty + 2;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  __shared__ double colscale[TN];
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * TM, n0 = blockIdx.y * TN;
+  const int nkb = p.Kp / KB;
+  const int nchunk = (nkb + KCHUNK_BLOCKS - 1) / KCHUNK_BLOCKS;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < STAGES; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], 1); }
+    for (int i = 0; i < 2; ++i) { mbar_init(&acc_full[i], 1); mbar_init(&acc_empty[i], 8 * 32); }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    fence_mbar_init();
+  }
+  for (int c = threadIdx.x; c < TN; c += SPLIT_THREADS) {
+    const int col = n0 + c;
+    colscale[c] = (col < p.N) ? ldexp(1.0, p.exB[col]) : 0.0;
+  }
+  if (warp == 1) tmem_alloc(tmem_slot, 256);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------------------------ TMA producer
+    if (lane == 0) {
+      prefetch_tmap(&tmA);
+      prefetch_tmap(&tmB);
+      long it = 0;
+      bool ok = true;
+      for (int d = p.s - 1; d >= 0 && ok; --d)
+        for (int t = 0; t <= d && ok; ++t) {
+          const int u = d - t;
+          for (int kb = 0; kb < nkb && ok; ++kb, ++it) {
+            const int st = (int)(it % STAGES);
+            const unsigned ph = (unsigned)((it / STAGES) & 1);
+            if (!wait_or_abort(&empty[st], ph ^ 1u, abort_flag)) { ok = false; break; }
+            unsigned char *sa = base + st * STAGE_BYTES;
+            mbar_arrive_expect_tx(&full[st], STAGE_BYTES);
+            tma_load_2d(sa, &tmA, &full[st], kb * KB, t * p.Mp + m0);
+            tma_load_2d(sa + TM * KB * 2, &tmB, &full[st], kb * KB, u * p.Np + n0);
+          }
+        }
+      // drain: every load issued has landed before the CTA can exit
+      for (long j = (it > STAGES ? it - STAGES : 0); j < it; ++j)
+        wait_or_abort(&full[j % STAGES], (unsigned)((j / STAGES) & 1), abort_flag);
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc = idesc_f16_f32(TM, TN);
+      long it = 0, cc = 0;
+      bool ok = true;
+      for (int d = p.s - 1; d >= 0 && ok; --d)
+        for (int t = 0; t <= d && ok; ++t)
+          for (int ch = 0; ch < nchunk && ok; ++ch, ++cc) {
+            const int buf = (int)(cc & 1);
+            if (!wait_or_abort(&acc_empty[buf], (unsigned)(((cc >> 1) & 1) ^ 1), abort_flag)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t dt = tmem + (uint32_t)(buf * TN);
+            const int kb0 = ch * KCHUNK_BLOCKS;
+            const int kb1 = (kb0 + KCHUNK_BLOCKS < nkb) ? kb0 + KCHUNK_BLOCKS : nkb;
+            for (int kb = kb0; kb < kb1; ++kb, ++it) {
+              const int st = (int)(it % STAGES);
+              if (!wait_or_abort(&full[st], (unsigned)((it / STAGES) & 1), abort_flag)) { ok = false; break; }
+              tc_fence_after();
+              const uint32_t sa = smem_u32(base + st * STAGE_BYTES);
+              const uint64_t da = sw128_kmajor_desc(sa);
+              const uint64_t db = sw128_kmajor_desc(sa + TM * KB * 2);
+#pragma unroll
+              for (int kk = 0; kk < KB / 16; ++kk)   // K = 16 per MMA: 32 bytes along the swizzled row
+                mma_f16(dt, da + (uint64_t)(2 * kk), db + (uint64_t)(2 * kk), idesc, (kb > kb0 || kk > 0) ? 1u : 0u);
+              mma_commit(&empty[st]);
+            }
+            if (!ok) break;
+            mma_commit(&acc_full[buf]);
+          }
+      // all issued MMAs complete before tensor memory is released
+      mma_commit(done);
+      wait_or_abort(done, 0, abort_flag);
+    }
+  } else {
+    // ------------------------------------------------ epilogue (warps 2..9)
+    const int q = warp & 3;                 // tensor-memory lane quarter of this warp
+    const int h = (warp - 2) >> 2;          // column half of the tile
+    const int row = q * 32 + lane;
+    const int gm = m0 + row;
+    const bool row_ok = gm < p.M;
+    const double rowpow = row_ok ? p.alpha : 0.0;
+    const int rexp = row_ok ? p.exA[gm] : 0;
+    int acc[EPI_COLS];
+#pragma unroll
+    for (int c = 0; c < EPI_COLS; ++c) acc[c] = 0;
+    long cc = 0;
+    bool first = true, ok = true;
+    for (int d = p.s - 1; d >= 0 && ok; --d) {
+      for (int t = 0; t <= d && ok; ++t)
+        for (int ch = 0; ch < nchunk; ++ch, ++cc) {
+          const int buf = (int)(cc & 1);
+          int okw = 1;
+          if (lane == 0) okw = wait_or_abort(&acc_full[buf], (unsigned)((cc >> 1) & 1), abort_flag) ? 1 : 0;
+          okw = __shfl_sync(0xffffffffu, okw, 0);
+          if (!okw) { ok = false; break; }
+          tc_fence_after();
+#pragma unroll
+          for (int cb = 0; cb < EPI_COLS / 16; ++cb) {
+            uint32_t r[16];
+            tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * TN + h * EPI_COLS + cb * 16), r);
+            tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) acc[cb * 16 + j] += __float2int_rn(__uint_as_float(r[j]));
+          }
+          tc_fence_before();
+          mbar_arrive(&acc_empty[buf]);
+        }
+      if (!ok) break;
+      // diagonal d complete: C (+)= alpha 2^(ea - 7(d+2)) acc 2^(eb)
+      const double fr = ldexp(rowpow, rexp - kSliceBits * (d + 2));
+#pragma unroll
+      for (int c = 0; c < EPI_COLS; ++c) {
+        const int gn = n0 + h * EPI_COLS + c;
+        if (row_ok && gn < p.N) {
+          double *cp = p.C + gm + (size_t)gn * p.ldc;
+          const double v = (double)acc[c] * fr * colscale[h * EPI_COLS + c];
+          if (first) *cp = (p.beta == 0.0) ? v : fma(p.beta, *cp, v);
+          else *cp += v;
+        }
+        acc[c] = 0;
+      }
+      first = false;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    tmem_dealloc(tmem, 256);
+  }
+}
+
+// ---------------------------------------------------------------- host side
+static int ceil_to(int x, int m) { return (x + m - 1) / m * m; }
+
+static void split_one(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda, const double *B,
+                      int ldb, double beta, double *C, int ldc, int s, cudaStream_t st) {
+  Context &c = ctx();
+  const int Mp = ceil_to(M, TM), Np = ceil_to(N, TN), Kp = ceil_to(K, KB);
+  __half *As = static_cast<__half *>(c.buffer(kBufS0, sizeof(__half) * (size_t)s * Mp * Kp));
+  __half *Bs = static_cast<__half *>(c.buffer(kBufS1, sizeof(__half) * (size_t)s * Np * Kp));
+  int *ex = static_cast<int *>(c.buffer(kBufS2, sizeof(int) * (size_t)(Mp + Np)));
+  int *exA = ex, *exB = ex + Mp;
+  // op(A)(i,k): TA==N -> A[i + k lda];  TA==T -> A[k + i lda]
+  const long ars = (TA == kNoTrans) ? 1 : lda, aks = (TA == kNoTrans) ? lda : 1;
+  // op(B)(k,j) seen as vector j over k: TB==N -> B[k + j ldb];  TB==T -> B[j + k ldb]
+  const long brs = (TB == kNoTrans) ? ldb : 1, bks = (TB == kNoTrans) ? 1 : ldb;
+  vec_exp_kernel<<<aks == 1 ? (M + 7) / 8 : (M + 31) / 32, 256, 0, st>>>(M, K, A, ars, aks, exA);
+  vec_exp_kernel<<<bks == 1 ? (N + 7) / 8 : (N + 31) / 32, 256, 0, st>>>(N, K, B, brs, bks, exB);
+  slice_kernel<<<dim3(Kp / 32, Mp / 32), 256, 0, st>>>(M, K, Mp, Kp, s, A, ars, aks, exA, As);
+  slice_kernel<<<dim3(Kp / 32, Np / 32), 256, 0, st>>>(N, K, Np, Kp, s, B, brs, bks, exB, Bs);
+  note_launch(4);
+  CUtensorMap tA, tB;
+  if (!encode_tmap_2d(&tA, As, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, Kp, (uint64_t)s * Mp, Kp, KB, TM,
+                      CU_TENSOR_MAP_SWIZZLE_128B) ||
+      !encode_tmap_2d(&tB, Bs, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, Kp, (uint64_t)s * Np, Kp, KB, TN,
+                      CU_TENSOR_MAP_SWIZZLE_128B)) {
+    fprintf(stderr, "atlas_gb300: split dgemm: tensor map encoding failed\n");
+    abort();
+  }
+  SplitArgs a;
+  a.M = M; a.N = N; a.Mp = Mp; a.Np = Np; a.Kp = Kp; a.s = s;
+  a.alpha = alpha; a.beta = beta; a.C = C; a.ldc = ldc; a.exA = exA; a.exB = exB;
+  ATLG_CHECK(cudaFuncSetAttribute(ozaki_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPLIT_SMEM));
+  ozaki_tc_kernel<<<dim3(Mp / TM, Np / TN), SPLIT_THREADS, SPLIT_SMEM, st>>>(tA, tB, a);
+  note_launch();
+  ATLG_CHECK(cudaGetLastError());
+}
+
+void dev_dgemm_split(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda, const double *B,
+                     int ldb, double beta, double *C, int ldc, int nslices, cudaStream_t st) {
+  if (M <= 0 || N <= 0) return;
+  if (nslices < 1) nslices = 1;
+  if (nslices > 8) nslices = 8;
+  if (alpha == 0.0 || K <= 0) {
+    dev_gescal(M, N, beta, C, ldc, st);
+    return;
+  }
+  // int32 sums stay exact for K <= 16384 (8 pairs x 16 chunks x 2^24 < 2^31)
+  const int kmax = 16384;
+  for (int k0 = 0; k0 < K; k0 += kmax) {
+    const int kk = (K - k0 < kmax) ? K - k0 : kmax;
+    const double *Ak = (TA == kNoTrans) ? A + (size_t)k0 * lda : A + k0;
+    const double *Bk = (TB == kNoTrans) ? B + k0 : B + (size_t)k0 * ldb;
+    split_one(TA, TB, M, N, kk, alpha, Ak, lda, Bk, ldb, k0 == 0 ? beta : 1.0, C, ldc, nslices, st);
+  }
+}
+
+unsigned split_status_read_and_clear() {
+  unsigned v = 0, z = 0;
+  ATLG_CHECK(cudaMemcpyFromSymbol(&v, g_split_status, sizeof(v)));
+  if (v) ATLG_CHECK(cudaMemcpyToSymbol(g_split_status, &z, sizeof(z)));
+  return v;
+}
+
+}  // namespace atlg
