@@ -157,6 +157,103 @@ def run_reference(args):
     return 0
 
 
+# ------------------------------------------------------------- other forms
+def measure_forms(G, O, torch, n=16384, kappas=(1e2, 1e6, 1e10), nslices=8):
+    """The two other FP64-accuracy forms at n=16384 (SURVEY configs 3 and 4):
+    mixed-precision dgesv on A = U diag(s) V^T (U, V from Householder QR of
+    seeded Gaussian matrices, s geometric 1..1/kappa) against the plain FP64
+    dgesv on the same matrix, and the split-precision DGEMM on
+    uniform[-1,1]*2^e operands (e in [-16,16]) against the double-double
+    oracle on sampled entries."""
+    import ctypes as C
+    L = G.lib()
+    st = L.atlg_stream()
+    out = {}
+    dev = "cuda"
+    g = torch.Generator(device=dev).manual_seed(4)
+    U, _ = torch.linalg.qr(torch.randn(n, n, device=dev, dtype=torch.float64, generator=g))
+    V, _ = torch.linalg.qr(torch.randn(n, n, device=dev, dtype=torch.float64, generator=g))
+    b = torch.randn(n, device=dev, dtype=torch.float64, generator=g)
+    piv = torch.zeros(n, dtype=torch.int32, device=dev)
+    info_d = torch.zeros(4, dtype=torch.int32, device=dev)
+    rows = []
+    plain_t = None
+    for kappa in kappas:
+        sv = torch.logspace(0, -np.log10(kappa), n, device=dev, dtype=torch.float64)
+        Acm = ((U * sv) @ V.T).t().contiguous()      # column-major A
+        A = torch.empty_like(Acm)
+        X = torch.zeros(n, device=dev, dtype=torch.float64)
+        berr, ferr, it, stt = C.c_double(), C.c_double(), C.c_int(), C.c_int()
+        ts = []
+        for rep in range(2):
+            A.copy_(Acm)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            info = L.atlg_dgesv_mixed_dev(n, 1, A.data_ptr(), n, piv.data_ptr(), b.data_ptr(), n, X.data_ptr(), n,
+                                          C.byref(berr), C.byref(ferr), C.byref(it), C.byref(stt), st)
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        row = {"kappa": kappa, "ms": min(ts) * 1e3, "tflops": dgesv_flops(n) / min(ts) / 1e12, "info": info,
+               "iters": it.value, "fallback_fp64": stt.value == 1, "backward_error": berr.value,
+               "n_eps": n * np.finfo(float).eps}
+        if plain_t is None or kappa == kappas[-1]:
+            A.copy_(Acm)
+            xb = b.clone()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            L.atlg_dgetrf_dev(n, n, A.data_ptr(), n, piv.data_ptr(), info_d.data_ptr(), st)
+            L.atlg_dgetrs_dev(102, 111, n, 1, A.data_ptr(), n, piv.data_ptr(), xb.data_ptr(), n, st)
+            torch.cuda.synchronize()
+            plain_t = time.perf_counter() - t0
+            row["forward_vs_plain_fp64"] = float((X - xb).abs().max() / xb.abs().max())
+        row["speedup_vs_plain_fp64"] = plain_t / min(ts)
+        rows.append(row)
+        del A, Acm
+    out["mixed_dgesv_n16384"] = rows
+    out["plain_dgesv_n16384"] = {"ms": plain_t * 1e3, "tflops": dgesv_flops(n) / plain_t / 1e12}
+    del U, V
+    torch.cuda.empty_cache()
+    # split-precision DGEMM 16384^3
+    A = (torch.rand(n, n, device=dev, dtype=torch.float64, generator=g) * 2 - 1) * \
+        torch.exp2(torch.randint(-16, 17, (n, n), device=dev, generator=g).double())
+    B = (torch.rand(n, n, device=dev, dtype=torch.float64, generator=g) * 2 - 1) * \
+        torch.exp2(torch.randint(-16, 17, (n, n), device=dev, generator=g).double())
+    Cm = torch.zeros(n, n, device=dev, dtype=torch.float64)
+    s = torch.cuda.ExternalStream(st)
+    ts = []
+    for rep in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        # column-major A, B: the torch tensors hold A^T row-major == A column-major
+        L.atlg_dgemm_split_dev(111, 111, n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0, Cm.data_ptr(), n,
+                               nslices, st)
+        e1.record(s)
+        torch.cuda.synchronize()
+        if rep:
+            ts.append(e0.elapsed_time(e1))
+    ms = min(ts)
+    # accuracy on 64 sampled entries against the double-double oracle
+    Ah = A.cpu().numpy().T      # column-major view of the device data
+    Bh = B.cpu().numpy().T
+    Ch = Cm.cpu().numpy().T
+    rng = np.random.default_rng(0)
+    ii = rng.integers(0, n, 64).astype(np.int32)
+    jj = rng.integers(0, n, 64).astype(np.int32)
+    hi, lo = O.dd_samples(111, 111, n, n, n, np.asfortranarray(Ah), np.asfortranarray(Bh), ii, jj)
+    ref = hi + lo
+    got = Ch[ii, jj]
+    rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
+    absab = np.array([np.abs(Ah[i, :]) @ np.abs(Bh[:, j]) for i, j in zip(ii, jj)])
+    out["split_dgemm_n16384"] = {"nslices": nslices, "ms": ms, "tflops_fp64_equiv": 2.0 * n ** 3 / ms / 1e9,
+                                 "tensor_tflops": nslices * (nslices + 1) / 2 * 2.0 * n ** 3 / ms / 1e9,
+                                 "max_rel_err_vs_double_double": float(rel.max()),
+                                 "max_err_over_sum_abs_vs_double_double": float((np.abs(got - ref) / absab).max()),
+                                 "samples": 64}
+    del A, B, Cm
+    torch.cuda.empty_cache()
+    return out
+
+
 # ------------------------------------------------------------------ GPU side
 def run_gpu(args):
     import torch
@@ -279,6 +376,9 @@ def run_gpu(args):
             cpu = {"value": dgesv_flops(ncpu) / tc / 1e12, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"one dgesv n={ncpu} nrhs=1 (oracle restatement of getrfC/getrs, OpenMP)"}
         bwd = O.backward_error(np.asfortranarray(A_h), x, b_h.reshape(-1))
+        forms = None
+        if world == 1 and not args.skip_extras:
+            forms = measure_forms(G, O, torch)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
@@ -297,6 +397,8 @@ def run_gpu(args):
             "clocks": clk,
             "accuracy": {"backward_error": bwd, "n_eps": n * np.finfo(float).eps},
         }
+        if forms is not None:
+            line["forms"] = forms
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
@@ -312,6 +414,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=8192)
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
+    ap.add_argument("--skip-extras", action="store_true",
+                    help="omit the n=16384 mixed-dgesv and split-DGEMM measurements")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

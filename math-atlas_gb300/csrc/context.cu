@@ -37,7 +37,10 @@ Context &ctx() {
     c->num_sms = p.multiProcessorCount;
     c->cc_major = p.major;
     c->cc_minor = p.minor;
-    ATLG_CHECK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    int lo = 0, hi = 0;
+    ATLG_CHECK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    // the library's own stream carries the factorization's critical path
+    ATLG_CHECK(cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, hi));
     void *fn = nullptr;
     cudaDriverEntryPointQueryResult q;
     ATLG_CHECK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
@@ -70,6 +73,20 @@ cudaEvent_t Context::event() {
   cudaEvent_t e;
   ATLG_CHECK(cudaEventCreate(&e));
   return e;
+}
+
+cudaStream_t Context::side_stream() {
+  if (!side) {
+    int lo = 0, hi = 0;
+    ATLG_CHECK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    ATLG_CHECK(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, lo));   // lo = least urgent
+  }
+  return side;
+}
+
+cudaEvent_t Context::sync_event(int i) {
+  if (!sync_ev[i]) ATLG_CHECK(cudaEventCreateWithFlags(&sync_ev[i], cudaEventDisableTiming));
+  return sync_ev[i];
 }
 
 bool encode_tmap_2d(CUtensorMap *map, const void *base, CUtensorMapDataType dtype, int elem_bytes,

@@ -33,6 +33,10 @@ struct Context {
   std::vector<ProfRec> recs;
   std::vector<cudaEvent_t> pool;
   cudaEvent_t event();
+  cudaStream_t side = nullptr;       // low-priority stream for overlapped updates
+  cudaEvent_t sync_ev[4] = {};       // cross-stream ordering (no timing)
+  cudaStream_t side_stream();
+  cudaEvent_t sync_event(int i);
 };
 
 inline void note_launch(unsigned n = 1);

@@ -41,6 +41,7 @@ __device__ unsigned g_lu_status;
 
 constexpr int NB = 64;          // panel width
 constexpr int PT = 256;         // threads per panel CTA
+constexpr size_t kPanelSmemMax = 192 * 1024;   // shared-memory panel slice limit
 
 template <typename T> struct Lim;
 template <> struct Lim<double> { __device__ static double safmin() { return DBL_MIN; } };
@@ -76,15 +77,30 @@ __device__ void block_argmax(T &val, int &idx, BlockArgmax<T> &sh) {
   __syncthreads();
 }
 
+// The rows a panel CTA owns, either in global memory (rows of the panel,
+// leading dimension lda) or copied to a column-major shared-memory tile of
+// R rows for the whole factorization of the panel.
+template <typename T, bool SM>
+struct PanelRows {
+  T *g;
+  int lda;
+  T *s;
+  int R, r0;
+  __device__ __forceinline__ T &at(int i, int c) const {
+    if (SM) return s[(i - r0) + c * R];
+    return g[i + (size_t)c * lda];
+  }
+};
+
 // Local candidate for column j among own rows [max(r0,j), r1); stage it.
-template <typename T>
-__device__ void stage_candidate(const T *A, int lda, int j, int jb, int r0, int r1, int par, int G, T *cval,
+template <typename T, bool SM>
+__device__ void stage_candidate(const PanelRows<T, SM> &A, int j, int jb, int r0, int r1, int par, int G, T *cval,
                                 int *cidx, T *crow, T *jrow, BlockArgmax<T> &sh, int *s_idx) {
   T best = T(-1);
   int bi = 0x7fffffff;
   const int lo = r0 > j ? r0 : j;
   for (int i = lo + threadIdx.x; i < r1; i += PT) {      // ascending rows per thread
-    T a = A[i + (size_t)j * lda];
+    T a = A.at(i, j);
     a = a < T(0) ? -a : a;
     if (a > best) { best = a; bi = i; }
   }
@@ -97,29 +113,46 @@ __device__ void stage_candidate(const T *A, int lda, int j, int jb, int r0, int 
   __syncthreads();
   const int ci = *s_idx;
   if (ci >= 0)
-    for (int c = threadIdx.x; c < jb; c += PT) crow[((size_t)par * G + blockIdx.x) * NB + c] = A[ci + (size_t)c * lda];
+    for (int c = threadIdx.x; c < jb; c += PT) crow[((size_t)par * G + blockIdx.x) * NB + c] = A.at(ci, c);
   if (j >= r0 && j < r1)
-    for (int c = threadIdx.x; c < jb; c += PT) jrow[par * NB + c] = A[j + (size_t)c * lda];
+    for (int c = threadIdx.x; c < jb; c += PT) jrow[par * NB + c] = A.at(j, c);
 }
 
-template <typename T>
+template <typename T, bool SM>
 __global__ void __launch_bounds__(PT)
-    panel_kernel(T *A, int lda, int M, int jb, int koff, int *ipiv, int *info, T *cval, int *cidx, T *crow,
+    panel_kernel(T *Ag, int lda, int M, int jb, int koff, int *ipiv, int *info, T *cval, int *cidx, T *crow,
                  T *jrow, unsigned *bar, int *perm) {
+  extern __shared__ __align__(16) unsigned char panel_dyn[];
   __shared__ BlockArgmax<T> sh;
   __shared__ T P[NB], J[NB];
-  __shared__ T lbuf[2048];
   __shared__ int s_idx, s_p, s_zero;
   __shared__ T s_piv;
   __shared__ int piv_local[NB];
+  constexpr int LB = SM ? 1 : 2048;
+  __shared__ T lbuf[LB];
 
   const int G = gridDim.x;
   const int chunk = (M + G - 1) / G;
   const int r0 = blockIdx.x * chunk;
   const int r1 = (r0 + chunk < M) ? r0 + chunk : M;
-  const bool big = (r1 - r0) > 2048;
+  const bool big = !SM && (r1 - r0) > 2048;
+  PanelRows<T, SM> A;
+  A.g = Ag;
+  A.lda = lda;
+  A.s = reinterpret_cast<T *>(panel_dyn);
+  A.R = chunk;
+  A.r0 = r0;
+  if (SM) {
+    const int nr = r1 - r0;
+    if (nr > 0)
+      for (int e = threadIdx.x; e < nr * jb; e += PT) {
+        const int i = e % nr, c = e / nr;
+        A.s[i + c * chunk] = Ag[(r0 + i) + (size_t)c * lda];
+      }
+    __syncthreads();
+  }
 
-  stage_candidate(A, lda, 0, jb, r0, r1, 0, G, cval, cidx, crow, jrow, sh, &s_idx);
+  stage_candidate(A, 0, jb, r0, r1, 0, G, cval, cidx, crow, jrow, sh, &s_idx);
   for (int j = 0; j < jb; ++j) {
     const int par = j & 1;
     if (!grid_barrier(&bar[0], &bar[1], G, &g_lu_status)) return;
@@ -167,20 +200,19 @@ __global__ void __launch_bounds__(PT)
       const int lo = r0 > j ? r0 : j;
       for (int i = lo + threadIdx.x; i < r1; i += PT) {
         if (i == j) {
-          if (!big) lbuf[i - r0] = T(0);
+          if (!SM && !big) lbuf[i - r0] = T(0);
           continue;
         }
-        const T src = (i == p) ? J[j] : A[i + (size_t)j * lda];
+        const T src = (i == p) ? J[j] : A.at(i, j);
         const T l = use_rcp ? src * rcp : src / pv;
-        A[i + (size_t)j * lda] = l;
-        if (!big) lbuf[i - r0] = l;
+        A.at(i, j) = l;
+        if (!SM && !big) lbuf[i - r0] = l;
       }
       // row j <- pivot row (all columns); row p <- old row j in the L part
       if (j >= r0 && j < r1)
-        for (int c = threadIdx.x; c < jb; c += PT)
-          A[j + (size_t)c * lda] = P[c];
+        for (int c = threadIdx.x; c < jb; c += PT) A.at(j, c) = P[c];
       if (p != j && p >= r0 && p < r1)
-        for (int c = threadIdx.x; c < j; c += PT) A[p + (size_t)c * lda] = J[c];
+        for (int c = threadIdx.x; c < j; c += PT) A.at(p, c) = J[c];
       __syncthreads();
       // pass 2: rank-1 update of columns j+1..jb-1 in own rows i > j
       const int ncol = jb - j - 1;
@@ -191,15 +223,24 @@ __global__ void __launch_bounds__(PT)
           const int i = lo + (int)(e % nrow);
           const int c = j + 1 + (int)(e / nrow);
           if (i == j) continue;
-          const T l = big ? A[i + (size_t)j * lda] : lbuf[i - r0];
-          const T src = (i == p) ? J[c] : A[i + (size_t)c * lda];
-          A[i + (size_t)c * lda] = src - l * P[c];
+          const T l = (SM || big) ? A.at(i, j) : lbuf[i - r0];
+          const T src = (i == p) ? J[c] : A.at(i, c);
+          A.at(i, c) = src - l * P[c];
         }
       }
       __syncthreads();
     }
     if (j + 1 < jb)
-      stage_candidate(A, lda, j + 1, jb, r0, r1, (j + 1) & 1, G, cval, cidx, crow, jrow, sh, &s_idx);
+      stage_candidate(A, j + 1, jb, r0, r1, (j + 1) & 1, G, cval, cidx, crow, jrow, sh, &s_idx);
+  }
+  if (SM) {
+    __syncthreads();
+    const int nr = r1 - r0;
+    if (nr > 0)
+      for (int e = threadIdx.x; e < nr * jb; e += PT) {
+        const int i = e % nr, c = e / nr;
+        Ag[(r0 + i) + (size_t)c * lda] = A.s[i + c * chunk];
+      }
   }
   // ---- CTA 0: reduce the NB interchanges to a permutation of rows ----
   if (blockIdx.x == 0 && threadIdx.x < 32) {
@@ -372,7 +413,19 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
   if (M <= 0 || N <= 0) return;
   Context &c = ctx();
   const int MN = M < N ? M : N;
+  // Look-ahead: the trailing update of step k is split into the next panel's
+  // columns (on the caller's stream, so panel k+1 can start at once) and the
+  // rest (on a low-priority side stream, overlapping panel k+1).  The panel
+  // grid then takes a quarter of the SMs, as few as its shared-memory slices
+  // allow, leaving the rest to the concurrent update.
+  const bool lookahead = MN > 2 * NB && N > 2 * NB;
   int G = c.num_sms;
+  if (lookahead) {
+    G = c.num_sms / 4;
+    const size_t need = (size_t)M * NB * sizeof(T);
+    while (G < c.num_sms && ((size_t)((M + G - 1) / G) * NB * sizeof(T)) > kPanelSmemMax) G += 1;
+    (void)need;
+  }
   // at least a few rows per CTA for the tallest panel
   if (G > (M + 7) / 8) G = (M + 7) / 8;
   if (G < 1) G = 1;
@@ -387,6 +440,11 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
   unsigned *bar = reinterpret_cast<unsigned *>(cidx + 2 * G);
   int *perm = reinterpret_cast<int *>(bar + 2);
   ATLG_CHECK(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st));
+  ATLG_CHECK(cudaFuncSetAttribute(panel_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kPanelSmemMax));
+  cudaStream_t side = c.side_stream();
+  cudaEvent_t ev_ready = c.sync_event(0), ev_side = c.sync_event(1);
+  bool side_pending = false;
 
   for (int k = 0; k < MN; k += NB) {
     const int jb = (MN - k < NB) ? MN - k : NB;
@@ -395,8 +453,18 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     int *ipk = ipiv + k;
     int koff = k;
     void *args[] = {&Ap, (void *)&lda, &Mp, (void *)&jb, &koff, &ipk, &info, &cval, &cidx, &crow, &jrow, &bar, &perm};
-    ATLG_CHECK(cudaLaunchCooperativeKernel((const void *)panel_kernel<T>, dim3(G), dim3(PT), args, 0, st));
+    // the CTA's rows of the panel live in shared memory when they fit
+    const size_t tile = sizeof(T) * (size_t)((Mp + G - 1) / G) * jb;
+    if (tile <= kPanelSmemMax)
+      ATLG_CHECK(cudaLaunchCooperativeKernel((const void *)panel_kernel<T, true>, dim3(G), dim3(PT), args, tile, st));
+    else
+      ATLG_CHECK(cudaLaunchCooperativeKernel((const void *)panel_kernel<T, false>, dim3(G), dim3(PT), args, 0, st));
     note_launch();
+    // the interchanges touch every other column: the side update must be done
+    if (side_pending) {
+      ATLG_CHECK(cudaStreamWaitEvent(st, ev_side, 0));
+      side_pending = false;
+    }
     const int c_from = k + jb;
     const int nl = (k + 31) / 32, nr = (N - c_from + 31) / 32;
     if (nl + nr > 0) {
@@ -406,11 +474,27 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     }
     if (c_from < N) {
       dev_trsm_llnu_block(A, lda, k, jb, A + k + (size_t)c_from * lda, lda, N - c_from, st);
-      if (k + jb < M)
-        gemm_any<T>(M - k - jb, N - c_from, jb, A + (k + jb) + (size_t)k * lda, lda, A + k + (size_t)c_from * lda,
-                    lda, A + (k + jb) + (size_t)c_from * lda, lda, st);
+      if (k + jb < M) {
+        const T *L21 = A + (k + jb) + (size_t)k * lda;
+        const int nxt = (c_from < MN) ? ((MN - c_from < NB) ? MN - c_from : NB) : 0;
+        if (lookahead && nxt > 0 && c_from + nxt < N) {
+          gemm_any<T>(M - k - jb, nxt, jb, L21, lda, A + k + (size_t)c_from * lda, lda,
+                      A + (k + jb) + (size_t)c_from * lda, lda, st);
+          ATLG_CHECK(cudaEventRecord(ev_ready, st));
+          ATLG_CHECK(cudaStreamWaitEvent(side, ev_ready, 0));
+          const int cb = c_from + nxt;
+          gemm_any<T>(M - k - jb, N - cb, jb, L21, lda, A + k + (size_t)cb * lda, lda, A + (k + jb) + (size_t)cb * lda,
+                      lda, side);
+          ATLG_CHECK(cudaEventRecord(ev_side, side));
+          side_pending = true;
+        } else {
+          gemm_any<T>(M - k - jb, N - c_from, jb, L21, lda, A + k + (size_t)c_from * lda, lda,
+                      A + (k + jb) + (size_t)c_from * lda, lda, st);
+        }
+      }
     }
   }
+  if (side_pending) ATLG_CHECK(cudaStreamWaitEvent(st, ev_side, 0));
 }
 
 void dev_dgetrf(int M, int N, double *A, int lda, int *ipiv, int *info, cudaStream_t st) {
