@@ -24,15 +24,17 @@
 // into C in FP64 with one exact power-of-two scaling, smallest diagonal
 // first.  K > 16384 is split into pieces accumulated through beta = 1.
 //
-// Kernel structure (one 128 x 128 tile of C per CTA, 6 warps):
-//   warp 0   TMA producer: 128 x 64 FP16 tiles of A_t and B_u (K-major,
-//            128-byte swizzle) into a 5-stage shared-memory ring;
-//   warp 1   allocates 256 tensor-memory columns (two 128-column FP32
+// Kernel structure (one 128 x 256 tile of C per CTA, 18 warps):
+//   warp 0   TMA producer: 128 x 64 and 256 x 64 FP16 tiles of A_t and B_u
+//            (K-major, 128-byte swizzle) into a 4-stage shared-memory ring
+//            (48 KB per stage: 512 MMA cycles of 128x256x16 cover the TMA
+//            latency);
+//   warp 1   allocates all 512 tensor-memory columns (two 256-column FP32
 //            accumulators) and issues the MMAs (one thread), committing to
 //            the ring's empty barriers and the accumulator-full barriers;
-//   warps 2-9 epilogue: warp w reads tensor-memory lane quarter w % 4;
-//            each thread owns one row of the tile and 64 of its columns
-//            (int32 sums).
+//   warps 2-17 epilogue: warp w reads tensor-memory lane quarter w % 4;
+//            each thread owns one row of the tile and 64 of its 256
+//            columns (int32 sums).
 // Every wait is bounded; a timeout sets the status word and an abort flag
 // that every role polls, so the CTA drains, frees its tensor memory and exits.
 #include <cuda_fp16.h>
@@ -49,10 +51,11 @@ namespace atlg {
 __device__ unsigned g_split_status;
 
 constexpr int kSliceBits = 7;
-constexpr int TM = 128, TN = 128, KB = 64, KCHUNK_BLOCKS = 16;   // 16 x 64 = 1024 = exact FP32 chunk
-constexpr int STAGES = 5;
-constexpr int STAGE_BYTES = (TM + TN) * KB * 2;                  // 32 KB
-constexpr int SPLIT_THREADS = 320;                             // 2 + 8 warps
+constexpr int TM = 128, TN = 256, KB = 64, KCHUNK_BLOCKS = 16;   // 16 x 64 = 1024 = exact FP32 chunk
+constexpr int STAGES = 4;
+constexpr int STAGE_BYTES = (TM + TN) * KB * 2;                  // 48 KB
+constexpr int EPI_WARPS = 16;
+constexpr int SPLIT_THREADS = 64 + EPI_WARPS * 32;             // 2 + 16 warps
 constexpr int EPI_COLS = 64;                                   // columns per epilogue thread
 constexpr int SPLIT_SMEM = STAGES * STAGE_BYTES + 1024 + 256;
 
@@ -165,7 +168,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1)
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < STAGES; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], 1); }
-    for (int i = 0; i < 2; ++i) { mbar_init(&acc_full[i], 1); mbar_init(&acc_empty[i], 8 * 32); }
+    for (int i = 0; i < 2; ++i) { mbar_init(&acc_full[i], 1); mbar_init(&acc_empty[i], EPI_WARPS * 32); }
     mbar_init(done, 1);
     *abort_flag = 0;
     fence_mbar_init();
@@ -174,7 +177,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1)
     const int col = n0 + c;
     colscale[c] = (col < p.N) ? ldexp(1.0, p.exB[col]) : 0.0;
   }
-  if (warp == 1) tmem_alloc(tmem_slot, 256);
+  if (warp == 1) tmem_alloc(tmem_slot, 2 * TN);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -239,9 +242,9 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1)
       wait_or_abort(done, 0, abort_flag);
     }
   } else {
-    // ------------------------------------------------ epilogue (warps 2..9)
+    // ------------------------------------------------ epilogue (warps 2..17)
     const int q = warp & 3;                 // tensor-memory lane quarter of this warp
-    const int h = (warp - 2) >> 2;          // column half of the tile
+    const int h = (warp - 2) >> 2;          // column quarter of the tile
     const int row = q * 32 + lane;
     const int gm = m0 + row;
     const bool row_ok = gm < p.M;
@@ -294,7 +297,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1)
   if (warp == 1) {
     __syncwarp();
     tc_fence_after();
-    tmem_dealloc(tmem, 256);
+    tmem_dealloc(tmem, 2 * TN);
   }
 }
 
