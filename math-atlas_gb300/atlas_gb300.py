@@ -28,7 +28,7 @@ EXPORTS = [
     "atlg_dgemm_dev_opts", "atlg_sgemm_dev", "atlg_dtrsm_dev", "atlg_dlaswp_dev", "atlg_dgetrf_dev",
     "atlg_sgetrf_dev", "atlg_dgetrs_dev", "atlg_launch_count", "atlg_prof_enable", "atlg_prof_collect",
     "atlg_probe_peaks", "dgesv_mixed", "dgesv_adjoint", "atlg_dgesv_mixed_dev", "atlg_dgesv_adjoint_dev",
-    "atlg_dlaswp_noalloc", "dgemm_split", "atlg_dgemm_split_dev",
+    "atlg_dlaswp_noalloc", "dgemm_split", "atlg_dgemm_split_dev", "atlg_sgemm_tf32x3_dev",
 ]
 
 _lib = None
@@ -86,6 +86,7 @@ def _declare(L):
         "atlg_dgesv_adjoint_dev": (_i, [_i, _i, _v, _i, _v, _v, _i, _v, _i, _v, _i, _v, _i, _v]),
         "dgemm_split": (None, [_i, _i, _i, _i, _i, _i, _d, _dp, _i, _dp, _i, _d, _dp, _i, _i]),
         "atlg_dgemm_split_dev": (_i, [_i, _i, _i, _i, _i, _d, _v, _i, _v, _i, _d, _v, _i, _i, _v]),
+        "atlg_sgemm_tf32x3_dev": (_i, [_i, _i, _i, _f, _v, _i, _v, _i, _v, _i, _v]),
         "atlg_launch_count": (C.c_ulonglong, []),
         "atlg_prof_enable": (None, [_i]),
         "atlg_prof_collect": (_i, [C.POINTER(_d), C.POINTER(_d), C.POINTER(_i)]),

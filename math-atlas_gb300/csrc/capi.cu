@@ -23,6 +23,7 @@
 #include "lu.cuh"
 #include "mixed.cuh"
 #include "split.cuh"
+#include "tf32.cuh"
 #include "trsm.cuh"
 
 using namespace atlg;
@@ -54,7 +55,8 @@ extern "C" void cblas_xerbla(int p, const char *rout, const char *form, ...) {
 namespace {
 
 void check_status(const char *rout) {
-  const unsigned s = gemm_status_read_and_clear() | lu_status_read_and_clear() | split_status_read_and_clear();
+  const unsigned s = gemm_status_read_and_clear() | lu_status_read_and_clear() | split_status_read_and_clear() |
+                     tf32_status_read_and_clear();
   if (s) {
     fprintf(stderr, "atlas_gb300: %s: device wait gave up (status 0x%x)\n", rout, s);
     fflush(stderr);
@@ -544,7 +546,21 @@ int atlg_num_sms(void) { return ctx().num_sms; }
 void *atlg_stream(void) { return ctx().stream; }
 
 unsigned atlg_status(void) {
-  return gemm_status_read_and_clear() | lu_status_read_and_clear() | split_status_read_and_clear();
+  return gemm_status_read_and_clear() | lu_status_read_and_clear() | split_status_read_and_clear() |
+         tf32_status_read_and_clear();
+}
+
+int atlg_sgemm_tf32x3_dev(int M, int N, int K, float alpha, const float *A, int lda, const float *B, int ldb,
+                          float *C, int ldc, void *stream) {
+  if (M < 0 || N < 0 || K < 0) return -1;
+  if (M == 0 || N == 0 || K == 0) return 0;
+  cudaStream_t st = stream_of(stream);
+  float *Ap = static_cast<float *>(ctx().buffer(kBufT0, sizeof(float) * tf32x3_packed_floats(M, K, false)));
+  float *Bp = static_cast<float *>(ctx().buffer(kBufT1, sizeof(float) * tf32x3_packed_floats(N, K, true)));
+  dev_sgemm_tf32x3_pack_a(M, K, A, lda, Ap, st);
+  dev_sgemm_tf32x3_pack_b(K, N, B, ldb, Bp, st);
+  dev_sgemm_tf32x3_packed(M, N, K, alpha, Ap, Bp, N, 0, C, ldc, st);
+  return 0;
 }
 
 int atlg_dgemm_split_dev(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda,

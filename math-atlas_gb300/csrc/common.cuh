@@ -151,6 +151,32 @@ __device__ __forceinline__ bool grid_barrier(unsigned *ctr, volatile unsigned *g
   return ok;
 }
 
+// Grid-wide barrier on a monotonic arrival counter: barrier number t (from
+// 1) of a grid of G co-resident CTAs completes when the counter reaches t*G.
+// One atomic per CTA and polling of the same word; no reset, no second
+// word.  Waits are bounded.
+__device__ __forceinline__ bool grid_barrier_count(unsigned *ctr, unsigned target, unsigned *status) {
+  __syncthreads();
+  bool ok = true;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(ctr, 1u);
+    volatile unsigned *vc = ctr;
+    unsigned i = 0;
+    while ((int)(*vc - target) < 0) {
+      if (++i > kGridPollLimit) {
+        atomicOr(status, kErrGridTimeout);
+        ok = false;
+        break;
+      }
+      if (i > 64) __nanosleep(20);
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok;
+}
+
 // ---------------------------------------------------------------- host
 struct Context;     // per-process library state (context.cuh)
 Context &ctx();

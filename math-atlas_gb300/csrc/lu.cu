@@ -33,6 +33,7 @@
 #include "context.cuh"
 #include "gemm.cuh"
 #include "lu.cuh"
+#include "tf32.cuh"
 #include "trsm.cuh"
 
 namespace atlg {
@@ -92,10 +93,18 @@ struct PanelRows {
   }
 };
 
+// Candidate records in global scratch, double buffered by column parity:
+// rec[(par*G + b)*RS + c] holds CTA b's candidate row (c < NB), then its
+// |a| (c = NB, negative: no candidate) and its row index (c = NB+1, exact in
+// T for any matrix this library can hold).  One record per CTA, so a
+// reader gets value, index and row of every candidate from one place.
+template <typename T> __host__ __device__ constexpr int rec_stride() { return sizeof(T) == 8 ? NB + 2 : NB + 4; }
+
 // Local candidate for column j among own rows [max(r0,j), r1); stage it.
 template <typename T, bool SM>
-__device__ void stage_candidate(const PanelRows<T, SM> &A, int j, int jb, int r0, int r1, int par, int G, T *cval,
-                                int *cidx, T *crow, T *jrow, BlockArgmax<T> &sh, int *s_idx) {
+__device__ void stage_candidate(const PanelRows<T, SM> &A, int j, int jb, int r0, int r1, int par, int G, T *rec,
+                                T *jrow, BlockArgmax<T> &sh, int *s_idx) {
+  constexpr int RS = rec_stride<T>();
   T best = T(-1);
   int bi = 0x7fffffff;
   const int lo = r0 > j ? r0 : j;
@@ -105,23 +114,24 @@ __device__ void stage_candidate(const PanelRows<T, SM> &A, int j, int jb, int r0
     if (a > best) { best = a; bi = i; }
   }
   block_argmax(best, bi, sh);
+  T *r = rec + ((size_t)par * G + blockIdx.x) * RS;
   if (threadIdx.x == 0) {
-    cval[par * G + blockIdx.x] = best;
-    cidx[par * G + blockIdx.x] = best >= T(0) ? bi : -1;
+    r[NB] = best;
+    r[NB + 1] = best >= T(0) ? (T)bi : T(-1);
     *s_idx = best >= T(0) ? bi : -1;
   }
   __syncthreads();
   const int ci = *s_idx;
   if (ci >= 0)
-    for (int c = threadIdx.x; c < jb; c += PT) crow[((size_t)par * G + blockIdx.x) * NB + c] = A.at(ci, c);
+    for (int c = threadIdx.x; c < jb; c += PT) r[c] = A.at(ci, c);
   if (j >= r0 && j < r1)
     for (int c = threadIdx.x; c < jb; c += PT) jrow[par * NB + c] = A.at(j, c);
 }
 
 template <typename T, bool SM>
 __global__ void __launch_bounds__(PT)
-    panel_kernel(T *Ag, int lda, int M, int jb, int koff, int *ipiv, int *info, T *cval, int *cidx, T *crow,
-                 T *jrow, unsigned *bar, int *perm) {
+    panel_kernel(T *Ag, int lda, int M, int jb, int koff, int *ipiv, int *info, T *rec, T *jrow, unsigned *bar,
+                 int *perm) {
   extern __shared__ __align__(16) unsigned char panel_dyn[];
   __shared__ BlockArgmax<T> sh;
   __shared__ T P[NB], J[NB];
@@ -152,16 +162,29 @@ __global__ void __launch_bounds__(PT)
     __syncthreads();
   }
 
-  stage_candidate(A, 0, jb, r0, r1, 0, G, cval, cidx, crow, jrow, sh, &s_idx);
+  constexpr int RS = rec_stride<T>();
+  // every CTA copies all G candidate records when they fit this buffer
+  constexpr int GATHER = (24 * 1024) / (RS * (int)sizeof(T));
+  __shared__ __align__(16) T gath[GATHER * RS];
+  const bool gather_all = G <= GATHER;
+
+  stage_candidate(A, 0, jb, r0, r1, 0, G, rec, jrow, sh, &s_idx);
   for (int j = 0; j < jb; ++j) {
     const int par = j & 1;
-    if (!grid_barrier(&bar[0], &bar[1], G, &g_lu_status)) return;
+    if (!grid_barrier_count(&bar[0], (unsigned)(koff + j + 1) * (unsigned)G, &g_lu_status)) return;
+    const T *rp = rec + (size_t)par * G * RS;
     // ---- global winner (identical in every CTA) ----
+    if (gather_all) {
+      // one round trip: every record (value, index, row) and row j
+      for (int e = threadIdx.x; e < G * RS; e += PT) gath[e] = rp[e];
+      for (int c = threadIdx.x; c < jb; c += PT) J[c] = jrow[par * NB + c];
+      __syncthreads();
+    }
     if (threadIdx.x < 32) {
       T best = T(-1);
       int bb = 0x7fffffff;
       for (int b = threadIdx.x; b < G; b += 32) {
-        const T v = cval[par * G + b];
+        const T v = gather_all ? gath[b * RS + NB] : rp[(size_t)b * RS + NB];
         if (v > best) { best = v; bb = b; }
       }
       for (int o = 16; o > 0; o >>= 1) {
@@ -170,7 +193,8 @@ __global__ void __launch_bounds__(PT)
         if (ov > best || (ov == best && ob < bb)) { best = ov; bb = ob; }
       }
       if (threadIdx.x == 0) {
-        const int p = (bb < G && best > T(0)) ? cidx[par * G + bb] : -1;
+        int p = -1;
+        if (bb < G && best > T(0)) p = (int)(gather_all ? gath[bb * RS + NB + 1] : rp[(size_t)bb * RS + NB + 1]);
         s_zero = (p < 0);
         s_p = (p < 0) ? j : p;
         s_piv = best;
@@ -188,8 +212,12 @@ __global__ void __launch_bounds__(PT)
     if (!zero) {
       const int wb = s_idx;
       for (int c = threadIdx.x; c < jb; c += PT) {
-        P[c] = crow[((size_t)par * G + wb) * NB + c];
-        J[c] = jrow[par * NB + c];
+        if (gather_all) {
+          P[c] = gath[wb * RS + c];
+        } else {
+          P[c] = rp[(size_t)wb * RS + c];
+          J[c] = jrow[par * NB + c];
+        }
       }
       __syncthreads();
       const T pv = P[j];
@@ -214,24 +242,22 @@ __global__ void __launch_bounds__(PT)
       if (p != j && p >= r0 && p < r1)
         for (int c = threadIdx.x; c < j; c += PT) A.at(p, c) = J[c];
       __syncthreads();
-      // pass 2: rank-1 update of columns j+1..jb-1 in own rows i > j
-      const int ncol = jb - j - 1;
-      const int nrow = r1 - lo;
-      if (ncol > 0 && nrow > 0) {
-        const long tot = (long)ncol * nrow;
-        for (long e = threadIdx.x; e < tot; e += PT) {
-          const int i = lo + (int)(e % nrow);
-          const int c = j + 1 + (int)(e / nrow);
-          if (i == j) continue;
-          const T l = (SM || big) ? A.at(i, j) : lbuf[i - r0];
-          const T src = (i == p) ? J[c] : A.at(i, c);
-          A.at(i, c) = src - l * P[c];
+      // pass 2: rank-1 update of columns j+1..jb-1 in own rows i > j; a
+      // thread per row walks the columns (consecutive threads touch
+      // consecutive rows of a column, no index division)
+      for (int i = lo + threadIdx.x; i < r1; i += PT) {
+        if (i == j) continue;
+        const T l = (SM || big) ? A.at(i, j) : lbuf[i - r0];
+        if (i == p) {
+          for (int c = j + 1; c < jb; ++c) A.at(i, c) = J[c] - l * P[c];
+        } else {
+#pragma unroll 4
+          for (int c = j + 1; c < jb; ++c) A.at(i, c) -= l * P[c];
         }
       }
       __syncthreads();
     }
-    if (j + 1 < jb)
-      stage_candidate(A, j + 1, jb, r0, r1, (j + 1) & 1, G, cval, cidx, crow, jrow, sh, &s_idx);
+    if (j + 1 < jb) stage_candidate(A, j + 1, jb, r0, r1, (j + 1) & 1, G, rec, jrow, sh, &s_idx);
   }
   if (SM) {
     __syncthreads();
@@ -407,8 +433,22 @@ void gemm_any<float>(int M, int N, int K, const float *A, int lda, const float *
   dev_sgemm(kNoTrans, kNoTrans, M, N, K, -1.0f, A, lda, B, ldb, 1.0f, C, ldc, st);
 }
 
+// Trailing update A22 -= L21 * U12 for columns [c0, c0+n) of the U12 block
+// (first column c_from): the FFMA/DFMA GEMM, or for the mixed solver's FP32
+// factor the 3xTF32 tensor-core update on panels packed once per step.
 template <typename T>
-static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaStream_t st) {
+static void trailing_update(bool tc, int m, int n, int jb, const T *L21, const T *U12, T *C, int lda, int boff,
+                            int ntot, const float *Ap, const float *Bp, cudaStream_t st) {
+  if (m <= 0 || n <= 0) return;
+  if (tc) {
+    dev_sgemm_tf32x3_packed(m, n, jb, -1.0f, Ap, Bp, ntot, boff, (float *)C + (size_t)boff * lda, lda, st);
+    return;
+  }
+  gemm_any<T>(m, n, jb, L21, lda, U12 + (size_t)boff * lda, lda, C + (size_t)boff * lda, lda, st);
+}
+
+template <typename T>
+static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaStream_t st, bool tc = false) {
   ATLG_CHECK(cudaMemsetAsync(info, 0, sizeof(int), st));
   if (M <= 0 || N <= 0) return;
   Context &c = ctx();
@@ -429,15 +469,13 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
   // at least a few rows per CTA for the tallest panel
   if (G > (M + 7) / 8) G = (M + 7) / 8;
   if (G < 1) G = 1;
-  // one scratch block: cval[2G] T, crow[2G*NB] T, jrow[2NB] T, cidx[2G] int, bar[2], perm[1+4NB]
-  const size_t tbytes = sizeof(T) * ((size_t)2 * G + (size_t)2 * G * NB + 2 * NB);
-  const size_t ibytes = sizeof(int) * ((size_t)2 * G + 2 + 1 + 4 * NB);
+  // one scratch block: rec[2G][RS] T, jrow[2NB] T, bar[2], perm[1+4NB]
+  const size_t tbytes = sizeof(T) * ((size_t)2 * G * rec_stride<T>() + 2 * NB);
+  const size_t ibytes = sizeof(int) * ((size_t)2 + 1 + 4 * NB);
   unsigned char *scr = static_cast<unsigned char *>(c.buffer(kBufW0, tbytes + ibytes + 64));
-  T *cval = reinterpret_cast<T *>(scr);
-  T *crow = cval + 2 * G;
-  T *jrow = crow + (size_t)2 * G * NB;
-  int *cidx = reinterpret_cast<int *>(scr + ((tbytes + 15) & ~size_t(15)));
-  unsigned *bar = reinterpret_cast<unsigned *>(cidx + 2 * G);
+  T *rec = reinterpret_cast<T *>(scr);
+  T *jrow = rec + (size_t)2 * G * rec_stride<T>();
+  unsigned *bar = reinterpret_cast<unsigned *>(scr + ((tbytes + 15) & ~size_t(15)));
   int *perm = reinterpret_cast<int *>(bar + 2);
   ATLG_CHECK(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st));
   ATLG_CHECK(cudaFuncSetAttribute(panel_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -452,7 +490,7 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     int Mp = M - k;
     int *ipk = ipiv + k;
     int koff = k;
-    void *args[] = {&Ap, (void *)&lda, &Mp, (void *)&jb, &koff, &ipk, &info, &cval, &cidx, &crow, &jrow, &bar, &perm};
+    void *args[] = {&Ap, (void *)&lda, &Mp, (void *)&jb, &koff, &ipk, &info, &rec, &jrow, &bar, &perm};
     // the CTA's rows of the panel live in shared memory when they fit
     const size_t tile = sizeof(T) * (size_t)((Mp + G - 1) / G) * jb;
     if (tile <= kPanelSmemMax)
@@ -475,21 +513,28 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     if (c_from < N) {
       dev_trsm_llnu_block(A, lda, k, jb, A + k + (size_t)c_from * lda, lda, N - c_from, st);
       if (k + jb < M) {
+        const int m = M - k - jb, ntot = N - c_from;
         const T *L21 = A + (k + jb) + (size_t)k * lda;
+        const T *U12 = A + k + (size_t)c_from * lda;
+        T *C = A + (k + jb) + (size_t)c_from * lda;
+        const bool use_tc = tc && m >= 256 && ntot >= 128;
+        float *Ap = nullptr, *Bp = nullptr;
+        if (use_tc) {
+          Ap = static_cast<float *>(c.buffer(kBufT0, sizeof(float) * tf32x3_packed_floats(m, jb, false)));
+          Bp = static_cast<float *>(c.buffer(kBufT1, sizeof(float) * tf32x3_packed_floats(ntot, jb, true)));
+          dev_sgemm_tf32x3_pack_a(m, jb, (const float *)L21, lda, Ap, st);
+          dev_sgemm_tf32x3_pack_b(jb, ntot, (const float *)U12, lda, Bp, st);
+        }
         const int nxt = (c_from < MN) ? ((MN - c_from < NB) ? MN - c_from : NB) : 0;
         if (lookahead && nxt > 0 && c_from + nxt < N) {
-          gemm_any<T>(M - k - jb, nxt, jb, L21, lda, A + k + (size_t)c_from * lda, lda,
-                      A + (k + jb) + (size_t)c_from * lda, lda, st);
+          trailing_update<T>(use_tc, m, nxt, jb, L21, U12, C, lda, 0, ntot, Ap, Bp, st);
           ATLG_CHECK(cudaEventRecord(ev_ready, st));
           ATLG_CHECK(cudaStreamWaitEvent(side, ev_ready, 0));
-          const int cb = c_from + nxt;
-          gemm_any<T>(M - k - jb, N - cb, jb, L21, lda, A + k + (size_t)cb * lda, lda, A + (k + jb) + (size_t)cb * lda,
-                      lda, side);
+          trailing_update<T>(use_tc, m, ntot - nxt, jb, L21, U12, C, lda, nxt, ntot, Ap, Bp, side);
           ATLG_CHECK(cudaEventRecord(ev_side, side));
           side_pending = true;
         } else {
-          gemm_any<T>(M - k - jb, N - c_from, jb, L21, lda, A + k + (size_t)c_from * lda, lda,
-                      A + (k + jb) + (size_t)c_from * lda, lda, st);
+          trailing_update<T>(use_tc, m, ntot, jb, L21, U12, C, lda, 0, ntot, Ap, Bp, st);
         }
       }
     }
@@ -502,6 +547,9 @@ void dev_dgetrf(int M, int N, double *A, int lda, int *ipiv, int *info, cudaStre
 }
 void dev_sgetrf(int M, int N, float *A, int lda, int *ipiv, int *info, cudaStream_t st) {
   getrf_impl<float>(M, N, A, lda, ipiv, info, st);
+}
+void dev_sgetrf_tc(int M, int N, float *A, int lda, int *ipiv, int *info, cudaStream_t st) {
+  getrf_impl<float>(M, N, A, lda, ipiv, info, st, true);
 }
 
 // ------------------------------------------------------------------ getrs

@@ -9,6 +9,10 @@ namespace atlg {
 // (device int: 0, or the 1-based index of the first exactly-zero pivot).
 void dev_dgetrf(int M, int N, double *A, int lda, int *ipiv, int *info, cudaStream_t st);
 void dev_sgetrf(int M, int N, float *A, int lda, int *ipiv, int *info, cudaStream_t st);
+// FP32 LU whose trailing updates run on tcgen05 tensor cores in 3xTF32 (the
+// mixed-precision solver's factor; pivots may differ from the FFMA sgetrf
+// at near-ties).
+void dev_sgetrf_tc(int M, int N, float *A, int lda, int *ipiv, int *info, cudaStream_t st);
 // ATL_laswp semantics on device data; rows [0, nrows) may move (nrows > every pivot).
 void dev_dlaswp(int N, double *A, int lda, int K1, int K2, const int *ipiv, int inci, int nrows, cudaStream_t st);
 void dev_slaswp(int N, float *A, int lda, int K1, int K2, const int *ipiv, int inci, int nrows, cudaStream_t st);

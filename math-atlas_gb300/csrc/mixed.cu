@@ -11,8 +11,9 @@
 // with eps = 2^-53, at most 30 refinement steps; refinement also stops as
 // stalled when the residual fails to halve twice in a row.
 //
-// GB300 mapping: the FP32 LU is the FFMA path of lu.cu (sgetrf) and the
-// FP32 solves are its sgetrs; the FP64 residual r = b - A x is one DGEMM (or
+// GB300 mapping: the FP32 LU is lu.cu's factorization with its trailing
+// updates on tcgen05 tensor cores in 3xTF32 (tf32.cu), and the FP32 solves
+// are its sgetrs; the FP64 residual r = b - A x is one DGEMM (or
 // DGEMV for one right-hand side) on the unmodified FP64 A; conversions and
 // norms are elementwise kernels.  All FP64 work on the GPU is the residual,
 // the update x += d and the norms; the O(n^3) work is FP32.
@@ -144,7 +145,7 @@ int dev_dgesv_mixed(int n, int nrhs, double *A, int lda, int *ipiv, const double
   ATLG_CHECK(cudaMemsetAsync(dinfo, 0, 2 * sizeof(int), st));
   d2s_kernel<<<grid_for((long)n * n), 256, 0, st>>>(n, n, A, lda, S, lds, dovf);
   note_launch();
-  dev_sgetrf(n, n, S, lds, ipiv, dinfo, st);
+  dev_sgetrf_tc(n, n, S, lds, ipiv, dinfo, st);
   int hinfo[2] = {0, 0};
   ATLG_CHECK(cudaMemcpyAsync(hinfo, dinfo, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
   ATLG_CHECK(cudaStreamSynchronize(st));

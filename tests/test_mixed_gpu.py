@@ -65,3 +65,22 @@ def test_dgesv_mixed_singular_reports_info(gb):
     b = np.ones((n, 1), order="F")
     info, berr, ferr, iters, status = gb.dgesv_mixed(A, np.zeros(n, dtype=np.int32), b, X)
     assert info == 6 and status == 2
+
+
+def test_tf32x3_update_is_fp32_accurate(gb):
+    """The mixed solver's factor update (3xTF32 on tcgen05) against an FP64
+    product: error at FP32 level, far below single-pass TF32 (~1e-3)."""
+    torch = pytest.importorskip("torch")
+    for (M, N, K) in ((1000, 700, 64), (513, 300, 200), (256, 128, 64)):
+        g = torch.Generator(device="cuda").manual_seed(M + N)
+        A = torch.randn(K, M, device="cuda", generator=g)     # column-major M x K storage
+        B = torch.randn(N, K, device="cuda", generator=g)     # column-major K x N storage
+        C = torch.randn(N, M, device="cuda", generator=g)
+        ref = C.double().T - (A.double().T @ B.double().T)
+        gb.lib().atlg_sgemm_tf32x3_dev(M, N, K, -1.0, A.data_ptr(), M, B.data_ptr(), K, C.data_ptr(), M, None)
+        torch.cuda.synchronize()
+        # relative to the result's magnitude: FP32 rounding is 6e-8, the
+        # 3xTF32 split adds ~2^-22; single-pass TF32 would be ~1e-3
+        err = (C.double().T - ref).abs().max().item() / ref.abs().max().item()
+        assert err < 1e-5, (M, N, K, err)
+        assert gb.lib().atlg_status() == 0
