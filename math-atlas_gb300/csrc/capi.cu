@@ -56,7 +56,7 @@ namespace {
 
 void check_status(const char *rout) {
   const unsigned s = gemm_status_read_and_clear() | lu_status_read_and_clear() | split_status_read_and_clear() |
-                     tf32_status_read_and_clear();
+                     tf32_status_read_and_clear() | trsv_status_read_and_clear();
   if (s) {
     fprintf(stderr, "atlas_gb300: %s: device wait gave up (status 0x%x)\n", rout, s);
     fflush(stderr);
@@ -547,7 +547,7 @@ void *atlg_stream(void) { return ctx().stream; }
 
 unsigned atlg_status(void) {
   return gemm_status_read_and_clear() | lu_status_read_and_clear() | split_status_read_and_clear() |
-         tf32_status_read_and_clear();
+         tf32_status_read_and_clear() | trsv_status_read_and_clear();
 }
 
 int atlg_sgemm_tf32x3_dev(int M, int N, int K, float alpha, const float *A, int lda, const float *B, int ldb,

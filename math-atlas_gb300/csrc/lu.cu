@@ -412,6 +412,32 @@ static void laswp_impl(int N, T *A, int lda, int K1, int K2, const int *ipiv, in
   ATLG_CHECK(cudaGetLastError());
 }
 
+// Row permutation of a factorization: perm[i] = source row of row i after
+// the interchanges ipiv[0..n) are applied in order (ATL_laswp forward), so
+// that the forward interchange of one vector is y[i] = b[perm[i]].
+void dev_perm_from_ipiv(const int *ipiv, int n, int *perm, cudaStream_t st) {
+  const int use_smem = n <= kPermSmemRows;
+  ATLG_CHECK(cudaFuncSetAttribute(laswp_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  laswp_perm_kernel<<<1, 1024, use_smem ? sizeof(int) * (size_t)n : 0, st>>>(ipiv, 0, n, 1, perm, n, use_smem);
+  note_launch();
+  ATLG_CHECK(cudaGetLastError());
+}
+
+template <typename T>
+__global__ void permute_vec_kernel(int n, const int *perm, const T *in, T *out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = in[perm[i]];
+}
+
+// x <- (LU)^-1 P x for one FP32 right-hand side with a precomputed permutation
+// (the refinement loop solves with the same factor many times).
+void dev_sgetrs_perm(int n, const float *LU, int lda, const int *perm, float *x, float *tmp, cudaStream_t st) {
+  permute_vec_kernel<float><<<(n + 255) / 256, 256, 0, st>>>(n, perm, x, tmp);
+  ATLG_CHECK(cudaMemcpyAsync(x, tmp, sizeof(float) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+  note_launch();
+  dev_strsv(kLower, kNoTrans, kUnit, n, LU, lda, x, st);
+  dev_strsv(kUpper, kNoTrans, kNonUnit, n, LU, lda, x, st);
+}
+
 void dev_dlaswp(int N, double *A, int lda, int K1, int K2, const int *ipiv, int inci, int nrows, cudaStream_t st) {
   laswp_impl<double>(N, A, lda, K1, K2, ipiv, inci, nrows, st);
 }
@@ -573,6 +599,23 @@ static void getrs_impl(int order, int trans, int N, int NRHS, const T *A, int ld
                        cudaStream_t st) {
   if (!N || !NRHS) return;
   // laswp over the N "rows" of B in the column-major sense, as the reference calls it
+  if (order == kColMajor && NRHS == 1) {
+    // one right-hand side: single-launch look-back TRSV for each factor
+    auto trsv = [&](int uplo, int ta, int diag) {
+      if (sizeof(T) == 8) dev_dtrsv(uplo, ta, diag, N, (const double *)A, lda, (double *)B, st);
+      else dev_strsv(uplo, ta, diag, N, (const float *)A, lda, (float *)B, st);
+    };
+    if (trans == kNoTrans) {
+      laswp_impl<T>(1, B, ldb, 0, N, ipiv, 1, N, st);
+      trsv(kLower, kNoTrans, kUnit);
+      trsv(kUpper, kNoTrans, kNonUnit);
+    } else {
+      trsv(kUpper, trans, kNonUnit);
+      trsv(kLower, trans, kUnit);
+      laswp_impl<T>(1, B, ldb, 0, N, ipiv, -1, N, st);
+    }
+    return;
+  }
   if (order == kColMajor) {
     if (trans == kNoTrans) {
       laswp_impl<T>(NRHS, B, ldb, 0, N, ipiv, 1, N, st);

@@ -21,6 +21,8 @@ void dev_dgetrs(int order, int trans, int N, int NRHS, const double *A, int lda,
                 cudaStream_t st);
 void dev_sgetrs(int order, int trans, int N, int NRHS, const float *A, int lda, const int *ipiv, float *B, int ldb,
                 cudaStream_t st);
+void dev_perm_from_ipiv(const int *ipiv, int n, int *perm, cudaStream_t st);
+void dev_sgetrs_perm(int n, const float *LU, int lda, const int *perm, float *x, float *tmp, cudaStream_t st);
 unsigned lu_status_read_and_clear();
 
 }  // namespace atlg

@@ -153,10 +153,23 @@ int dev_dgesv_mixed(int n, int nrhs, double *A, int lda, int *ipiv, const double
 
   int iter = 0;
   if (!fallback) {
+    // one right-hand side: the row permutation is computed once and every
+    // solve is a gather plus two single-launch triangular solves
+    int *perm = nullptr;
+    float *tmp32 = nullptr;
+    if (nrhs == 1) {
+      perm = static_cast<int *>(c.buffer(kBufV1, sizeof(int) * (size_t)n + sizeof(float) * (size_t)n + 256));
+      tmp32 = reinterpret_cast<float *>(perm + ((n + 63) & ~63));
+      dev_perm_from_ipiv(ipiv, n, perm, st);
+    }
+    auto solve32 = [&](float *v) {
+      if (nrhs == 1) dev_sgetrs_perm(n, S, lds, perm, v, tmp32, st);
+      else dev_sgetrs(kColMajor, kNoTrans, n, nrhs, S, lds, ipiv, v, lds, st);
+    };
     // x0 = (A32)^-1 b in FP32, promoted
     d2s_kernel<<<grid_for((long)n * nrhs), 256, 0, st>>>(n, nrhs, B, ldb, R32, lds, dovf);
     note_launch();
-    dev_sgetrs(kColMajor, kNoTrans, n, nrhs, S, lds, ipiv, R32, lds, st);
+    solve32(R32);
     s2d_kernel<<<grid_for((long)n * nrhs), 256, 0, st>>>(n, nrhs, R32, lds, X, ldx);
     note_launch();
     double prev = INFINITY;
@@ -188,7 +201,7 @@ int dev_dgesv_mixed(int n, int nrhs, double *A, int lda, int *ipiv, const double
       // d = (A32)^-1 r in FP32; x += d
       d2s_kernel<<<grid_for((long)n * nrhs), 256, 0, st>>>(n, nrhs, R, ldr, R32, lds, dovf);
       note_launch();
-      dev_sgetrs(kColMajor, kNoTrans, n, nrhs, S, lds, ipiv, R32, lds, st);
+      solve32(R32);
       axpy_s2d_kernel<<<grid_for((long)n * nrhs), 256, 0, st>>>(n, nrhs, R32, lds, X, ldx);
       note_launch();
       {

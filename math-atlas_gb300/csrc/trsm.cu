@@ -204,3 +204,159 @@ void dev_trsm_llnu_block(const float *A, int lda, int k, int n, float *B, int ld
 }
 
 }  // namespace atlg
+
+// ---------------------------------------------------------------- TRSV
+// One right-hand side (the solve after a factorization): a single launch
+// with one CTA per 64-row block.  CTAs take blocks in solve order from an
+// atomic ticket; a CTA folds in the contribution of every earlier block as
+// soon as that block's flag is published, then solves its diagonal block
+// (warp substitution, reciprocal diagonal) and publishes its piece of x.  A
+// CTA only waits on blocks whose tickets were taken before its own, so every
+// block it waits for is running or done; every wait is bounded.
+namespace atlg {
+
+__device__ unsigned g_trsv_status;
+constexpr int TV_B = 64;
+constexpr unsigned kFlagPollLimit = 1u << 24;
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    trsv_lookback_kernel(int n, const T *__restrict__ A, int lda, int ta, int lower, int unit, T *x, int *flags,
+                         int *ticket) {
+  __shared__ T tri[TV_B][TV_B + 1];
+  __shared__ T rinv[TV_B];
+  __shared__ T part[8][TV_B];
+  __shared__ int s_b, s_fail;
+  const int nb = (n + TV_B - 1) / TV_B;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    const int t = atomicAdd(ticket, 1);
+    s_b = lower ? t : nb - 1 - t;
+    s_fail = 0;
+  }
+  __syncthreads();
+  const int b = s_b;
+  const int r0 = b * TV_B;
+  const int nr = (n - r0 < TV_B) ? n - r0 : TV_B;
+  // diagonal block of op(A), reciprocal diagonal
+  for (int e = threadIdx.x; e < nr * nr; e += 256) {
+    const int i = e % nr, k = e / nr;
+    tri[i][k] = (ta == kNoTrans) ? A[(r0 + i) + (size_t)(r0 + k) * lda] : A[(r0 + k) + (size_t)(r0 + i) * lda];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nr; i += 256) rinv[i] = unit ? T(1) : T(1) / tri[i][i];
+  // contributions of earlier blocks: warp w takes columns k = c0 + w, w+8, ...
+  T acc0 = T(0), acc1 = T(0);              // rows lane, lane+32 (op(A) = A)
+  T accT[8];                               // rows w*8..w*8+7, lanes over k (op(A) = A^T)
+#pragma unroll
+  for (int q = 0; q < 8; ++q) accT[q] = T(0);
+  for (int s = 0; s < nb - 1; ++s) {
+    const int c = lower ? s : nb - 1 - s;
+    if (lower ? c >= b : c <= b) break;
+    if (threadIdx.x == 0) {
+      unsigned i = 0;
+      while (atomicAdd(&flags[c], 0) == 0) {
+        if (++i > kFlagPollLimit) { atomicOr(&g_trsv_status, kErrGridTimeout); s_fail = 1; break; }
+        if (i > 32) __nanosleep(64);
+      }
+      __threadfence();
+    }
+    __syncthreads();
+    if (s_fail) return;
+    const int c0 = c * TV_B;
+    const int nc = (n - c0 < TV_B) ? n - c0 : TV_B;
+    if (ta == kNoTrans) {
+      for (int k = w; k < nc; k += 8) {
+        const T xk = __ldcg(x + c0 + k);          // published by another CTA: read at L2
+        const T *col = A + r0 + (size_t)(c0 + k) * lda;
+        if (lane < nr) acc0 = fma(col[lane], xk, acc0);
+        if (lane + 32 < nr) acc1 = fma(col[lane + 32], xk, acc1);
+      }
+    } else {
+      for (int k = lane; k < nc; k += 32) {
+        const T xk = __ldcg(x + c0 + k);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int i = w * 8 + q;
+          if (i < nr) accT[q] = fma(A[(c0 + k) + (size_t)(r0 + i) * lda], xk, accT[q]);
+        }
+      }
+    }
+  }
+  // gather the partial sums: part[w][row]
+  if (ta == kNoTrans) {
+    part[w][lane] = acc0;
+    part[w][lane + 32] = acc1;
+  } else {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      T v = accT[q];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) part[0][w * 8 + q] = v;
+    }
+  }
+  __syncthreads();
+  if (w == 0) {
+    T y0 = T(0), y1 = T(0);
+    if (ta == kNoTrans) {
+      for (int q = 0; q < 8; ++q) { y0 += part[q][lane]; y1 += part[q][lane + 32]; }
+    } else {
+      y0 = part[0][lane];
+      y1 = part[0][lane + 32];
+    }
+    T x0 = lane < nr ? x[r0 + lane] - y0 : T(0);
+    T x1 = lane + 32 < nr ? x[r0 + lane + 32] - y1 : T(0);
+    if (lower) {
+      for (int k = 0; k < nr; ++k) {
+        T bk = __shfl_sync(0xffffffffu, k < 32 ? x0 : x1, k & 31);
+        bk *= rinv[k];
+        if (lane == (k & 31)) { if (k < 32) x0 = bk; else x1 = bk; }
+        if (lane > k && lane < nr) x0 -= tri[lane][k] * bk;
+        if (lane + 32 > k && lane + 32 < nr) x1 -= tri[lane + 32][k] * bk;
+      }
+    } else {
+      for (int k = nr - 1; k >= 0; --k) {
+        T bk = __shfl_sync(0xffffffffu, k < 32 ? x0 : x1, k & 31);
+        bk *= rinv[k];
+        if (lane == (k & 31)) { if (k < 32) x0 = bk; else x1 = bk; }
+        if (lane < k) x0 -= tri[lane][k] * bk;
+        if (lane + 32 < k) x1 -= tri[lane + 32][k] * bk;
+      }
+    }
+    if (lane < nr) x[r0 + lane] = x0;
+    if (lane + 32 < nr) x[r0 + lane + 32] = x1;
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) atomicExch(&flags[b], 1);
+  }
+}
+
+// op(A) x = x for one right-hand side (incx = 1), cblas Uplo/Trans/Diag.
+template <typename T>
+static void trsv_impl(int uplo, int tA, int diag, int n, const T *A, int lda, T *x, cudaStream_t st) {
+  if (n <= 0) return;
+  const int ta = (tA == kNoTrans) ? kNoTrans : kTrans;
+  const int lower = ((uplo == kLower) != (ta != kNoTrans)) ? 1 : 0;
+  const int nb = (n + TV_B - 1) / TV_B;
+  int *w = static_cast<int *>(ctx().buffer(kBufV0, sizeof(int) * (size_t)(nb + 32)));
+  ATLG_CHECK(cudaMemsetAsync(w, 0, sizeof(int) * (size_t)(nb + 32), st));
+  trsv_lookback_kernel<T><<<nb, 256, 0, st>>>(n, A, lda, ta, lower, diag == kUnit ? 1 : 0, x, w + 32, w);
+  note_launch();
+  ATLG_CHECK(cudaGetLastError());
+}
+
+void dev_dtrsv(int uplo, int ta, int diag, int n, const double *A, int lda, double *x, cudaStream_t st) {
+  trsv_impl<double>(uplo, ta, diag, n, A, lda, x, st);
+}
+void dev_strsv(int uplo, int ta, int diag, int n, const float *A, int lda, float *x, cudaStream_t st) {
+  trsv_impl<float>(uplo, ta, diag, n, A, lda, x, st);
+}
+
+unsigned trsv_status_read_and_clear() {
+  unsigned v = 0, z = 0;
+  ATLG_CHECK(cudaMemcpyFromSymbol(&v, g_trsv_status, sizeof(v)));
+  if (v) ATLG_CHECK(cudaMemcpyToSymbol(g_trsv_status, &z, sizeof(z)));
+  return v;
+}
+
+}  // namespace atlg

@@ -13,4 +13,9 @@ void dev_strsm(int side, int uplo, int ta, int diag, int M, int N, float alpha, 
 void dev_trsm_llnu_block(const double *A, int lda, int k, int n, double *B, int ldb, int ncols, cudaStream_t st);
 void dev_trsm_llnu_block(const float *A, int lda, int k, int n, float *B, int ldb, int ncols, cudaStream_t st);
 
+// op(A) x = x for one right-hand side, one launch (look-back over 64-row blocks).
+void dev_dtrsv(int uplo, int ta, int diag, int n, const double *A, int lda, double *x, cudaStream_t st);
+void dev_strsv(int uplo, int ta, int diag, int n, const float *A, int lda, float *x, cudaStream_t st);
+unsigned trsv_status_read_and_clear();
+
 }  // namespace atlg

@@ -139,3 +139,20 @@ def test_dgetrf_full_size_8192(gb, ora):
     normA = float(torch.from_numpy(np.ascontiguousarray(ora.gegen(n, n, seed).T)).abs().sum(dim=1).max())
     resid = float(D.abs().sum(dim=0).max()) / (normA * np.finfo(float).eps * n)
     assert resid <= LU_THRESH, resid
+
+
+@pytest.mark.parametrize("n", [1, 63, 64, 65, 1000, 3001])
+@pytest.mark.parametrize("trans", [111, 112])
+def test_dgetrs_one_rhs_lookback_trsv(gb, ora, n, trans):
+    """One right-hand side takes the single-launch look-back triangular
+    solves; edge sizes around the 64-row block."""
+    A = ora.gegen(n, n, n * n + n)
+    ipiv = np.zeros(n, dtype=np.int32)
+    assert gb.clapack_dgetrf(102, n, n, A, n, ipiv) == 0
+    b0 = ora.gegen(n, 1, 5 + n)
+    bg = b0.copy(order="F")
+    gb.clapack_dgetrs(102, trans, n, 1, A, n, ipiv, bg, n)
+    bo = b0.copy(order="F")
+    ora.lib().ora_dgetrs(102, trans, n, 1, A, n, ipiv, bo, n)
+    assert np.allclose(bg, bo, rtol=1e-9, atol=1e-9 * np.abs(bo).max())
+    assert gb.status() == 0
