@@ -276,18 +276,26 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1)
           mbar_arrive(&acc_empty[buf]);
         }
       if (!ok) break;
-      // diagonal d complete: C (+)= alpha 2^(ea - 7(d+2)) acc 2^(eb)
+      // diagonal d complete: C (+)= alpha 2^(ea - 7(d+2)) acc 2^(eb); C is
+      // read in batches of 8 independent loads before any store
       const double fr = ldexp(rowpow, rexp - kSliceBits * (d + 2));
+      const bool need_old = !first || p.beta != 0.0;
+      const double cscale = first ? p.beta : 1.0;
 #pragma unroll
-      for (int c = 0; c < EPI_COLS; ++c) {
-        const int gn = n0 + h * EPI_COLS + c;
-        if (row_ok && gn < p.N) {
-          double *cp = p.C + gm + (size_t)gn * p.ldc;
-          const double v = (double)acc[c] * fr * colscale[h * EPI_COLS + c];
-          if (first) *cp = (p.beta == 0.0) ? v : fma(p.beta, *cp, v);
-          else *cp += v;
+      for (int c0 = 0; c0 < EPI_COLS; c0 += 8) {
+        double old[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int gn = n0 + h * EPI_COLS + c0 + j;
+          old[j] = (need_old && row_ok && gn < p.N) ? p.C[gm + (size_t)gn * p.ldc] : 0.0;
         }
-        acc[c] = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int gn = n0 + h * EPI_COLS + c0 + j;
+          const double v = (double)acc[c0 + j] * fr * colscale[h * EPI_COLS + c0 + j];
+          if (row_ok && gn < p.N) p.C[gm + (size_t)gn * p.ldc] = need_old ? fma(cscale, old[j], v) : v;
+          acc[c0 + j] = 0;
+        }
       }
       first = false;
     }

@@ -147,6 +147,20 @@ __global__ void __launch_bounds__(XT_THREADS, 2)
     const int h = (warp - 2) >> 2;            // which 128-column half
     const int row = q * 32 + lane;
     const int gm = m0 + row;
+    const bool rok = gm < p.M;
+    float *crow = p.C + gm;
+    // C is read in batches of 16 independent loads (the first batch before
+    // the accumulator is ready), so the read-modify-write is bandwidth-
+    // rather than latency-bound
+    float cv[16];
+    auto load_batch = [&](int cb) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int gn = n0 + h * 128 + cb * 16 + j;
+        cv[j] = (rok && gn < p.N) ? __ldcs(crow + (size_t)gn * p.ldc) : 0.f;
+      }
+    };
+    load_batch(0);
     int okw = 1;
     if (lane == 0) okw = xt_wait(acc_full, 0, abort_flag) ? 1 : 0;
     okw = __shfl_sync(0xffffffffu, okw, 0);
@@ -157,15 +171,14 @@ __global__ void __launch_bounds__(XT_THREADS, 2)
         uint32_t r[16];
         tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * 128 + cb * 16), r);
         tmem_wait_ld();
-        if (gm < p.M) {
+        float out[16];
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int gn = n0 + h * 128 + cb * 16 + j;
-            if (gn < p.N) {
-              float *cp = p.C + gm + (size_t)gn * p.ldc;
-              *cp = fmaf(p.alpha, __uint_as_float(r[j]), *cp);
-            }
-          }
+        for (int j = 0; j < 16; ++j) out[j] = fmaf(p.alpha, __uint_as_float(r[j]), cv[j]);
+        if (cb + 1 < 8) load_batch(cb + 1);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int gn = n0 + h * 128 + cb * 16 + j;
+          if (rok && gn < p.N) __stcs(crow + (size_t)gn * p.ldc, out[j]);
         }
       }
     }

@@ -253,6 +253,26 @@ __global__ void __launch_bounds__(256)
   for (int s = 0; s < nb - 1; ++s) {
     const int c = lower ? s : nb - 1 - s;
     if (lower ? c >= b : c <= b) break;
+    const int c0 = c * TV_B;
+    const int nc = (n - c0 < TV_B) ? n - c0 : TV_B;
+    // this block's part of A does not depend on x: load it before waiting
+    T pa[16];
+    if (ta == kNoTrans) {
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        const int k = w + 8 * m;
+        const T *col = A + r0 + (size_t)(c0 + k) * lda;
+        pa[2 * m] = (k < nc && lane < nr) ? col[lane] : T(0);
+        pa[2 * m + 1] = (k < nc && lane + 32 < nr) ? col[lane + 32] : T(0);
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int i = w * 8 + q;
+        pa[2 * q] = (i < nr && lane < nc) ? A[(c0 + lane) + (size_t)(r0 + i) * lda] : T(0);
+        pa[2 * q + 1] = (i < nr && lane + 32 < nc) ? A[(c0 + lane + 32) + (size_t)(r0 + i) * lda] : T(0);
+      }
+    }
     if (threadIdx.x == 0) {
       unsigned i = 0;
       while (atomicAdd(&flags[c], 0) == 0) {
@@ -263,24 +283,19 @@ __global__ void __launch_bounds__(256)
     }
     __syncthreads();
     if (s_fail) return;
-    const int c0 = c * TV_B;
-    const int nc = (n - c0 < TV_B) ? n - c0 : TV_B;
     if (ta == kNoTrans) {
-      for (int k = w; k < nc; k += 8) {
-        const T xk = __ldcg(x + c0 + k);          // published by another CTA: read at L2
-        const T *col = A + r0 + (size_t)(c0 + k) * lda;
-        if (lane < nr) acc0 = fma(col[lane], xk, acc0);
-        if (lane + 32 < nr) acc1 = fma(col[lane + 32], xk, acc1);
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        const int k = w + 8 * m;
+        const T xk = (k < nc) ? __ldcg(x + c0 + k) : T(0);      // published by another CTA: read at L2
+        acc0 = fma(pa[2 * m], xk, acc0);
+        acc1 = fma(pa[2 * m + 1], xk, acc1);
       }
     } else {
-      for (int k = lane; k < nc; k += 32) {
-        const T xk = __ldcg(x + c0 + k);
+      const T x0 = (lane < nc) ? __ldcg(x + c0 + lane) : T(0);
+      const T x1 = (lane + 32 < nc) ? __ldcg(x + c0 + lane + 32) : T(0);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int i = w * 8 + q;
-          if (i < nr) accT[q] = fma(A[(c0 + k) + (size_t)(r0 + i) * lda], xk, accT[q]);
-        }
-      }
+      for (int q = 0; q < 8; ++q) accT[q] = fma(pa[2 * q + 1], x1, fma(pa[2 * q], x0, accT[q]));
     }
   }
   // gather the partial sums: part[w][row]
