@@ -406,6 +406,63 @@ def run_gpu(args):
     return 0
 
 
+def run_case(args):
+    """Single-kernel workloads for profiling runs (ncu captures in profiles/):
+    split  -- split-precision DGEMM n^3 (7 slices), run twice
+    sgetrf -- FP32 LU (FFMA trailing update) at n
+    mixed  -- mixed-precision dgesv at n on A = G/sqrt(n) + 4I, run twice
+    Prints one JSON line with the device time of the last run."""
+    import ctypes as C
+    import torch
+    import atlas_gb300 as G
+    L = G.lib()
+    st = L.atlg_stream()
+    s = torch.cuda.ExternalStream(st)
+    n = args.n
+    g = torch.Generator(device="cuda").manual_seed(1)
+    ms = None
+    if args.case == "split":
+        A = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g)
+        B = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g)
+        Cm = torch.zeros(n, n, device="cuda", dtype=torch.float64)
+        for _ in range(2):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            L.atlg_dgemm_split_dev(111, 111, n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0, Cm.data_ptr(), n,
+                                   7, st)
+            e1.record(s)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+    elif args.case == "sgetrf":
+        S = torch.randn(n, n, device="cuda", dtype=torch.float32, generator=g)
+        piv = torch.zeros(n, dtype=torch.int32, device="cuda")
+        inf = torch.zeros(4, dtype=torch.int32, device="cuda")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        L.atlg_sgetrf_dev(n, n, S.data_ptr(), n, piv.data_ptr(), inf.data_ptr(), st)
+        e1.record(s)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+    else:
+        A0 = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g) / n ** 0.5 + \
+            4 * torch.eye(n, device="cuda", dtype=torch.float64)
+        b = torch.randn(n, device="cuda", dtype=torch.float64, generator=g)
+        A = A0.clone()
+        X = torch.zeros(n, device="cuda", dtype=torch.float64)
+        piv = torch.zeros(n, dtype=torch.int32, device="cuda")
+        berr, ferr, it, stt = C.c_double(), C.c_double(), C.c_int(), C.c_int()
+        for _ in range(2):
+            A.copy_(A0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            L.atlg_dgesv_mixed_dev(n, 1, A.data_ptr(), n, piv.data_ptr(), b.data_ptr(), n, X.data_ptr(), n,
+                                   C.byref(berr), C.byref(ferr), C.byref(it), C.byref(stt), st)
+            torch.cuda.synchronize()
+            ms = (time.perf_counter() - t0) * 1e3
+    print(json.dumps({"case": args.case, "n": n, "ms": ms, "status": int(L.atlg_status())}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -414,11 +471,15 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=8192)
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
+    ap.add_argument("--case", choices=["split", "sgetrf", "mixed"], default=None,
+                    help="run one kernel workload for a profiling capture instead of the benchmark")
     ap.add_argument("--skip-extras", action="store_true",
                     help="omit the n=16384 mixed-dgesv and split-DGEMM measurements")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.case:
+        return run_case(args)
     return run_gpu(args)
 
 
