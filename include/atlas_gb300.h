@@ -126,6 +126,10 @@ int atlg_dgemm_dev_opts(int TA, int TB, int M, int N, int K, double alpha, const
 int atlg_dgemm_split_dev(int TA, int TB, int M, int N, int K, double alpha, const double *A,
                          int lda, const double *B, int ldb, double beta, double *C, int ldc,
                          int nslices, void *stream);
+/* C += alpha * A * B (FP32, column-major, no transposes) on tcgen05 tensor
+ * cores with the 3xTF32 split (the mixed solver's factor update). */
+int atlg_sgemm_tf32x3_dev(int M, int N, int K, float alpha, const float *A, int lda,
+                          const float *B, int ldb, float *C, int ldc, void *stream);
 int atlg_sgemm_dev(int TA, int TB, int M, int N, int K, float alpha, const float *A, int lda,
                    const float *B, int ldb, float beta, float *C, int ldc, void *stream);
 int atlg_dtrsm_dev(int Side, int Uplo, int TA, int Diag, int M, int N, double alpha,
