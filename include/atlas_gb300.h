@@ -36,6 +36,13 @@ enum CBLAS_UPLO {CblasUpper=121, CblasLower=122};
 enum CBLAS_DIAG {CblasNonUnit=131, CblasUnit=132};
 enum CBLAS_SIDE {CblasLeft=141, CblasRight=142};
 #endif
+/* AtlasBase/Clint/atlas-clp.base:624-627 (clapack.h aliases) */
+#ifndef ATLAS_ORDER
+#define ATLAS_ORDER CBLAS_ORDER
+#endif
+#ifndef ATLAS_UPLO
+#define ATLAS_UPLO CBLAS_UPLO
+#endif
 
 /* ---- error reporting: AtlasBase/Clint/cblas.base:14 (cblas_errprn), :42 (cblas_xerbla) */
 int  cblas_errprn(int ierr, int info, const char *form, ...);
@@ -61,6 +68,16 @@ void cblas_strsm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side,
                  const enum CBLAS_DIAG Diag, const int M, const int N, const float alpha,
                  const float *A, const int lda, float *B, const int ldb);
 
+/* ---- Level 3: AtlasBase/Clint/cblas.base:339-450 (SYRK template, d and s) */
+void cblas_dsyrk(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo,
+                 const enum CBLAS_TRANSPOSE Trans, const int N, const int K,
+                 const double alpha, const double *A, const int lda, const double beta,
+                 double *C, const int ldc);
+void cblas_ssyrk(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo,
+                 const enum CBLAS_TRANSPOSE Trans, const int N, const int K,
+                 const float alpha, const float *A, const int lda, const float beta,
+                 float *C, const int ldc);
+
 /* ---- LAPACK: AtlasBase/Clint/atlas-clp.base:140 (clapack_getrf, d and s) */
 int clapack_dgetrf(const enum CBLAS_ORDER Order, const int M, const int N, double *A,
                    const int lda, int *ipiv);
@@ -78,6 +95,22 @@ int clapack_dgesv(const enum CBLAS_ORDER Order, const int N, const int NRHS, dou
                   const int lda, int *ipiv, double *B, const int ldb);
 int clapack_sgesv(const enum CBLAS_ORDER Order, const int N, const int NRHS, float *A,
                   const int lda, int *ipiv, float *B, const int ldb);
+
+/* ---- LAPACK: AtlasBase/Clint/atlas-clp.base:320-362 (clapack_potrf, d and s) */
+int clapack_dpotrf(const enum ATLAS_ORDER Order, const enum ATLAS_UPLO Uplo, const int N,
+                   double *A, const int lda);
+int clapack_spotrf(const enum ATLAS_ORDER Order, const enum ATLAS_UPLO Uplo, const int N,
+                   float *A, const int lda);
+/* ---- LAPACK: AtlasBase/Clint/atlas-clp.base:363-410 (clapack_potrs, d and s) */
+int clapack_dpotrs(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const int N,
+                   const int NRHS, const double *A, const int lda, double *B, const int ldb);
+int clapack_spotrs(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const int N,
+                   const int NRHS, const float *A, const int lda, float *B, const int ldb);
+/* ---- LAPACK: AtlasBase/Clint/atlas-clp.base:266-315 (clapack_posv, d and s) */
+int clapack_dposv(const enum ATLAS_ORDER Order, const enum ATLAS_UPLO Uplo, const int N,
+                  const int NRHS, double *A, const int lda, double *B, const int ldb);
+int clapack_sposv(const enum ATLAS_ORDER Order, const enum ATLAS_UPLO Uplo, const int N,
+                  const int NRHS, float *A, const int lda, float *B, const int ldb);
 
 /* ---- new methods (no reference counterpart: ATLAS has neither a
  *      mixed-precision solver nor an adjoint).  Column-major. */
@@ -154,6 +187,13 @@ int atlg_dgetrf_dev(int M, int N, double *A, int lda, int *ipiv, int *info, void
 int atlg_sgetrf_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void *stream);
 int atlg_dgetrs_dev(int Order, int Trans, int N, int NRHS, const double *A, int lda,
                     const int *ipiv, double *B, int ldb, void *stream);
+/* column-major SYRK / Cholesky on device data (Uplo, Trans, Order take the
+ * CBLAS values); potrf returns info and synchronizes once per 64 columns */
+int atlg_dsyrk_dev(int Uplo, int Trans, int N, int K, double alpha, const double *A, int lda,
+                   double beta, double *C, int ldc, void *stream);
+int atlg_dpotrf_dev(int Uplo, int N, double *A, int lda, void *stream);
+int atlg_dpotrs_dev(int Order, int Uplo, int N, int NRHS, const double *A, int lda, double *B,
+                    int ldb, void *stream);
 /* berr, ferr (NRHS entries), iters and status are host pointers; synchronizes */
 int atlg_dgesv_mixed_dev(int N, int NRHS, double *A, int lda, int *ipiv, const double *B,
                          int ldb, double *X, int ldx, double *berr, double *ferr, int *iters,

@@ -29,6 +29,8 @@ EXPORTS = [
     "atlg_sgetrf_dev", "atlg_dgetrs_dev", "atlg_launch_count", "atlg_prof_enable", "atlg_prof_collect",
     "atlg_probe_peaks", "dgesv_mixed", "dgesv_adjoint", "atlg_dgesv_mixed_dev", "atlg_dgesv_adjoint_dev",
     "atlg_dlaswp_noalloc", "dgemm_split", "atlg_dgemm_split_dev", "atlg_sgemm_tf32x3_dev",
+    "cblas_dsyrk", "cblas_ssyrk", "clapack_dpotrf", "clapack_spotrf", "clapack_dpotrs", "clapack_spotrs",
+    "clapack_dposv", "clapack_sposv", "atlg_dsyrk_dev", "atlg_dpotrf_dev", "atlg_dpotrs_dev",
 ]
 
 _lib = None
@@ -66,6 +68,17 @@ def _declare(L):
         "clapack_sgetrs": (_i, [_i, _i, _i, _i, _sp, _i, _ip, _sp, _i]),
         "clapack_dgesv": (_i, [_i, _i, _i, _dp, _i, _ip, _dp, _i]),
         "clapack_sgesv": (_i, [_i, _i, _i, _sp, _i, _ip, _sp, _i]),
+        "cblas_dsyrk": (None, [_i, _i, _i, _i, _i, _d, _dp, _i, _d, _dp, _i]),
+        "cblas_ssyrk": (None, [_i, _i, _i, _i, _i, _f, _sp, _i, _f, _sp, _i]),
+        "clapack_dpotrf": (_i, [_i, _i, _i, _dp, _i]),
+        "clapack_spotrf": (_i, [_i, _i, _i, _sp, _i]),
+        "clapack_dpotrs": (_i, [_i, _i, _i, _i, _dp, _i, _dp, _i]),
+        "clapack_spotrs": (_i, [_i, _i, _i, _i, _sp, _i, _sp, _i]),
+        "clapack_dposv": (_i, [_i, _i, _i, _i, _dp, _i, _dp, _i]),
+        "clapack_sposv": (_i, [_i, _i, _i, _i, _sp, _i, _sp, _i]),
+        "atlg_dsyrk_dev": (_i, [_i, _i, _i, _i, _d, _v, _i, _d, _v, _i, _v]),
+        "atlg_dpotrf_dev": (_i, [_i, _i, _v, _i, _v]),
+        "atlg_dpotrs_dev": (_i, [_i, _i, _i, _i, _v, _i, _v, _i, _v]),
         "atlg_num_sms": (_i, []),
         "atlg_stream": (_v, []),
         "atlg_status": (_u, []),
@@ -139,6 +152,38 @@ def clapack_dgesv(order, N, NRHS, A, lda, ipiv, B, ldb):
 
 def clapack_sgesv(order, N, NRHS, A, lda, ipiv, B, ldb):
     return lib().clapack_sgesv(order, N, NRHS, A, lda, ipiv, B, ldb)
+
+
+def cblas_dsyrk(order, uplo, trans, N, K, alpha, A, lda, beta, Cm, ldc):
+    lib().cblas_dsyrk(order, uplo, trans, N, K, alpha, A, lda, beta, Cm, ldc)
+
+
+def cblas_ssyrk(order, uplo, trans, N, K, alpha, A, lda, beta, Cm, ldc):
+    lib().cblas_ssyrk(order, uplo, trans, N, K, alpha, A, lda, beta, Cm, ldc)
+
+
+def clapack_dpotrf(order, uplo, N, A, lda):
+    return lib().clapack_dpotrf(order, uplo, N, A, lda)
+
+
+def clapack_spotrf(order, uplo, N, A, lda):
+    return lib().clapack_spotrf(order, uplo, N, A, lda)
+
+
+def clapack_dpotrs(order, uplo, N, NRHS, A, lda, B, ldb):
+    return lib().clapack_dpotrs(order, uplo, N, NRHS, A, lda, B, ldb)
+
+
+def clapack_spotrs(order, uplo, N, NRHS, A, lda, B, ldb):
+    return lib().clapack_spotrs(order, uplo, N, NRHS, A, lda, B, ldb)
+
+
+def clapack_dposv(order, uplo, N, NRHS, A, lda, B, ldb):
+    return lib().clapack_dposv(order, uplo, N, NRHS, A, lda, B, ldb)
+
+
+def clapack_sposv(order, uplo, N, NRHS, A, lda, B, ldb):
+    return lib().clapack_sposv(order, uplo, N, NRHS, A, lda, B, ldb)
 
 
 def dgemm_split(ta, tb, alpha, A, B, beta, Cm, nslices=7):

@@ -19,6 +19,7 @@
 #include "../../include/atlas_gb300.h"
 #include "common.cuh"
 #include "context.cuh"
+#include "chol.cuh"
 #include "gemm.cuh"
 #include "lu.cuh"
 #include "mixed.cuh"
@@ -84,6 +85,10 @@ void to_host(T *h, int ldh, const T *d, int ldd, int rows, int cols, cudaStream_
 }
 
 cudaStream_t stream_of(void *s) { return s ? static_cast<cudaStream_t>(s) : ctx().stream; }
+
+template <typename T>
+void dev_syrk_any(int uplo, int trans, int n, int k, T alpha, const T *A, int lda, T beta, T *C, int ldc,
+                  cudaStream_t st);
 
 // ---------------------------------------------------------------------- GEMM
 template <typename T>
@@ -157,6 +162,25 @@ void host_gemm(const char *rout, int Order, int TA, int TB, int M, int N, int K,
                const T *B, int ldb, T beta, T *C, int ldc) {
   if (gemm_check<T>(rout, Order, TA, TB, M, N, K, lda, ldb, ldc)) return;
   if (M == 0 || N == 0) return;
+  // A op(A)^T asked for as a GEMM: SYRK of the upper triangle, then mirror
+  // it (AtlasBase/Clint/cblas.base:220-231).  One operand must be NoTrans:
+  // Trans against ConjTrans is A^T A^T for real data, not a SYRK.
+  if (A == B && M == N && TA != TB && lda == ldb && beta == T(0) && K > 0 && alpha != T(0) &&
+      (TA == CblasNoTrans || TB == CblasNoTrans)) {
+    const int tr = (Order == CblasColMajor) ? TA : TB;
+    cudaStream_t st = ctx().stream;
+    int ldd_a, ldd_c = even_up(N);
+    const T *dA = (tr == CblasNoTrans) ? to_dev<T>(kBufA, A, N, K, lda, &ldd_a, st)
+                                       : to_dev<T>(kBufA, A, K, N, lda, &ldd_a, st);
+    T *dC = static_cast<T *>(ctx().buffer(kBufC, sizeof(T) * (size_t)ldd_c * N));
+    dev_syrk_any<T>(kUpper, tr == CblasNoTrans ? kNoTrans : kTrans, N, K, alpha, dA, ldd_a, beta, dC, ldd_c, st);
+    if (sizeof(T) == 8) dev_dsyreflect(N, (double *)dC, ldd_c, st);
+    else dev_ssyreflect(N, (float *)dC, ldd_c, st);
+    to_host<T>(C, ldc, dC, ldd_c, N, N, st);
+    ATLG_CHECK(cudaStreamSynchronize(st));
+    check_status(rout);
+    return;
+  }
   if (Order == CblasRowMajor) {   // C^T = op(B)^T op(A)^T in column-major terms
     const T *t = A; A = B; B = t;
     int ti = lda; lda = ldb; ldb = ti;
@@ -359,6 +383,152 @@ int host_gesv(const char *rout, int Order, int N, int NRHS, T *A, int lda, int *
   return info;
 }
 
+// ------------------------------------------------------- SYRK and Cholesky
+// cblas_?syrk: checks and the RowMajor flip of Uplo and Trans follow
+// AtlasBase/Clint/cblas.base:356-449.
+int syrk_check(const char *rout, int Order, int Uplo, int Trans, int N, int K, int lda, int ldc) {
+  int info = 2000;
+  if (Uplo != CblasUpper && Uplo != CblasLower)
+    info = cblas_errprn(2, info, "UPLO must be %d or %d, but is set to %d", CblasUpper, CblasLower, Uplo);
+  if (N < 0) info = cblas_errprn(4, info, "N cannot be less than zero; it is set to %d.", N);
+  if (K < 0) info = cblas_errprn(5, info, "K cannot be less than zero; it is set to %d.", K);
+  if (Order == CblasColMajor || Order == CblasRowMajor) {
+    // ColMajor NoTrans and RowMajor Trans store A with N rows per column
+    const bool n_rows = (Order == CblasColMajor) == (Trans == CblasNoTrans);
+    if (Trans != CblasNoTrans && Trans != CblasTrans && Trans != CblasConjTrans)
+      info = cblas_errprn(3, info, "Trans must be %d, %d or %d, but is set to %d", CblasNoTrans, CblasTrans,
+                          CblasConjTrans, Trans);
+    if (n_rows) {
+      if (lda < N || lda < 1) info = cblas_errprn(8, info, "lda must be >= MAX(N,1): lda=%d N=%d", lda, N);
+    } else {
+      if (lda < K || lda < 1) info = cblas_errprn(8, info, "lda must be >= MAX(K,1): lda=%d K=%d", lda, K);
+    }
+  } else
+    info = cblas_errprn(1, info, "Order must be %d or %d, but is set to %d", CblasRowMajor, CblasColMajor, Order);
+  if (ldc < N || ldc < 1) info = cblas_errprn(11, info, "ldc must be >= MAX(N,1): ldc=%d N=%d", ldc, N);
+  if (info != 2000) {
+    cblas_xerbla(info, rout, "");
+    return info;
+  }
+  return 0;
+}
+
+template <typename T>
+void dev_syrk_any(int uplo, int trans, int n, int k, T alpha, const T *A, int lda, T beta, T *C, int ldc,
+                  cudaStream_t st) {
+  if (sizeof(T) == 8)
+    dev_dsyrk(uplo, trans, n, k, (double)alpha, (const double *)A, lda, (double)beta, (double *)C, ldc, st);
+  else
+    dev_ssyrk(uplo, trans, n, k, (float)alpha, (const float *)A, lda, (float)beta, (float *)C, ldc, st);
+}
+
+template <typename T>
+void host_syrk(const char *rout, int Order, int Uplo, int Trans, int N, int K, T alpha, const T *A, int lda, T beta,
+               T *C, int ldc) {
+  if (syrk_check(rout, Order, Uplo, Trans, N, K, lda, ldc)) return;
+  if (Order == CblasRowMajor) {
+    Uplo = (Uplo == CblasUpper) ? CblasLower : CblasUpper;
+    Trans = (Trans == CblasNoTrans) ? CblasTrans : CblasNoTrans;
+  }
+  if (N == 0) return;
+  if (Trans == CblasConjTrans) Trans = CblasTrans;
+  cudaStream_t st = ctx().stream;
+  int ldd_a = 2, ldd_c;
+  // the whole square goes both ways, so the other triangle comes back as it was
+  T *dC = to_dev<T>(kBufC, C, N, N, ldc, &ldd_c, st);
+  const T *dA = nullptr;
+  if (K > 0 && alpha != T(0))
+    dA = (Trans == CblasNoTrans) ? to_dev<T>(kBufA, A, N, K, lda, &ldd_a, st) : to_dev<T>(kBufA, A, K, N, lda, &ldd_a, st);
+  dev_syrk_any<T>(Uplo, Trans, N, K, alpha, dA, ldd_a, beta, dC, ldd_c, st);
+  to_host<T>(C, ldc, dC, ldd_c, N, N, st);
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  check_status(rout);
+}
+
+template <typename T>
+int dev_potrf_any(int uplo, int n, T *A, int lda, cudaStream_t st) {
+  return (sizeof(T) == 8) ? dev_dpotrf(uplo, n, (double *)A, lda, st) : dev_spotrf(uplo, n, (float *)A, lda, st);
+}
+template <typename T>
+void dev_potrs_any(int order, int uplo, int n, int nrhs, const T *A, int lda, T *B, int ldb, cudaStream_t st) {
+  if (sizeof(T) == 8) dev_dpotrs(order, uplo, n, nrhs, (const double *)A, lda, (double *)B, ldb, st);
+  else dev_spotrs(order, uplo, n, nrhs, (const float *)A, lda, (float *)B, ldb, st);
+}
+
+// ATL_potrf's dispatch (AtlasBase/Clint/atlas-lp.base:336-357): RowMajor
+// real data is the column-major factorization of the other triangle.
+inline int potrf_uplo(int Order, int Uplo) {
+  const int u = (Uplo == CblasUpper) ? kUpper : kLower;
+  if (Order == CblasColMajor) return u;
+  return u == kUpper ? kLower : kUpper;
+}
+
+// clapack_?potrf / ?potrs / ?posv argument checks (AtlasBase/Clint/
+// atlas-clp.base:266-410).  Unlike cblas, every failing check calls xerbla.
+void lp_check_ou(const char *rout, int Order, int Uplo, int N) {
+  if (Order != CblasRowMajor && Order != CblasColMajor)
+    cblas_xerbla(1, rout, "Order must be %d or %d, but is set to %d\n", CblasRowMajor, CblasColMajor, Order);
+  if (Uplo != CblasUpper && Uplo != CblasLower)
+    cblas_xerbla(2, rout, "Uplo must be %d or %d, but is set to %d\n", CblasUpper, CblasLower, Uplo);
+  if (N < 0) cblas_xerbla(3, rout, "N cannot be less than zero 0,; is set to %d.\n", N);
+}
+
+template <typename T>
+int host_potrf(const char *rout, int Order, int Uplo, int N, T *A, int lda) {
+  lp_check_ou(rout, Order, Uplo, N);
+  if (lda < N || lda < 1) cblas_xerbla(5, rout, "lda must be >= MAX(N,1): lda=%d N=%d\n", lda, N);
+  if (N == 0) return 0;
+  cudaStream_t st = ctx().stream;
+  int ldd;
+  T *dA = to_dev<T>(kBufA, A, N, N, lda, &ldd, st);
+  const int info = dev_potrf_any<T>(potrf_uplo(Order, Uplo), N, dA, ldd, st);
+  to_host<T>(A, lda, dA, ldd, N, N, st);
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  check_status(rout);
+  return info;
+}
+
+template <typename T>
+int host_potrs(const char *rout, int Order, int Uplo, int N, int NRHS, const T *A, int lda, T *B, int ldb) {
+  lp_check_ou(rout, Order, Uplo, N);
+  if (NRHS < 0) cblas_xerbla(4, rout, "NRHS cannot be less than zero 0,; is set to %d.\n", NRHS);
+  if (lda < N || lda < 1) cblas_xerbla(6, rout, "lda must be >= MAX(N,1): lda=%d N=%d\n", lda, N);
+  if (ldb < N || ldb < 1) cblas_xerbla(8, rout, "ldb must be >= MAX(N,1): ldb=%d N=%d\n", ldb, N);
+  if (N == 0 || NRHS == 0) return 0;
+  cudaStream_t st = ctx().stream;
+  int ldd_a, ldd_b;
+  const T *dA = to_dev<T>(kBufA, A, N, N, lda, &ldd_a, st);
+  T *dB = to_dev<T>(kBufB, B, N, NRHS, ldb, &ldd_b, st);
+  dev_potrs_any<T>(Order, Uplo == CblasUpper ? kUpper : kLower, N, NRHS, dA, ldd_a, dB, ldd_b, st);
+  to_host<T>(B, ldb, dB, ldd_b, N, NRHS, st);
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  check_status(rout);
+  return 0;
+}
+
+template <typename T>
+int host_posv(const char *rout, int Order, int Uplo, int N, int NRHS, T *A, int lda, T *B, int ldb) {
+  lp_check_ou(rout, Order, Uplo, N);
+  if (NRHS < 0) cblas_xerbla(4, rout, "NRHS cannot be less than zero 0,; is set to %d.\n", NRHS);
+  if (lda < N || lda < 1) cblas_xerbla(6, rout, "lda must be >= MAX(N,1): lda=%d N=%d\n", lda, N);
+  if (ldb < N || ldb < 1) cblas_xerbla(8, rout, "ldb must be >= MAX(N,1): ldb=%d N=%d\n", ldb, N);
+  if (N == 0) return 0;
+  cudaStream_t st = ctx().stream;
+  int ldd_a;
+  T *dA = to_dev<T>(kBufA, A, N, N, lda, &ldd_a, st);
+  const int info = dev_potrf_any<T>(potrf_uplo(Order, Uplo), N, dA, ldd_a, st);
+  to_host<T>(A, lda, dA, ldd_a, N, N, st);
+  if (info == 0 && NRHS > 0) {
+    int ldd_b;
+    T *dB = to_dev<T>(kBufB, B, N, NRHS, ldb, &ldd_b, st);
+    dev_potrs_any<T>(Order, Uplo == CblasUpper ? kUpper : kLower, N, NRHS, dA, ldd_a, dB, ldd_b, st);
+    to_host<T>(B, ldb, dB, ldd_b, N, NRHS, st);
+  }
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  check_status(rout);
+  return info;
+}
+
 // ------------------------------------------------------------- new methods
 int mixed_dev(int N, int NRHS, double *A, int lda, int *ipiv, const double *B, int ldb, double *X, int ldx,
               double *berr, double *ferr, int *iters, int *status, cudaStream_t st) {
@@ -433,6 +603,39 @@ int clapack_dgesv(const enum CBLAS_ORDER Order, const int N, const int NRHS, dou
 int clapack_sgesv(const enum CBLAS_ORDER Order, const int N, const int NRHS, float *A, const int lda, int *ipiv,
                   float *B, const int ldb) {
   return host_gesv<float>("clapack_sgesv", Order, N, NRHS, A, lda, ipiv, B, ldb);
+}
+
+void cblas_dsyrk(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE Trans,
+                 const int N, const int K, const double alpha, const double *A, const int lda, const double beta,
+                 double *C, const int ldc) {
+  host_syrk<double>("cblas_dsyrk", Order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc);
+}
+void cblas_ssyrk(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE Trans,
+                 const int N, const int K, const float alpha, const float *A, const int lda, const float beta,
+                 float *C, const int ldc) {
+  host_syrk<float>("cblas_ssyrk", Order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc);
+}
+int clapack_dpotrf(const enum ATLAS_ORDER Order, const enum ATLAS_UPLO Uplo, const int N, double *A, const int lda) {
+  return host_potrf<double>("clapack_dpotrf", Order, Uplo, N, A, lda);
+}
+int clapack_spotrf(const enum ATLAS_ORDER Order, const enum ATLAS_UPLO Uplo, const int N, float *A, const int lda) {
+  return host_potrf<float>("clapack_spotrf", Order, Uplo, N, A, lda);
+}
+int clapack_dpotrs(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const int N, const int NRHS,
+                   const double *A, const int lda, double *B, const int ldb) {
+  return host_potrs<double>("clapack_dpotrs", Order, Uplo, N, NRHS, A, lda, B, ldb);
+}
+int clapack_spotrs(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const int N, const int NRHS,
+                   const float *A, const int lda, float *B, const int ldb) {
+  return host_potrs<float>("clapack_spotrs", Order, Uplo, N, NRHS, A, lda, B, ldb);
+}
+int clapack_dposv(const enum ATLAS_ORDER Order, const enum ATLAS_UPLO Uplo, const int N, const int NRHS, double *A,
+                  const int lda, double *B, const int ldb) {
+  return host_posv<double>("clapack_dposv", Order, Uplo, N, NRHS, A, lda, B, ldb);
+}
+int clapack_sposv(const enum ATLAS_ORDER Order, const enum ATLAS_UPLO Uplo, const int N, const int NRHS, float *A,
+                  const int lda, float *B, const int ldb) {
+  return host_posv<float>("clapack_sposv", Order, Uplo, N, NRHS, A, lda, B, ldb);
 }
 
 // Split-precision DGEMM (no reference counterpart; see split.cu): the
@@ -651,6 +854,22 @@ int atlg_dgesv_adjoint_dev(int n, int nrhs, const double *LU, int lda, const int
                            const double *gX, int ldgx, double *gA, int ldga, double *gB, int ldgb, void *stream) {
   if (n < 0 || nrhs < 0) return -1;
   adjoint_dev(n, nrhs, LU, lda, ipiv, X, ldx, gX, ldgx, gA, ldga, gB, ldgb, stream_of(stream));
+  return 0;
+}
+int atlg_dsyrk_dev(int Uplo, int Trans, int N, int K, double alpha, const double *A, int lda, double beta,
+                   double *C, int ldc, void *stream) {
+  if (N < 0 || K < 0) return -1;
+  dev_dsyrk(Uplo, Trans == kNoTrans ? kNoTrans : kTrans, N, K, alpha, A, lda, beta, C, ldc, stream_of(stream));
+  return 0;
+}
+int atlg_dpotrf_dev(int Uplo, int N, double *A, int lda, void *stream) {
+  if (N < 0 || lda < (N > 1 ? N : 1)) return -1;
+  return dev_dpotrf(Uplo, N, A, lda, stream_of(stream));
+}
+int atlg_dpotrs_dev(int Order, int Uplo, int N, int NRHS, const double *A, int lda, double *B, int ldb,
+                    void *stream) {
+  if (N < 0 || NRHS < 0) return -1;
+  dev_dpotrs(Order, Uplo, N, NRHS, A, lda, B, ldb, stream_of(stream));
   return 0;
 }
 int atlg_dgetrs_dev(int Order, int Trans, int N, int NRHS, const double *A, int lda, const int *ipiv, double *B,

@@ -53,7 +53,7 @@ template <typename T, int BM, int BN, int BK, int TM, int TN, int NT, int STAGES
           bool USE_TMA>
 __global__ void __launch_bounds__(NT)
     gemm_kernel(int M, int N, int K, T alpha, const T *__restrict__ A, int lda,
-                const T *__restrict__ B, int ldb, T beta, T *__restrict__ C, int ldc,
+                const T *__restrict__ B, int ldb, T beta, T *__restrict__ C, int ldc, int uplo,
                 const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB) {
   using KC = GemmKernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, USE_TMA>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -63,6 +63,8 @@ __global__ void __launch_bounds__(NT)
   const int tid = threadIdx.x;
   const int m0 = blockIdx.x * BM;
   const int n0 = blockIdx.y * BN;
+  // triangle-masked update (SYRK): tiles wholly outside the triangle exit
+  if ((uplo == kLower && m0 + BM <= n0) || (uplo == kUpper && n0 + BN <= m0)) return;
   const int KT = (K + BK - 1) / BK;
   const int tx = tid % KC::GX, ty = tid / KC::GX;
 
@@ -168,7 +170,7 @@ __global__ void __launch_bounds__(NT)
 #pragma unroll
     for (int i = 0; i < TM; ++i) {
       const int m = m0 + tx + i * KC::GX;
-      if (m >= M) continue;
+      if (m >= M || (uplo == kLower && m < n) || (uplo == kUpper && m > n)) continue;
       const T v = alpha * acc[i][j];
       c[m] = (beta == T(0)) ? v : fma(beta, c[m], v);
     }
@@ -182,7 +184,7 @@ template <> struct DT<float>  { static constexpr CUtensorMapDataType v = CU_TENS
 
 template <typename T, int BM, int BN, int BK, int TM, int TN, int NT, int STAGES, int TA, int TB>
 static void launch_cfg(int M, int N, int K, T alpha, const T *A, int lda, const T *B, int ldb,
-                       T beta, T *C, int ldc, cudaStream_t st, bool allow_tma) {
+                       T beta, T *C, int ldc, cudaStream_t st, bool allow_tma, int uplo) {
   dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN);
   CUtensorMap tmA, tmB;
   bool tma = allow_tma;
@@ -199,7 +201,7 @@ static void launch_cfg(int M, int N, int K, T alpha, const T *A, int lda, const 
     using KC = GemmKernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, true>;
     auto k = gemm_kernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, true>;
     ATLG_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, KC::SMEM_BYTES));
-    k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, tmA, tmB);
+    k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, uplo, tmA, tmB);
     note_launch();
   } else {
     memset(&tmA, 0, sizeof(tmA));
@@ -207,7 +209,7 @@ static void launch_cfg(int M, int N, int K, T alpha, const T *A, int lda, const 
     using KC = GemmKernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, false>;
     auto k = gemm_kernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, false>;
     ATLG_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, KC::SMEM_BYTES));
-    k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, tmA, tmB);
+    k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, uplo, tmA, tmB);
     note_launch();
   }
   ATLG_CHECK(cudaGetLastError());
@@ -230,18 +232,18 @@ static int pick_dtile(int M, int N, int nsm) {
 
 template <int TA, int TB>
 static void dgemm_t(int M, int N, int K, double alpha, const double *A, int lda, const double *B, int ldb,
-                    double beta, double *C, int ldc, cudaStream_t st, bool tma, int nsm) {
+                    double beta, double *C, int ldc, cudaStream_t st, bool tma, int nsm, int uplo) {
   switch (pick_dtile(M, N, nsm)) {
-    case 0: launch_cfg<double, 64, 64, 16, 8, 4, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma); break;
-    case 1: launch_cfg<double, 64, 32, 16, 4, 4, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma); break;
-    default: launch_cfg<double, 32, 32, 16, 4, 2, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma); break;
+    case 0: launch_cfg<double, 64, 64, 16, 8, 4, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo); break;
+    case 1: launch_cfg<double, 64, 32, 16, 4, 4, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo); break;
+    default: launch_cfg<double, 32, 32, 16, 4, 2, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo); break;
   }
 }
 
 template <int TA, int TB>
 static void sgemm_t(int M, int N, int K, float alpha, const float *A, int lda, const float *B, int ldb,
-                    float beta, float *C, int ldc, cudaStream_t st, bool tma) {
-  launch_cfg<float, 128, 128, 16, 8, 8, 256, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma);
+                    float beta, float *C, int ldc, cudaStream_t st, bool tma, int uplo) {
+  launch_cfg<float, 128, 128, 16, 8, 8, 256, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo);
 }
 
 __global__ void scale_kernel_d(int M, int N, double beta, double *C, int ldc) {
@@ -375,15 +377,15 @@ void dev_dgemm(int TA, int TB, int M, int N, int K, double alpha, const double *
   if (alpha == 0.0 || K <= 0) { dev_gescal(M, N, beta, C, ldc, st); return; }
   const bool ta = TA != kNoTrans, tb = TB != kNoTrans;
   const int nsm = o.num_sms > 0 ? o.num_sms : ctx().num_sms;
-  if (N == 1 && o.allow_gemv) {   // matrix-vector product: x = op(B)(:,0)
+  if (N == 1 && o.allow_gemv && o.uplo == 0) {   // matrix-vector product: x = op(B)(:,0)
     gemv_launch<double>(TA, M, K, alpha, A, lda, B, tb ? ldb : 1, beta, C, st);
     return;
   }
   ProfScope ps(st, 2.0 * M * N * K);
-  if (!ta && !tb) dgemm_t<kNoTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm);
-  else if (!ta && tb) dgemm_t<kNoTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm);
-  else if (ta && !tb) dgemm_t<kTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm);
-  else dgemm_t<kTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm);
+  if (!ta && !tb) dgemm_t<kNoTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo);
+  else if (!ta && tb) dgemm_t<kNoTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo);
+  else if (ta && !tb) dgemm_t<kTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo);
+  else dgemm_t<kTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo);
 }
 
 void dev_sgemm(int TA, int TB, int M, int N, int K, float alpha, const float *A, int lda, const float *B,
@@ -391,15 +393,15 @@ void dev_sgemm(int TA, int TB, int M, int N, int K, float alpha, const float *A,
   if (M <= 0 || N <= 0) return;
   if (alpha == 0.0f || K <= 0) { dev_gescal(M, N, beta, C, ldc, st); return; }
   const bool ta = TA != kNoTrans, tb = TB != kNoTrans;
-  if (N == 1 && o.allow_gemv) {
+  if (N == 1 && o.allow_gemv && o.uplo == 0) {
     gemv_launch<float>(TA, M, K, alpha, A, lda, B, tb ? ldb : 1, beta, C, st);
     return;
   }
   ProfScope ps(st, 2.0 * M * N * K);
-  if (!ta && !tb) sgemm_t<kNoTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma);
-  else if (!ta && tb) sgemm_t<kNoTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma);
-  else if (ta && !tb) sgemm_t<kTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma);
-  else sgemm_t<kTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma);
+  if (!ta && !tb) sgemm_t<kNoTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo);
+  else if (!ta && tb) sgemm_t<kNoTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo);
+  else if (ta && !tb) sgemm_t<kTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo);
+  else sgemm_t<kTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo);
 }
 
 unsigned gemm_status_read_and_clear() {

@@ -9,6 +9,7 @@ struct GemmOpts {
   bool allow_tma = true;   // false forces the cp.async loader (tests cover both)
   int num_sms = 0;         // 0: the device's SM count
   bool allow_gemv = true;  // N == 1 goes to the matrix-vector kernels
+  int uplo = 0;            // kLower / kUpper: update only that triangle of C (M == N), as SYRK
 };
 
 // Column-major C = alpha*op(A)*op(B) + beta*C, all pointers on the device.

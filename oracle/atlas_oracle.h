@@ -6,9 +6,9 @@
  * bench's CPU baseline call it.  The product library never links, loads or
  * calls it.
  *
- * Parity pin: the random generator, laswp, pivot order and the LU / GEMM /
- * TRSM results of this restatement are checked against routines extracted
- * from the reference's own basefiles (oracle/ref_build.sh builds them into
+ * Parity pin: the random generator, laswp, pivot order, Cholesky info and
+ * the LU / Cholesky / GEMM / SYRK / TRSM results of this restatement are
+ * checked against routines extracted from the reference's own basefiles (oracle/ref_build.sh builds them into
  * oracle/_ref/) and against the fixtures in tests/golden/ that were generated
  * from that build (tests/golden/make_golden.py).
  *
@@ -86,6 +86,33 @@ void ora_sgetrs(int Order, int Trans, int N, int NRHS, const float *A,
                 int lda, const int *ipiv, float *B, int ldb);
 int  ora_dgesv(int Order, int N, int NRHS, double *A, int lda, int *ipiv,
                double *B, int ldb);
+
+/* --- SYRK and Cholesky ---------------------------------------------------- */
+/* reference-BLAS SYRK (AtlasBase/Antoine/atlrefblas.base:7573-8100) */
+void ora_dsyrk(int Uplo, int Trans, int N, int K, double alpha, const double *A,
+               int lda, double beta, double *C, int ldc);
+void ora_ssyrk(int Uplo, int Trans, int N, int K, float alpha, const float *A,
+               int lda, float beta, float *C, int ldc);
+/* cblas_syrk order handling (AtlasBase/Clint/cblas.base:440-448) */
+void ora_dcblas_syrk(int Order, int Uplo, int Trans, int N, int K, double alpha,
+                     const double *A, int lda, double beta, double *C, int ldc);
+void ora_scblas_syrk(int Order, int Uplo, int Trans, int N, int K, float alpha,
+                     const float *A, int lda, float beta, float *C, int ldc);
+/* ATL_potrf with the recursive ATL_potrfU / ATL_potrfL
+ * (AtlasBase/Clint/atlas-lp.base:332-968); returns 0 or the 1-based index of
+ * the first non-positive pivot. */
+int  ora_dpotrf(int Order, int Uplo, int N, double *A, int lda);
+int  ora_spotrf(int Order, int Uplo, int N, float *A, int lda);
+/* ATL_potrs (AtlasBase/Clint/atlas-lp.base:969-1052) */
+void ora_dpotrs(int Order, int Uplo, int N, int NRHS, const double *A, int lda,
+                double *B, int ldb);
+void ora_spotrs(int Order, int Uplo, int N, int NRHS, const float *A, int lda,
+                float *B, int ldb);
+/* clapack_posv (AtlasBase/Clint/atlas-clp.base:266-315) */
+int  ora_dposv(int Order, int Uplo, int N, int NRHS, double *A, int lda,
+               double *B, int ldb);
+int  ora_sposv(int Order, int Uplo, int N, int NRHS, float *A, int lda,
+               float *B, int ldb);
 
 /* --- tester residuals ---------------------------------------------------- */
 /* xdlutst residual (AtlasBase/Clint/atlas-tlp.base:1992-2058) for a

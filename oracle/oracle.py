@@ -81,6 +81,16 @@ def _declare(L):
                                         np.ctypeslib.ndpointer(np.float64), np.ctypeslib.ndpointer(np.float64)]),
         "ora_dbackward_error": (_d, [_i, _dp, _i, np.ctypeslib.ndpointer(np.float64),
                                     np.ctypeslib.ndpointer(np.float64)]),
+        "ora_dsyrk": (None, [_i, _i, _i, _i, _d, _dp, _i, _d, _dp, _i]),
+        "ora_ssyrk": (None, [_i, _i, _i, _i, _f, _sp, _i, _f, _sp, _i]),
+        "ora_dcblas_syrk": (None, [_i, _i, _i, _i, _i, _d, _dp, _i, _d, _dp, _i]),
+        "ora_scblas_syrk": (None, [_i, _i, _i, _i, _i, _f, _sp, _i, _f, _sp, _i]),
+        "ora_dpotrf": (_i, [_i, _i, _i, _dp, _i]),
+        "ora_spotrf": (_i, [_i, _i, _i, _sp, _i]),
+        "ora_dpotrs": (None, [_i, _i, _i, _i, _dp, _i, _dp, _i]),
+        "ora_spotrs": (None, [_i, _i, _i, _i, _sp, _i, _sp, _i]),
+        "ora_dposv": (_i, [_i, _i, _i, _i, _dp, _i, _dp, _i]),
+        "ora_sposv": (_i, [_i, _i, _i, _i, _sp, _i, _sp, _i]),
         "ora_set_threads": (_i, [_i]),
         "ora_get_threads": (_i, []),
     }
@@ -122,6 +132,28 @@ def gemm(TA, TB, M, N, K, alpha, A, B, beta, C):
 def trsm(Side, Uplo, TA, Diag, M, N, alpha, A, B):
     f = lib().ora_dtrsm if B.dtype == np.float64 else lib().ora_strsm
     f(Side, Uplo, TA, Diag, M, N, alpha, A, A.shape[0], B, B.shape[0])
+    return B
+
+
+def syrk(Uplo, Trans, N, K, alpha, A, beta, C, order=ColMajor):
+    """C <- alpha*op(A)*op(A)^T + beta*C on the Uplo triangle, in place."""
+    f = lib().ora_dcblas_syrk if C.dtype == np.float64 else lib().ora_scblas_syrk
+    f(order, Uplo, Trans, N, K, alpha, A, A.shape[0], beta, C, C.shape[0])
+    return C
+
+
+def potrf(A, uplo=Lower, N=None, order=ColMajor):
+    """In-place Cholesky of the uplo triangle; returns info."""
+    N = A.shape[1] if N is None else N
+    f = lib().ora_dpotrf if A.dtype == np.float64 else lib().ora_spotrf
+    return f(order, uplo, N, A, A.shape[0])
+
+
+def potrs(A, B, uplo=Lower, N=None, order=ColMajor):
+    N = A.shape[1] if N is None else N
+    f = lib().ora_dpotrs if A.dtype == np.float64 else lib().ora_spotrs
+    nrhs = B.shape[1]
+    f(order, uplo, N, nrhs, A, A.shape[0], B, B.shape[0])
     return B
 
 

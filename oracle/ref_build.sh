@@ -3,10 +3,11 @@
 # the oracle (TEST INFRASTRUCTURE ONLY).
 #
 #  1. compiles the reference's basefile extractor (extract.c) with gcc;
-#  2. extracts, one routine per file, ATL_getrfC/getrfR/getf2/laswp/getrs
-#     (AtlasBase/Clint/atlas-lp.base), ATL_rand/gegen/epsilon
-#     (AtlasBase/Clint/atlas-tst.base) and the C reference BLAS it runs on
-#     (gemm, trsm, ger, scal, swap, iamax from AtlasBase/Antoine/atlrefblas.base);
+#  2. extracts, one routine per file, ATL_getrfC/getrfR/getf2/laswp/getrs and
+#     ATL_potrfU/potrfL/potrf/potrs (AtlasBase/Clint/atlas-lp.base),
+#     ATL_rand/gegen/epsilon (AtlasBase/Clint/atlas-tst.base) and the C
+#     reference BLAS they run on (gemm, trsm, syrk, ger, scal, swap, iamax from
+#     AtlasBase/Antoine/atlrefblas.base);
 #  3. compiles them, double and single precision, with the stand-in headers in
 #     oracle/ref_shim/ into oracle/_ref/libatlref.so.
 # Everything it writes goes to oracle/_ref/ (git-ignored).  The reference's own
@@ -27,7 +28,7 @@ $X -b $R/Clint/atlas.base -o cblas.h rout=cblas.h
 for h in misc lvl3 level3 level1 level2 lvl2; do
    $X -b $R/Antoine/atlrefblas.base -o atlas_ref$h.h rout=atlas_ref$h.h type=none
 done
-RB="gemm gemmNN gemmNT gemmTN gemmTT trsm ger scal swap"
+RB="gemm gemmNN gemmNT gemmTN gemmTT trsm ger scal swap syrk syrkLN syrkLT syrkUN syrkUT"
 for s in L R; do for u in L U; do for t in N T; do for d in N U; do RB="$RB trsm$s$u$t$d"; done; done; done; done
 for r in $RB; do
    $X -b $R/Antoine/atlrefblas.base -o ATL_dref$r.c rout=$r type=dble
@@ -35,7 +36,7 @@ for r in $RB; do
 done
 $X -b $R/Antoine/atlrefblas.base -o ATL_idrefamax.c rout=amax type=dble
 $X -b $R/Antoine/atlrefblas.base -o ATL_isrefamax.c rout=amax type=real
-for r in ATL_getrfC ATL_getrfR ATL_getf2 ATL_laswp ATL_getrs; do
+for r in ATL_getrfC ATL_getrfR ATL_getf2 ATL_laswp ATL_getrs ATL_potrfU ATL_potrfL ATL_potrf ATL_potrs; do
    $X -b $R/Clint/atlas-lp.base -o $r.c rout=$r 2>/dev/null
 done
 for r in ATL_rand ATL_gegen ATL_epsilon; do
@@ -45,7 +46,8 @@ CF="-O2 -fPIC -w -ffp-contract=off -fno-strict-aliasing -fwrapv -I$SRC -I$HERE/r
 OBJ=""
 for f in ATL_dref*.c ATL_idrefamax.c; do $CC $CF -DDREAL -c $f -o ${f%.c}.o; OBJ="$OBJ ${f%.c}.o"; done
 for f in ATL_sref*.c ATL_isrefamax.c; do $CC $CF -DSREAL -c $f -o ${f%.c}.o; OBJ="$OBJ ${f%.c}.o"; done
-for f in ATL_getrfC ATL_getrfR ATL_getf2 ATL_laswp ATL_getrs ATL_gegen ATL_epsilon; do
+for f in ATL_getrfC ATL_getrfR ATL_getf2 ATL_laswp ATL_getrs ATL_potrfU ATL_potrfL ATL_potrf ATL_potrs \
+         ATL_gegen ATL_epsilon; do
    $CC $CF -DDREAL -c $f.c -o d_$f.o
    $CC $CF -DSREAL -c $f.c -o s_$f.o
    OBJ="$OBJ d_$f.o s_$f.o"

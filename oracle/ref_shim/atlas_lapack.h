@@ -18,6 +18,20 @@ void ATL_dgetrs(const enum CBLAS_ORDER, const enum CBLAS_TRANSPOSE, const int, c
                 const double*, const int, const int*, double*, const int);
 void ATL_sgetrs(const enum CBLAS_ORDER, const enum CBLAS_TRANSPOSE, const int, const int,
                 const float*, const int, const int*, float*, const int);
+#define ATL_potrfU Mjoin(PATL,potrfU)
+#define ATL_potrfL Mjoin(PATL,potrfL)
+#define ATL_potrf  Mjoin(PATL,potrf)
+#define ATL_potrs  Mjoin(PATL,potrs)
+int  ATL_dpotrfU(const int, double*, const int);
+int  ATL_spotrfU(const int, float*, const int);
+int  ATL_dpotrfL(const int, double*, const int);
+int  ATL_spotrfL(const int, float*, const int);
+int  ATL_dpotrf(const enum ATLAS_ORDER, const enum ATLAS_UPLO, const int, double*, const int);
+int  ATL_spotrf(const enum ATLAS_ORDER, const enum ATLAS_UPLO, const int, float*, const int);
+void ATL_dpotrs(const enum CBLAS_ORDER, const enum CBLAS_UPLO, const int, const int, const double*,
+                const int, double*, const int);
+void ATL_spotrs(const enum CBLAS_ORDER, const enum CBLAS_UPLO, const int, const int, const float*,
+                const int, float*, const int);
 void ATL_dger(const int, const int, const double, const double*, const int, const double*,
               const int, double*, const int);
 void ATL_sger(const int, const int, const float, const float*, const int, const float*,

@@ -26,6 +26,11 @@ void ATL_##P##laswp(const int, T*, const int, const int, const int, const int*, 
 void ATL_##P##getrs(const enum CBLAS_ORDER, const enum CBLAS_TRANSPOSE, const int, const int, \
    const T*, const int, const int*, T*, const int); \
 void ATL_##P##gegen(const int, const int, T*, const int, const int); \
+void ATL_##P##refsyrk(const enum ATLAS_UPLO, const enum ATLAS_TRANS, const int, const int, const T, \
+   const T*, const int, const T, T*, const int); \
+int  ATL_##P##potrf(const enum ATLAS_ORDER, const enum ATLAS_UPLO, const int, T*, const int); \
+void ATL_##P##potrs(const enum CBLAS_ORDER, const enum CBLAS_UPLO, const int, const int, const T*, \
+   const int, T*, const int); \
 \
 void refshim_##P##gemm(enum CBLAS_ORDER o, enum CBLAS_TRANSPOSE ta, enum CBLAS_TRANSPOSE tb, \
    int M, int N, int K, T al, const T *A, int lda, const T *B, int ldb, T be, T *C, int ldc) \
@@ -86,7 +91,25 @@ void atlref_##P##trsm(int order, int s, int u, int t, int d, int M, int N, T al,
    T *B, int ldb) \
 { refshim_##P##trsm((enum CBLAS_ORDER)order, (enum CBLAS_SIDE)s, (enum CBLAS_UPLO)u, \
                     (enum CBLAS_TRANSPOSE)t, (enum CBLAS_DIAG)d, M, N, al, A, lda, B, ldb); } \
-int atlref_i##P##amax(int N, const T *X, int incx) { return ATL_i##P##refamax(N, X, incx); }
+int atlref_i##P##amax(int N, const T *X, int incx) { return ATL_i##P##refamax(N, X, incx); } \
+/* cblas_syrk's RowMajor flip of Uplo and Trans (AtlasBase/Clint/cblas.base:440-448) */ \
+void refshim_##P##syrk(enum CBLAS_ORDER o, enum CBLAS_UPLO u, enum CBLAS_TRANSPOSE t, int N, int K, \
+   T al, const T *A, int lda, T be, T *C, int ldc) \
+{ \
+   if (o == CblasColMajor) \
+      ATL_##P##refsyrk((enum ATLAS_UPLO)u, (enum ATLAS_TRANS)t, N, K, al, A, lda, be, C, ldc); \
+   else \
+      ATL_##P##refsyrk(u == CblasUpper ? AtlasLower : AtlasUpper, \
+                       t == CblasNoTrans ? AtlasTrans : AtlasNoTrans, N, K, al, A, lda, be, C, ldc); \
+} \
+void atlref_##P##syrk(int order, int u, int t, int N, int K, T al, const T *A, int lda, T be, T *C, \
+   int ldc) \
+{ refshim_##P##syrk((enum CBLAS_ORDER)order, (enum CBLAS_UPLO)u, (enum CBLAS_TRANSPOSE)t, N, K, al, A, lda, \
+                    be, C, ldc); } \
+int  atlref_##P##potrf(int order, int u, int N, T *A, int lda) \
+{ return ATL_##P##potrf((enum ATLAS_ORDER)order, (enum ATLAS_UPLO)u, N, A, lda); } \
+void atlref_##P##potrs(int order, int u, int N, int NRHS, const T *A, int lda, T *B, int ldb) \
+{ ATL_##P##potrs((enum CBLAS_ORDER)order, (enum CBLAS_UPLO)u, N, NRHS, A, lda, B, ldb); }
 
 DEF_REF(double, d)
 DEF_REF(float, s)

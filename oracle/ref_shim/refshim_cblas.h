@@ -20,6 +20,10 @@ void refshim_dgemv(enum CBLAS_ORDER, enum CBLAS_TRANSPOSE, int, int, double, con
                    const double*, int, double, double*, int);
 void refshim_sgemv(enum CBLAS_ORDER, enum CBLAS_TRANSPOSE, int, int, float, const float*, int,
                    const float*, int, float, float*, int);
+void refshim_dsyrk(enum CBLAS_ORDER, enum CBLAS_UPLO, enum CBLAS_TRANSPOSE, int, int, double,
+                   const double*, int, double, double*, int);
+void refshim_ssyrk(enum CBLAS_ORDER, enum CBLAS_UPLO, enum CBLAS_TRANSPOSE, int, int, float,
+                   const float*, int, float, float*, int);
 int  refshim_idamax(int, const double*, int);
 int  refshim_isamax(int, const float*, int);
 void refshim_dscal(int, double, double*, int);
@@ -30,6 +34,7 @@ void refshim_sswap(int, float*, int, float*, int);
 #if defined(DREAL)
    #define cblas_gemm refshim_dgemm
    #define cblas_trsm refshim_dtrsm
+   #define cblas_syrk refshim_dsyrk
    #define cblas_trsv refshim_dtrsv
    #define cblas_gemv refshim_dgemv
    #define cblas_iamax refshim_idamax
@@ -38,6 +43,7 @@ void refshim_sswap(int, float*, int, float*, int);
 #else
    #define cblas_gemm refshim_sgemm
    #define cblas_trsm refshim_strsm
+   #define cblas_syrk refshim_ssyrk
    #define cblas_trsv refshim_strsv
    #define cblas_gemv refshim_sgemv
    #define cblas_iamax refshim_isamax

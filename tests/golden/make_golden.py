@@ -40,6 +40,12 @@ def load():
     R.atlref_dlaswp.argtypes = [I, dp, I, I, I, ip, I]
     R.atlref_dgemm.argtypes = [I, I, I, I, I, I, D, dp, I, dp, I, D, dp, I]
     R.atlref_dtrsm.argtypes = [I, I, I, I, I, I, I, D, dp, I, dp, I]
+    R.atlref_dsyrk.argtypes = [I, I, I, I, I, D, dp, I, D, dp, I]
+    R.atlref_dpotrf.argtypes = [I, I, I, dp, I]
+    R.atlref_dpotrf.restype = I
+    R.atlref_spotrf.argtypes = [I, I, I, sp, I]
+    R.atlref_spotrf.restype = I
+    R.atlref_dpotrs.argtypes = [I, I, I, I, dp, I, dp, I]
     return R
 
 
@@ -53,6 +59,14 @@ def gegen(R, M, N, lda, seed, dtype=np.float64):
 LU_CASES = [(1, 1, 1), (2, 2, 2), (3, 5, 4), (5, 3, 7), (17, 17, 17), (64, 64, 64),
             (100, 100, 103), (37, 80, 40), (80, 37, 80), (129, 129, 130), (200, 200, 200),
             (257, 513, 260)]
+# (N, lda) of the Cholesky fixtures; the SPD input is G G^T + N I from a
+# gegen matrix G, built here once and stored
+CHOL_CASES = [(1, 1), (2, 3), (3, 3), (4, 6), (5, 5), (7, 9), (17, 17), (64, 64), (100, 103),
+              (129, 130), (200, 200)]
+# (N, lda, bad): the CHOL_CASES input with A[bad, bad] = -1
+CHOL_BAD = [(17, 17, 3), (100, 103, 57), (129, 130, 128), (64, 64, 0), (200, 200, 199)]
+SYRK_CASES = [(121, 111, 37, 29), (122, 111, 37, 29), (121, 112, 20, 45), (122, 112, 20, 45),
+              (122, 111, 64, 1)]
 GEMM_CASES = [(111, 111, 37, 29, 41, 1.0, 0.0), (111, 112, 64, 64, 64, 1.0, 0.0),
               (112, 111, 33, 65, 17, -1.5, 0.5), (112, 112, 50, 20, 70, 0.75, -2.0),
               (111, 111, 128, 96, 1, 1.0, 1.0)]
@@ -150,6 +164,45 @@ def main():
                     B = gegen(R, M, N, M, M * N + 3)
                     R.atlref_dtrsm(102, side, uplo, ta, diag, M, N, 1.5, A, na, B, M)
                     out[f"trsm_{side}_{uplo}_{ta}_{diag}"] = B
+    # reference-BLAS syrk through cblas_syrk's order mapping
+    out["syrk_cases"] = np.array(SYRK_CASES, dtype=np.int64)
+    for (uplo, tr, N, K) in SYRK_CASES:
+        for order in (101, 102):
+            nt = (tr == 111) == (order == 102)      # A stored with N rows
+            lda, cols = (N, K) if nt else (K, N)
+            A = gegen(R, lda, cols, lda, 99 + N + K)
+            Cm = gegen(R, N, N, N, 5 + N)
+            R.atlref_dsyrk(order, uplo, tr, N, K, 1.5, A, lda, 0.5, Cm, N)
+            out[f"syrk_{order}_{uplo}_{tr}_{N}_{K}"] = Cm
+
+    # Cholesky: ATL_potrf for both triangles and orders, then ATL_potrs
+    out["chol_cases"] = np.array(CHOL_CASES, dtype=np.int64)
+    for (n, lda) in CHOL_CASES:
+        G = gegen(R, n, n, n, n * n + lda)
+        A = np.full((lda, n), -2.56e9, order="F")
+        A[:n, :n] = G @ G.T + n * np.eye(n)
+        A[:n, :n] = 0.5 * (A[:n, :n] + A[:n, :n].T)
+        out[f"chol_{n}_{lda}_a"] = A
+        for uplo in (121, 122):
+            for order in (101, 102):
+                F = A.copy(order="F")
+                info = R.atlref_dpotrf(order, uplo, n, F, lda)
+                out[f"chol_{n}_{lda}_{uplo}_{order}_info"] = np.array(info)
+                if n <= 130:
+                    out[f"chol_{n}_{lda}_{uplo}_{order}_f"] = F
+                    B = gegen(R, n, 3, n, 77 + n)
+                    R.atlref_dpotrs(order, uplo, n, 3, F, lda, B, n)
+                    out[f"chol_{n}_{lda}_{uplo}_{order}_x"] = B
+        Fs = A.astype(np.float32, order="F")
+        out[f"chol_{n}_{lda}_s_info"] = np.array(R.atlref_spotrf(102, 122, n, Fs, lda))
+    # not positive definite: a negative diagonal entry (info = its 1-based index)
+    out["chol_bad"] = np.array(CHOL_BAD, dtype=np.int64)
+    for (n, lda, bad) in CHOL_BAD:
+        A = out[f"chol_{n}_{lda}_a"].copy(order="F")
+        A[bad, bad] = -1.0
+        for uplo in (121, 122):
+            F = A.copy(order="F")
+            out[f"cholbad_{n}_{bad}_{uplo}_info"] = np.array(R.atlref_dpotrf(102, uplo, n, F, lda))
     np.savez_compressed(OUT, **out)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")
 

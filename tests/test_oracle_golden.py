@@ -107,3 +107,66 @@ def test_lu_residual_within_tester_threshold(ora):
         A = ora.gegen(M, N, M * N + M)
         info, ipiv = ora.getrf(A)
         assert ora.lu_resid(M, N, A, ipiv, M * N + M) <= 100.0
+
+
+def test_syrk_bit_exact_with_reference_blas(ora, golden):
+    for (uplo, tr, N, K) in golden["syrk_cases"]:
+        uplo, tr, N, K = int(uplo), int(tr), int(N), int(K)
+        for order in (101, 102):
+            nt = (tr == 111) == (order == 102)
+            lda, cols = (N, K) if nt else (K, N)
+            A = ora.gegen(lda, cols, 99 + N + K)
+            Cm = ora.gegen(N, N, 5 + N)
+            ora.syrk(uplo, tr, N, K, 1.5, A, 0.5, Cm, order=order)
+            assert np.array_equal(Cm, golden[f"syrk_{order}_{uplo}_{tr}_{N}_{K}"]), (order, uplo, tr)
+
+
+def test_syrk_touches_one_triangle(ora):
+    N, K = 30, 11
+    A = ora.gegen(N, K, 3)
+    Cm = ora.gegen(N, N, 4)
+    C0 = Cm.copy(order="F")
+    ora.syrk(ora.Lower, ora.NoTrans, N, K, 1.0, A, 0.0, Cm)
+    iu = np.triu_indices(N, 1)
+    assert np.array_equal(Cm[iu], C0[iu])
+    assert np.allclose(np.tril(Cm), np.tril(A @ A.T), rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("uplo", [121, 122])
+@pytest.mark.parametrize("order", [101, 102])
+def test_potrf_potrs_match_reference(ora, golden, uplo, order):
+    for (n, lda) in golden["chol_cases"]:
+        n, lda = int(n), int(lda)
+        key = f"chol_{n}_{lda}_{uplo}_{order}"
+        F = golden[f"chol_{n}_{lda}_a"].copy(order="F")
+        info = ora.potrf(F, uplo=uplo, N=n, order=order)
+        assert info == int(golden[key + "_info"]) == 0
+        if key + "_f" not in golden:
+            continue
+        ref = golden[key + "_f"]
+        # bit-exact through the unrolled 1..4 cases and one level of recursion;
+        # deeper, the TRSM summation order differs from the reference BLAS
+        if n <= 17:
+            assert np.array_equal(F, ref), key
+        assert np.abs(F - ref).max() <= 1e-13 * n, key
+        assert (F[n:] == -2.56e9).all()
+        B = ora.gegen(n, 3, 77 + n)
+        ora.potrs(F, B, uplo=uplo, N=n, order=order)
+        assert np.allclose(B, golden[key + "_x"], rtol=1e-11, atol=1e-13), key
+
+
+def test_potrf_info_not_positive_definite(ora, golden):
+    for (n, lda, bad) in golden["chol_bad"]:
+        n, lda, bad = int(n), int(lda), int(bad)
+        for uplo in (121, 122):
+            A = golden[f"chol_{n}_{lda}_a"].copy(order="F")
+            A[bad, bad] = -1.0
+            info = ora.potrf(A, uplo=uplo, N=n)
+            assert info == int(golden[f"cholbad_{n}_{bad}_{uplo}_info"]) == bad + 1
+
+
+def test_spotrf_info(ora, golden):
+    for (n, lda) in golden["chol_cases"]:
+        n, lda = int(n), int(lda)
+        F = golden[f"chol_{n}_{lda}_a"].astype(np.float32, order="F")
+        assert ora.potrf(F, uplo=ora.Lower, N=n) == int(golden[f"chol_{n}_{lda}_s_info"])
