@@ -254,6 +254,61 @@ def measure_forms(G, O, torch, n=16384, kappas=(1e2, 1e6, 1e10), nslices=8):
     return out
 
 
+def spd_device(torch, n, seed):
+    """Symmetric S with entries uniform(-0.5, 0.5) plus n*I on the device,
+    column-major (symmetric, so row-major is the same); positive definite by
+    Gershgorin (every eigenvalue >= n/2)."""
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    A = torch.rand(n, n, device="cuda", dtype=torch.float64, generator=g) - 0.5
+    A = (A + A.T) * 0.5
+    A.diagonal().add_(float(n))
+    return A
+
+
+def measure_next(G, O, torch, n=16384):
+    """Rows beyond the LU path, same bar: the Cholesky solve (dpotrf +
+    dpotrs, Lower) at n, timed on the device API, its backward error, and
+    the oracle's recursive potrf on a bounded host sample."""
+    import ctypes as C
+    L = G.lib()
+    st = L.atlg_stream()
+    out = {}
+    A0 = spd_device(torch, n, 11)
+    b = torch.rand(n, device="cuda", dtype=torch.float64) - 0.5
+    A = torch.empty_like(A0)
+    ts = []
+    for rep in range(3):
+        A.copy_(A0)
+        x = b.clone()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        info = L.atlg_dpotrf_dev(122, n, C.c_void_p(A.data_ptr()), n, st)
+        L.atlg_dpotrs_dev(102, 122, n, 1, C.c_void_p(A.data_ptr()), n, C.c_void_p(x.data_ptr()), n, st)
+        torch.cuda.synchronize()
+        if rep:
+            ts.append(time.perf_counter() - t0)
+    r = b - A0 @ x
+    berr = float(r.abs().max() / (A0.abs().sum(dim=1).max() * x.abs().max() + b.abs().max()))
+    sec = min(ts)
+    flops = n ** 3 / 3.0 + 2.0 * n * n
+    row = {"n": n, "uplo": "Lower", "ms": sec * 1e3, "tflops": flops / sec / 1e12, "info": info,
+           "backward_error": berr, "n_eps": n * np.finfo(float).eps,
+           "timing": "wall clock around dpotrf+dpotrs on the library stream (potrf reads info once per "
+                     "64-column block), best of 2 after one warm-up"}
+    del A, A0
+    torch.cuda.empty_cache()
+    # oracle: the reference's recursive potrfL restated, on the host cores
+    nc = 2048
+    Ah = np.asfortranarray(spd_device(torch, nc, 12).cpu().numpy())
+    t0 = time.perf_counter()
+    O.potrf(Ah, uplo=O.Lower)
+    tc = time.perf_counter() - t0
+    row["cpu_baseline"] = {"value": nc ** 3 / 3.0 / tc / 1e12, "unit": "TFLOP/s", "cores": 1, "kind": "port",
+                           "sample": f"oracle recursive potrfL n={nc} (reference-BLAS trsm/syrk, one thread)"}
+    out["dposv_cholesky_n16384"] = row
+    return out
+
+
 # ------------------------------------------------------------------ GPU side
 def run_gpu(args):
     import torch
@@ -377,8 +432,10 @@ def run_gpu(args):
                    "sample": f"one dgesv n={ncpu} nrhs=1 (oracle restatement of getrfC/getrs, OpenMP)"}
         bwd = O.backward_error(np.asfortranarray(A_h), x, b_h.reshape(-1))
         forms = None
+        nxt = None
         if world == 1 and not args.skip_extras:
             forms = measure_forms(G, O, torch)
+            nxt = measure_next(G, O, torch)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
@@ -399,6 +456,8 @@ def run_gpu(args):
         }
         if forms is not None:
             line["forms"] = forms
+        if nxt is not None:
+            line["next_rows"] = nxt
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
@@ -411,6 +470,7 @@ def run_case(args):
     split  -- split-precision DGEMM n^3 (7 slices), run twice
     sgetrf -- FP32 LU (FFMA trailing update) at n
     mixed  -- mixed-precision dgesv at n on A = G/sqrt(n) + 4I, run twice
+    potrf  -- FP64 Cholesky (Lower) at n on a diagonally dominant SPD matrix
     Prints one JSON line with the device time of the last run."""
     import ctypes as C
     import torch
@@ -443,6 +503,16 @@ def run_case(args):
         e1.record(s)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
+    elif args.case == "potrf":
+        A0 = spd_device(torch, n, 11)
+        A = torch.empty_like(A0)
+        for _ in range(2):
+            A.copy_(A0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            L.atlg_dpotrf_dev(122, n, C.c_void_p(A.data_ptr()), n, st)
+            torch.cuda.synchronize()
+            ms = (time.perf_counter() - t0) * 1e3
     else:
         A0 = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g) / n ** 0.5 + \
             4 * torch.eye(n, device="cuda", dtype=torch.float64)
@@ -471,7 +541,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=8192)
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
-    ap.add_argument("--case", choices=["split", "sgetrf", "mixed"], default=None,
+    ap.add_argument("--case", choices=["split", "sgetrf", "mixed", "potrf"], default=None,
                     help="run one kernel workload for a profiling capture instead of the benchmark")
     ap.add_argument("--skip-extras", action="store_true",
                     help="omit the n=16384 mixed-dgesv and split-DGEMM measurements")

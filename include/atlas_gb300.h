@@ -68,6 +68,33 @@ void cblas_strsm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side,
                  const enum CBLAS_DIAG Diag, const int M, const int N, const float alpha,
                  const float *A, const int lda, float *B, const int ldb);
 
+/* ---- Level 3: AtlasBase/Clint/cblas.base:587-692 (TRMM, the TRSM template's
+ *      twin: same checks and RowMajor mapping; d and s) */
+void cblas_dtrmm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side,
+                 const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TA,
+                 const enum CBLAS_DIAG Diag, const int M, const int N, const double alpha,
+                 const double *A, const int lda, double *B, const int ldb);
+void cblas_strmm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side,
+                 const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TA,
+                 const enum CBLAS_DIAG Diag, const int M, const int N, const float alpha,
+                 const float *A, const int lda, float *B, const int ldb);
+
+/* ---- Level 2: AtlasBase/Clint/cblas-lvl2.base:21-93 (GEMV, d and s) */
+void cblas_dgemv(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TA, const int M,
+                 const int N, const double alpha, const double *A, const int lda,
+                 const double *X, const int incX, const double beta, double *Y,
+                 const int incY);
+void cblas_sgemv(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TA, const int M,
+                 const int N, const float alpha, const float *A, const int lda,
+                 const float *X, const int incX, const float beta, float *Y, const int incY);
+/* ---- Level 2: AtlasBase/Clint/cblas-lvl2.base:273-357 (TRSV, d and s) */
+void cblas_dtrsv(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo,
+                 const enum CBLAS_TRANSPOSE TA, const enum CBLAS_DIAG Diag, const int N,
+                 const double *A, const int lda, double *X, const int incX);
+void cblas_strsv(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo,
+                 const enum CBLAS_TRANSPOSE TA, const enum CBLAS_DIAG Diag, const int N,
+                 const float *A, const int lda, float *X, const int incX);
+
 /* ---- Level 3: AtlasBase/Clint/cblas.base:339-450 (SYRK template, d and s) */
 void cblas_dsyrk(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo,
                  const enum CBLAS_TRANSPOSE Trans, const int N, const int K,
@@ -194,6 +221,14 @@ int atlg_dsyrk_dev(int Uplo, int Trans, int N, int K, double alpha, const double
 int atlg_dpotrf_dev(int Uplo, int N, double *A, int lda, void *stream);
 int atlg_dpotrs_dev(int Order, int Uplo, int N, int NRHS, const double *A, int lda, double *B,
                     int ldb, void *stream);
+/* column-major TRMM; GEMV with M, N the dimensions of A (a negative incX
+ * counts from the far end; y contiguous); TRSV with incX = 1 */
+int atlg_dtrmm_dev(int Side, int Uplo, int TA, int Diag, int M, int N, double alpha,
+                   const double *A, int lda, double *B, int ldb, void *stream);
+int atlg_dgemv_dev(int TA, int M, int N, double alpha, const double *A, int lda,
+                   const double *X, int incX, double beta, double *Y, void *stream);
+int atlg_dtrsv_dev(int Uplo, int TA, int Diag, int N, const double *A, int lda, double *X,
+                   void *stream);
 /* berr, ferr (NRHS entries), iters and status are host pointers; synchronizes */
 int atlg_dgesv_mixed_dev(int N, int NRHS, double *A, int lda, int *ipiv, const double *B,
                          int ldb, double *X, int ldx, double *berr, double *ferr, int *iters,

@@ -31,6 +31,8 @@ EXPORTS = [
     "atlg_dlaswp_noalloc", "dgemm_split", "atlg_dgemm_split_dev", "atlg_sgemm_tf32x3_dev",
     "cblas_dsyrk", "cblas_ssyrk", "clapack_dpotrf", "clapack_spotrf", "clapack_dpotrs", "clapack_spotrs",
     "clapack_dposv", "clapack_sposv", "atlg_dsyrk_dev", "atlg_dpotrf_dev", "atlg_dpotrs_dev",
+    "cblas_dtrmm", "cblas_strmm", "cblas_dgemv", "cblas_sgemv", "cblas_dtrsv", "cblas_strsv",
+    "atlg_dtrmm_dev", "atlg_dgemv_dev", "atlg_dtrsv_dev",
 ]
 
 _lib = None
@@ -53,6 +55,8 @@ def lib():
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="F_CONTIGUOUS")
 _sp = np.ctypeslib.ndpointer(dtype=np.float32, flags="F_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_v1d = np.ctypeslib.ndpointer(dtype=np.float64, ndim=1, flags="C_CONTIGUOUS")
+_v1s = np.ctypeslib.ndpointer(dtype=np.float32, ndim=1, flags="C_CONTIGUOUS")
 _i, _d, _f, _v, _u = C.c_int, C.c_double, C.c_float, C.c_void_p, C.c_uint
 
 
@@ -79,6 +83,15 @@ def _declare(L):
         "atlg_dsyrk_dev": (_i, [_i, _i, _i, _i, _d, _v, _i, _d, _v, _i, _v]),
         "atlg_dpotrf_dev": (_i, [_i, _i, _v, _i, _v]),
         "atlg_dpotrs_dev": (_i, [_i, _i, _i, _i, _v, _i, _v, _i, _v]),
+        "cblas_dtrmm": (None, [_i, _i, _i, _i, _i, _i, _i, _d, _dp, _i, _dp, _i]),
+        "cblas_strmm": (None, [_i, _i, _i, _i, _i, _i, _i, _f, _sp, _i, _sp, _i]),
+        "cblas_dgemv": (None, [_i, _i, _i, _i, _d, _dp, _i, _v1d, _i, _d, _v1d, _i]),
+        "cblas_sgemv": (None, [_i, _i, _i, _i, _f, _sp, _i, _v1s, _i, _f, _v1s, _i]),
+        "cblas_dtrsv": (None, [_i, _i, _i, _i, _i, _dp, _i, _v1d, _i]),
+        "cblas_strsv": (None, [_i, _i, _i, _i, _i, _sp, _i, _v1s, _i]),
+        "atlg_dtrmm_dev": (_i, [_i, _i, _i, _i, _i, _i, _d, _v, _i, _v, _i, _v]),
+        "atlg_dgemv_dev": (_i, [_i, _i, _i, _d, _v, _i, _v, _i, _d, _v, _v]),
+        "atlg_dtrsv_dev": (_i, [_i, _i, _i, _i, _v, _i, _v, _v]),
         "atlg_num_sms": (_i, []),
         "atlg_stream": (_v, []),
         "atlg_status": (_u, []),
@@ -152,6 +165,30 @@ def clapack_dgesv(order, N, NRHS, A, lda, ipiv, B, ldb):
 
 def clapack_sgesv(order, N, NRHS, A, lda, ipiv, B, ldb):
     return lib().clapack_sgesv(order, N, NRHS, A, lda, ipiv, B, ldb)
+
+
+def cblas_dtrmm(order, side, uplo, ta, diag, M, N, alpha, A, lda, B, ldb):
+    lib().cblas_dtrmm(order, side, uplo, ta, diag, M, N, alpha, A, lda, B, ldb)
+
+
+def cblas_strmm(order, side, uplo, ta, diag, M, N, alpha, A, lda, B, ldb):
+    lib().cblas_strmm(order, side, uplo, ta, diag, M, N, alpha, A, lda, B, ldb)
+
+
+def cblas_dgemv(order, ta, M, N, alpha, A, lda, X, incx, beta, Y, incy):
+    lib().cblas_dgemv(order, ta, M, N, alpha, A, lda, X, incx, beta, Y, incy)
+
+
+def cblas_sgemv(order, ta, M, N, alpha, A, lda, X, incx, beta, Y, incy):
+    lib().cblas_sgemv(order, ta, M, N, alpha, A, lda, X, incx, beta, Y, incy)
+
+
+def cblas_dtrsv(order, uplo, ta, diag, N, A, lda, X, incx):
+    lib().cblas_dtrsv(order, uplo, ta, diag, N, A, lda, X, incx)
+
+
+def cblas_strsv(order, uplo, ta, diag, N, A, lda, X, incx):
+    lib().cblas_strsv(order, uplo, ta, diag, N, A, lda, X, incx)
 
 
 def cblas_dsyrk(order, uplo, trans, N, K, alpha, A, lda, beta, Cm, ldc):

@@ -10,11 +10,15 @@
 //
 // Argument checking follows AtlasBase/Clint/cblas.base (cblas_errprn :14,
 // cblas_xerbla :42 -- message to stderr and exit(-1); GEMM checks :119-216,
-// TRSM checks :611-677) and AtlasBase/Clint/atlas-clp.base (clapack_gesv :62,
-// clapack_getrf :140, clapack_getrs :218).
+// TRSM/TRMM checks :611-677, SYRK :356-449), AtlasBase/Clint/cblas-lvl2.base
+// (GEMV :21-93, TRSV :273-357) and AtlasBase/Clint/atlas-clp.base
+// (clapack_gesv :62, clapack_getrf :140, clapack_getrs :218, clapack_posv
+// :266, clapack_potrf :320, clapack_potrs :363).
 #include <stdarg.h>
 #include <stdlib.h>
 #include <string.h>
+
+#include <vector>
 
 #include "../../include/atlas_gb300.h"
 #include "common.cuh"
@@ -25,6 +29,7 @@
 #include "mixed.cuh"
 #include "split.cuh"
 #include "tf32.cuh"
+#include "trmm.cuh"
 #include "trsm.cuh"
 
 using namespace atlg;
@@ -529,6 +534,143 @@ int host_posv(const char *rout, int Order, int Uplo, int N, int NRHS, T *A, int 
   return info;
 }
 
+// ---------------------------------------------------------------- TRMM
+template <typename T>
+void dev_trmm_any(int side, int uplo, int ta, int diag, int M, int N, T alpha, const T *A, int lda, T *B, int ldb,
+                  cudaStream_t st) {
+  if (sizeof(T) == 8)
+    dev_dtrmm(side, uplo, ta, diag, M, N, (double)alpha, (const double *)A, lda, (double *)B, ldb, st);
+  else
+    dev_strmm(side, uplo, ta, diag, M, N, (float)alpha, (const float *)A, lda, (float *)B, ldb, st);
+}
+
+// cblas_?trmm: TRSM's checks and RowMajor flip (AtlasBase/Clint/cblas.base:587-692).
+template <typename T>
+void host_trmm(const char *rout, int Order, int Side, int Uplo, int TA, int Diag, int M, int N, T alpha, const T *A,
+               int lda, T *B, int ldb) {
+  if (trsm_check(rout, Order, Side, Uplo, TA, Diag, M, N, lda, ldb)) return;
+  if (Order == CblasRowMajor) {
+    Side = (Side == CblasLeft) ? CblasRight : CblasLeft;
+    Uplo = (Uplo == CblasUpper) ? CblasLower : CblasUpper;
+    const int t = M; M = N; N = t;
+  }
+  if (M == 0 || N == 0) return;
+  cudaStream_t st = ctx().stream;
+  const int na = (Side == CblasLeft) ? M : N;
+  int ldd_a, ldd_b;
+  const T *dA = to_dev<T>(kBufA, A, na, na, lda, &ldd_a, st);
+  T *dB = to_dev<T>(kBufB, B, M, N, ldb, &ldd_b, st);
+  dev_trmm_any<T>(Side, Uplo, TA, Diag, M, N, alpha, dA, ldd_a, dB, ldd_b, st);
+  to_host<T>(B, ldb, dB, ldd_b, M, N, st);
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  check_status(rout);
+}
+
+// ------------------------------------------------------------ GEMV, TRSV
+// Strided host vector <-> contiguous copy; a negative increment counts from
+// the far end, as the cblas wrappers arrange (AtlasBase/Clint/cblas-lvl2.base:
+// 71-80, 339).
+template <typename T>
+void vec_pack(std::vector<T> &v, const T *X, int n, int inc) {
+  v.resize(n > 0 ? n : 1);
+  for (int i = 0; i < n; ++i) v[i] = X[inc > 0 ? (size_t)i * inc : (size_t)(n - 1 - i) * (size_t)(-inc)];
+}
+template <typename T>
+void vec_unpack(const std::vector<T> &v, T *X, int n, int inc) {
+  for (int i = 0; i < n; ++i) X[inc > 0 ? (size_t)i * inc : (size_t)(n - 1 - i) * (size_t)(-inc)] = v[i];
+}
+
+template <typename T>
+void host_gemv(const char *rout, int Order, int TA, int M, int N, T alpha, const T *A, int lda, const T *X, int incX,
+               T beta, T *Y, int incY) {
+  int info = 2000;
+  if (TA != CblasNoTrans && TA != CblasTrans && TA != CblasConjTrans)
+    info = cblas_errprn(2, info, "TransA must be %d, %d or %d, but is set to %d", CblasNoTrans, CblasTrans,
+                        CblasConjTrans, TA);
+  if (M < 0) info = cblas_errprn(3, info, "M cannot be less than zero; is set to %d.", M);
+  if (N < 0) info = cblas_errprn(4, info, "N cannot be less than zero; is set to %d.", N);
+  if (!incX) info = cblas_errprn(9, info, "incX cannot be zero; is set to %d.", incX);
+  if (!incY) info = cblas_errprn(12, info, "incY cannot be zero; is set to %d.", incY);
+  if (Order == CblasColMajor) {
+    if (lda < M || lda < 1) info = cblas_errprn(7, info, "lda must be >= MAX(M,1): lda=%d M=%d", lda, M);
+  } else if (Order == CblasRowMajor) {
+    if (lda < N || lda < 1) info = cblas_errprn(7, info, "lda must be >= MAX(N,1): lda=%d N=%d", lda, N);
+  } else
+    info = cblas_errprn(1, info, "Order must be %d or %d, but is set to %d", CblasRowMajor, CblasColMajor, Order);
+  if (info != 2000) {
+    cblas_xerbla(info, rout, "");
+    return;
+  }
+  if (M == 0 || N == 0) return;
+  const int lx = (TA == CblasNoTrans) ? N : M, ly = (TA == CblasNoTrans) ? M : N;
+  // column-major view: A has ra x ca entries; op is TA (ColMajor) or its flip
+  const int ra = (Order == CblasColMajor) ? M : N, ca = (Order == CblasColMajor) ? N : M;
+  int op = (TA == CblasNoTrans) ? kNoTrans : kTrans;
+  if (Order == CblasRowMajor) op = (op == kNoTrans) ? kTrans : kNoTrans;
+  cudaStream_t st = ctx().stream;
+  std::vector<T> hx, hy;
+  vec_pack(hx, X, lx, incX);
+  if (beta != T(0)) vec_pack(hy, Y, ly, incY);
+  else hy.assign(ly, T(0));
+  int ldd_a;
+  const T *dA = to_dev<T>(kBufA, A, ra, ca, lda, &ldd_a, st);
+  T *dx = static_cast<T *>(ctx().buffer(kBufB, sizeof(T) * (size_t)lx));
+  T *dy = static_cast<T *>(ctx().buffer(kBufC, sizeof(T) * (size_t)ly));
+  ATLG_CHECK(cudaMemcpyAsync(dx, hx.data(), sizeof(T) * lx, cudaMemcpyHostToDevice, st));
+  if (beta != T(0)) ATLG_CHECK(cudaMemcpyAsync(dy, hy.data(), sizeof(T) * ly, cudaMemcpyHostToDevice, st));
+  if (sizeof(T) == 8)
+    dev_dgemv(op, ly, lx, (double)alpha, (const double *)dA, ldd_a, (const double *)dx, 1, (double)beta,
+              (double *)dy, st);
+  else
+    dev_sgemv(op, ly, lx, (float)alpha, (const float *)dA, ldd_a, (const float *)dx, 1, (float)beta, (float *)dy,
+              st);
+  ATLG_CHECK(cudaMemcpyAsync(hy.data(), dy, sizeof(T) * ly, cudaMemcpyDeviceToHost, st));
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  vec_unpack(hy, Y, ly, incY);
+  check_status(rout);
+}
+
+template <typename T>
+void host_trsv(const char *rout, int Order, int Uplo, int TA, int Diag, int N, const T *A, int lda, T *X, int incX) {
+  int info = 2000;
+  if (Order != CblasColMajor && Order != CblasRowMajor)
+    info = cblas_errprn(1, info, "Order must be %d or %d, but is set to %d", CblasRowMajor, CblasColMajor, Order);
+  if (Uplo != CblasUpper && Uplo != CblasLower)
+    info = cblas_errprn(2, info, "UPLO must be %d or %d, but is set to %d", CblasUpper, CblasLower, Uplo);
+  if (TA != CblasNoTrans && TA != CblasTrans && TA != CblasConjTrans)
+    info = cblas_errprn(3, info, "TransA must be %d, %d or %d, but is set to %d", CblasNoTrans, CblasTrans,
+                        CblasConjTrans, TA);
+  if (Diag != CblasUnit && Diag != CblasNonUnit)
+    info = cblas_errprn(4, info, "DIAG must be %d or %d, but is set to %d", CblasUnit, CblasNonUnit, Diag);
+  if (N < 0) info = cblas_errprn(5, info, "N cannot be less than zero; is set to %d.", N);
+  if (lda < N || lda < 1) info = cblas_errprn(7, info, "lda must be >= MAX(N,1): lda=%d N=%d", lda, N);
+  if (!incX) info = cblas_errprn(9, info, "incX cannot be zero; is set to %d.", incX);
+  if (info != 2000) {
+    cblas_xerbla(info, rout, "");
+    return;
+  }
+  if (N == 0) return;
+  int uplo = (Uplo == CblasUpper) ? kUpper : kLower;
+  int ta = (TA == CblasNoTrans) ? kNoTrans : kTrans;
+  if (Order == CblasRowMajor) {
+    uplo = (uplo == kUpper) ? kLower : kUpper;
+    ta = (ta == kNoTrans) ? kTrans : kNoTrans;
+  }
+  cudaStream_t st = ctx().stream;
+  std::vector<T> hx;
+  vec_pack(hx, X, N, incX);
+  int ldd_a;
+  const T *dA = to_dev<T>(kBufA, A, N, N, lda, &ldd_a, st);
+  T *dx = static_cast<T *>(ctx().buffer(kBufB, sizeof(T) * (size_t)N));
+  ATLG_CHECK(cudaMemcpyAsync(dx, hx.data(), sizeof(T) * N, cudaMemcpyHostToDevice, st));
+  if (sizeof(T) == 8) dev_dtrsv(uplo, ta, Diag, N, (const double *)dA, ldd_a, (double *)dx, st);
+  else dev_strsv(uplo, ta, Diag, N, (const float *)dA, ldd_a, (float *)dx, st);
+  ATLG_CHECK(cudaMemcpyAsync(hx.data(), dx, sizeof(T) * N, cudaMemcpyDeviceToHost, st));
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  vec_unpack(hx, X, N, incX);
+  check_status(rout);
+}
+
 // ------------------------------------------------------------- new methods
 int mixed_dev(int N, int NRHS, double *A, int lda, int *ipiv, const double *B, int ldb, double *X, int ldx,
               double *berr, double *ferr, int *iters, int *status, cudaStream_t st) {
@@ -636,6 +778,37 @@ int clapack_dposv(const enum ATLAS_ORDER Order, const enum ATLAS_UPLO Uplo, cons
 int clapack_sposv(const enum ATLAS_ORDER Order, const enum ATLAS_UPLO Uplo, const int N, const int NRHS, float *A,
                   const int lda, float *B, const int ldb) {
   return host_posv<float>("clapack_sposv", Order, Uplo, N, NRHS, A, lda, B, ldb);
+}
+
+void cblas_dtrmm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side, const enum CBLAS_UPLO Uplo,
+                 const enum CBLAS_TRANSPOSE TA, const enum CBLAS_DIAG Diag, const int M, const int N,
+                 const double alpha, const double *A, const int lda, double *B, const int ldb) {
+  host_trmm<double>("cblas_dtrmm", Order, Side, Uplo, TA, Diag, M, N, alpha, A, lda, B, ldb);
+}
+void cblas_strmm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side, const enum CBLAS_UPLO Uplo,
+                 const enum CBLAS_TRANSPOSE TA, const enum CBLAS_DIAG Diag, const int M, const int N,
+                 const float alpha, const float *A, const int lda, float *B, const int ldb) {
+  host_trmm<float>("cblas_strmm", Order, Side, Uplo, TA, Diag, M, N, alpha, A, lda, B, ldb);
+}
+void cblas_dgemv(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TA, const int M, const int N,
+                 const double alpha, const double *A, const int lda, const double *X, const int incX,
+                 const double beta, double *Y, const int incY) {
+  host_gemv<double>("cblas_dgemv", Order, TA, M, N, alpha, A, lda, X, incX, beta, Y, incY);
+}
+void cblas_sgemv(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TA, const int M, const int N,
+                 const float alpha, const float *A, const int lda, const float *X, const int incX,
+                 const float beta, float *Y, const int incY) {
+  host_gemv<float>("cblas_sgemv", Order, TA, M, N, alpha, A, lda, X, incX, beta, Y, incY);
+}
+void cblas_dtrsv(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TA,
+                 const enum CBLAS_DIAG Diag, const int N, const double *A, const int lda, double *X,
+                 const int incX) {
+  host_trsv<double>("cblas_dtrsv", Order, Uplo, TA, Diag, N, A, lda, X, incX);
+}
+void cblas_strsv(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TA,
+                 const enum CBLAS_DIAG Diag, const int N, const float *A, const int lda, float *X,
+                 const int incX) {
+  host_trsv<float>("cblas_strsv", Order, Uplo, TA, Diag, N, A, lda, X, incX);
 }
 
 // Split-precision DGEMM (no reference counterpart; see split.cu): the
@@ -870,6 +1043,25 @@ int atlg_dpotrs_dev(int Order, int Uplo, int N, int NRHS, const double *A, int l
                     void *stream) {
   if (N < 0 || NRHS < 0) return -1;
   dev_dpotrs(Order, Uplo, N, NRHS, A, lda, B, ldb, stream_of(stream));
+  return 0;
+}
+int atlg_dtrmm_dev(int Side, int Uplo, int TA, int Diag, int M, int N, double alpha, const double *A, int lda,
+                   double *B, int ldb, void *stream) {
+  if (M < 0 || N < 0) return -1;
+  dev_dtrmm(Side, Uplo, TA, Diag, M, N, alpha, A, lda, B, ldb, stream_of(stream));
+  return 0;
+}
+int atlg_dgemv_dev(int TA, int M, int N, double alpha, const double *A, int lda, const double *X, int incX,
+                   double beta, double *Y, void *stream) {
+  if (M < 0 || N < 0 || incX == 0) return -1;
+  const int lx = (TA == kNoTrans) ? N : M, ly = (TA == kNoTrans) ? M : N;
+  if (incX < 0) X += (size_t)(lx - 1) * (size_t)(-incX);
+  dev_dgemv(TA, ly, lx, alpha, A, lda, X, incX, beta, Y, stream_of(stream));
+  return 0;
+}
+int atlg_dtrsv_dev(int Uplo, int TA, int Diag, int N, const double *A, int lda, double *X, void *stream) {
+  if (N < 0) return -1;
+  dev_dtrsv(Uplo, TA, Diag, N, A, lda, X, stream_of(stream));
   return 0;
 }
 int atlg_dgetrs_dev(int Order, int Trans, int N, int NRHS, const double *A, int lda, const int *ipiv, double *B,

@@ -114,55 +114,51 @@ void dev_dsyreflect(int n, double *C, int ldc, cudaStream_t st) { syreflect_impl
 void dev_ssyreflect(int n, float *C, int ldc, cudaStream_t st) { syreflect_impl<float>(n, C, ldc, st); }
 
 // Factor the nb x nb diagonal block at A (nb <= 64) in shared memory, as
-// L L^T (Lower) or U^T U (Upper, handled as the transpose).  On a
-// non-positive pivot j it stores that value, writes koff + j + 1 to *info
-// and stops.
+// L L^T (Lower) or U^T U (Upper, handled as the transpose).  One barrier per
+// column: step j reads the pivot, every thread forms 1/sqrt redundantly and
+// applies the rank-1 update with the scaled column computed on the fly;
+// column j itself is scaled in step j+1, when nothing reads it any more.
+// Four threads share a row.  On a non-positive pivot j the block keeps that
+// value, *info gets koff + j + 1 and the factorization stops.
 template <typename T>
 __global__ void __launch_bounds__(256) potf2_kernel(int nb, int uplo, T *A, int lda, int koff, int *info) {
   __shared__ T a[CB][CB + 1];
-  __shared__ T s_r;
-  __shared__ int s_fail;
   const int tid = threadIdx.x;
+  const int row = tid >> 2, q = tid & 3;
   for (int e = tid; e < nb * nb; e += 256) {
     const int i = e % nb, k = e / nb;
     if (i >= k) a[i][k] = (uplo == kLower) ? A[i + (size_t)k * lda] : A[k + (size_t)i * lda];
   }
-  if (tid == 0) s_fail = 0;
   __syncthreads();
-  int done = nb;
+  int fail = 0;
+  T s_prev = T(0), r_prev = T(0);
   for (int j = 0; j < nb; ++j) {
-    if (tid == 0) {
-      const T ajj = a[j][j];
-      if (!(ajj > T(0))) {
-        s_fail = j + 1;
-      } else {
-        const T r = sqrt(ajj);
-        a[j][j] = r;
-        s_r = T(1) / r;
-      }
+    const T ajj = a[j][j];   // same value in every thread: the loop exits uniformly
+    if (j > 0 && q == 0) {   // finish column j-1
+      if (row == j - 1) a[row][row] = s_prev;
+      else if (row > j - 1 && row < nb) a[row][j - 1] *= r_prev;
     }
-    __syncthreads();
-    if (s_fail) { done = j + 1; break; }
-    const T r = s_r;
-    for (int i = j + 1 + tid; i < nb; i += 256) a[i][j] *= r;
-    __syncthreads();
-    // rank-1 update of the trailing triangle: 4 threads per row
-    const int i = j + 1 + (tid >> 2);
-    if (i < nb) {
-      const T lij = a[i][j];
-      for (int k = j + 1 + (tid & 3); k <= i; k += 4) a[i][k] -= lij * a[k][j];
+    if (!(ajj > T(0))) { fail = j + 1; break; }
+    const T sj = sqrt(ajj), r = T(1) / sj;
+    if (row > j && row < nb) {
+      const T lij = a[row][j] * r;
+      for (int k = j + 1 + q; k <= row; k += 4) a[row][k] -= lij * (a[k][j] * r);
     }
+    s_prev = sj;
+    r_prev = r;
     __syncthreads();
   }
-  // write back the processed columns (the failing pivot keeps its value)
+  if (!fail && q == 0 && row == nb - 1) a[row][row] = s_prev;
   __syncthreads();
+  // write back the processed columns (the failing pivot column as it stands)
+  const int done = fail ? fail : nb;
   for (int e = tid; e < nb * nb; e += 256) {
     const int i = e % nb, k = e / nb;
     if (i < k || k >= done) continue;
     if (uplo == kLower) A[i + (size_t)k * lda] = a[i][k];
     else A[k + (size_t)i * lda] = a[i][k];
   }
-  if (tid == 0 && s_fail && *info == 0) *info = koff + s_fail;
+  if (tid == 0 && fail && *info == 0) *info = koff + fail;
 }
 
 template <typename T>

@@ -53,7 +53,7 @@ template <typename T, int BM, int BN, int BK, int TM, int TN, int NT, int STAGES
           bool USE_TMA>
 __global__ void __launch_bounds__(NT)
     gemm_kernel(int M, int N, int K, T alpha, const T *__restrict__ A, int lda,
-                const T *__restrict__ B, int ldb, T beta, T *__restrict__ C, int ldc, int uplo,
+                const T *__restrict__ B, int ldb, T beta, T *__restrict__ C, int ldc, int uplo, int tri,
                 const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB) {
   using KC = GemmKernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, USE_TMA>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -65,7 +65,19 @@ __global__ void __launch_bounds__(NT)
   const int n0 = blockIdx.y * BN;
   // triangle-masked update (SYRK): tiles wholly outside the triangle exit
   if ((uplo == kLower && m0 + BM <= n0) || (uplo == kUpper && n0 + BN <= m0)) return;
-  const int KT = (K + BK - 1) / BK;
+  // triangular operand (TRMM): only the k-tiles that meet the triangle
+  int kt0 = 0, kt1 = (K + BK - 1) / BK;
+  if (tri) {
+    const bool up = (tri & kTriUpper) != 0;
+    if ((tri & kTriWhich) == kTriA) {          // op(A) upper: k >= m;  lower: k <= m
+      if (up) kt0 = m0 / BK;
+      else kt1 = ((K < m0 + BM ? K : m0 + BM) + BK - 1) / BK;
+    } else {                                    // op(B) upper: k <= n;  lower: k >= n
+      if (up) kt1 = ((K < n0 + BN ? K : n0 + BN) + BK - 1) / BK;
+      else kt0 = n0 / BK;
+    }
+  }
+  const int KT = kt1 - kt0;
   const int tx = tid % KC::GX, ty = tid / KC::GX;
 
   T acc[TM][TN];
@@ -110,6 +122,37 @@ __global__ void __launch_bounds__(NT)
     }
   };
 
+  // zero the elements of a triangular operand's stage that lie outside the
+  // triangle (1 on a unit diagonal); only stages that cross the diagonal
+  auto tri_mask_stage = [&](int ktg, int s) {
+    const int k0 = ktg * BK;
+    const bool up = (tri & kTriUpper) != 0, unit = (tri & kTriUnit) != 0;
+    if ((tri & kTriWhich) == kTriA) {
+      if (!(k0 < m0 + BM && m0 < k0 + BK)) return;
+      T *sa = stageA(s);
+#pragma unroll 1
+      for (int e = tid; e < KC::A_ELEMS; e += NT) {
+        int m, k;
+        if (TA == kNoTrans) { m = e % BM; k = e / BM; } else { k = e % BK; m = e / BK; }
+        const int gm = m0 + m, gk = k0 + k;
+        if (up ? gk < gm : gk > gm) sa[e] = T(0);
+        else if (unit && gk == gm) sa[e] = T(1);
+      }
+    } else {
+      if (!(k0 < n0 + BN && n0 < k0 + BK)) return;
+      T *sb = stageB(s);
+#pragma unroll 1
+      for (int e = tid; e < KC::B_ELEMS; e += NT) {
+        int k, n;
+        if (TB == kNoTrans) { k = e % BK; n = e / BK; } else { n = e % BN; k = e / BN; }
+        const int gn = n0 + n, gk = k0 + k;
+        if (up ? gk > gn : gk < gn) sb[e] = T(0);
+        else if (unit && gk == gn) sb[e] = T(1);
+      }
+    }
+    __syncthreads();
+  };
+
   if (USE_TMA) {
     if (tid == 0) {
       prefetch_tmap(&tmA);
@@ -119,11 +162,11 @@ __global__ void __launch_bounds__(NT)
     }
     __syncthreads();
     if (tid == 0)
-      for (int s = 0; s < STAGES && s < KT; ++s) issue_tma(s, s);
+      for (int s = 0; s < STAGES && s < KT; ++s) issue_tma(kt0 + s, s);
   } else {
 #pragma unroll
     for (int s = 0; s < STAGES - 1; ++s) {
-      if (s < KT) issue_cpasync(s, s);
+      if (s < KT) issue_cpasync(kt0 + s, s);
       cp_async_commit();
     }
   }
@@ -137,9 +180,10 @@ __global__ void __launch_bounds__(NT)
       cp_async_wait<STAGES - 2>();
       __syncthreads();
       const int nk = kt + STAGES - 1;
-      if (nk < KT) issue_cpasync(nk, nk % STAGES);
+      if (nk < KT) issue_cpasync(kt0 + nk, nk % STAGES);
       cp_async_commit();
     }
+    if (tri) tri_mask_stage(kt0 + kt, s);
     const T *sa = stageA(s), *sb = stageB(s);
 #pragma unroll
     for (int k = 0; k < BK; ++k) {
@@ -155,7 +199,10 @@ __global__ void __launch_bounds__(NT)
     }
     if (USE_TMA) {
       __syncthreads();                       // every thread is done with stage s
-      if (tid == 0 && kt + STAGES < KT) issue_tma(kt + STAGES, s);
+      if (tid == 0 && kt + STAGES < KT) {
+        if (tri) fence_proxy_async();   // masked in place: order before the next TMA write
+        issue_tma(kt0 + kt + STAGES, s);
+      }
     }
   }
   if (!USE_TMA) cp_async_wait<0>();
@@ -184,7 +231,7 @@ template <> struct DT<float>  { static constexpr CUtensorMapDataType v = CU_TENS
 
 template <typename T, int BM, int BN, int BK, int TM, int TN, int NT, int STAGES, int TA, int TB>
 static void launch_cfg(int M, int N, int K, T alpha, const T *A, int lda, const T *B, int ldb,
-                       T beta, T *C, int ldc, cudaStream_t st, bool allow_tma, int uplo) {
+                       T beta, T *C, int ldc, cudaStream_t st, bool allow_tma, int uplo, int tri) {
   dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN);
   CUtensorMap tmA, tmB;
   bool tma = allow_tma;
@@ -201,7 +248,7 @@ static void launch_cfg(int M, int N, int K, T alpha, const T *A, int lda, const 
     using KC = GemmKernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, true>;
     auto k = gemm_kernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, true>;
     ATLG_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, KC::SMEM_BYTES));
-    k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, uplo, tmA, tmB);
+    k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, uplo, tri, tmA, tmB);
     note_launch();
   } else {
     memset(&tmA, 0, sizeof(tmA));
@@ -209,7 +256,7 @@ static void launch_cfg(int M, int N, int K, T alpha, const T *A, int lda, const 
     using KC = GemmKernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, false>;
     auto k = gemm_kernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, false>;
     ATLG_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, KC::SMEM_BYTES));
-    k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, uplo, tmA, tmB);
+    k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, uplo, tri, tmA, tmB);
     note_launch();
   }
   ATLG_CHECK(cudaGetLastError());
@@ -232,18 +279,18 @@ static int pick_dtile(int M, int N, int nsm) {
 
 template <int TA, int TB>
 static void dgemm_t(int M, int N, int K, double alpha, const double *A, int lda, const double *B, int ldb,
-                    double beta, double *C, int ldc, cudaStream_t st, bool tma, int nsm, int uplo) {
+                    double beta, double *C, int ldc, cudaStream_t st, bool tma, int nsm, int uplo, int tri) {
   switch (pick_dtile(M, N, nsm)) {
-    case 0: launch_cfg<double, 64, 64, 16, 8, 4, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo); break;
-    case 1: launch_cfg<double, 64, 32, 16, 4, 4, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo); break;
-    default: launch_cfg<double, 32, 32, 16, 4, 2, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo); break;
+    case 0: launch_cfg<double, 64, 64, 16, 8, 4, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo, tri); break;
+    case 1: launch_cfg<double, 64, 32, 16, 4, 4, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo, tri); break;
+    default: launch_cfg<double, 32, 32, 16, 4, 2, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo, tri); break;
   }
 }
 
 template <int TA, int TB>
 static void sgemm_t(int M, int N, int K, float alpha, const float *A, int lda, const float *B, int ldb,
-                    float beta, float *C, int ldc, cudaStream_t st, bool tma, int uplo) {
-  launch_cfg<float, 128, 128, 16, 8, 8, 256, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo);
+                    float beta, float *C, int ldc, cudaStream_t st, bool tma, int uplo, int tri) {
+  launch_cfg<float, 128, 128, 16, 8, 8, 256, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo, tri);
 }
 
 __global__ void scale_kernel_d(int M, int N, double beta, double *C, int ldc) {
@@ -350,6 +397,19 @@ static void gemv_launch(int TA, int M, int K, T alpha, const T *A, int lda, cons
   ATLG_CHECK(cudaGetLastError());
 }
 
+void dev_dgemv(int TA, int M, int K, double alpha, const double *A, int lda, const double *x, int incx, double beta,
+               double *y, cudaStream_t st) {
+  if (M <= 0) return;
+  if (alpha == 0.0 || K <= 0) { dev_gescal(M, 1, beta, y, M, st); return; }
+  gemv_launch<double>(TA == kNoTrans ? kNoTrans : kTrans, M, K, alpha, A, lda, x, incx, beta, y, st);
+}
+void dev_sgemv(int TA, int M, int K, float alpha, const float *A, int lda, const float *x, int incx, float beta,
+               float *y, cudaStream_t st) {
+  if (M <= 0) return;
+  if (alpha == 0.0f || K <= 0) { dev_gescal(M, 1, beta, y, M, st); return; }
+  gemv_launch<float>(TA == kNoTrans ? kNoTrans : kTrans, M, K, alpha, A, lda, x, incx, beta, y, st);
+}
+
 // CUDA-event bracket around one GEMM launch when profiling is on.
 struct ProfScope {
   cudaStream_t st;
@@ -377,15 +437,15 @@ void dev_dgemm(int TA, int TB, int M, int N, int K, double alpha, const double *
   if (alpha == 0.0 || K <= 0) { dev_gescal(M, N, beta, C, ldc, st); return; }
   const bool ta = TA != kNoTrans, tb = TB != kNoTrans;
   const int nsm = o.num_sms > 0 ? o.num_sms : ctx().num_sms;
-  if (N == 1 && o.allow_gemv && o.uplo == 0) {   // matrix-vector product: x = op(B)(:,0)
+  if (N == 1 && o.allow_gemv && o.uplo == 0 && o.tri == 0) {   // matrix-vector product: x = op(B)(:,0)
     gemv_launch<double>(TA, M, K, alpha, A, lda, B, tb ? ldb : 1, beta, C, st);
     return;
   }
   ProfScope ps(st, 2.0 * M * N * K);
-  if (!ta && !tb) dgemm_t<kNoTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo);
-  else if (!ta && tb) dgemm_t<kNoTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo);
-  else if (ta && !tb) dgemm_t<kTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo);
-  else dgemm_t<kTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo);
+  if (!ta && !tb) dgemm_t<kNoTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo, o.tri);
+  else if (!ta && tb) dgemm_t<kNoTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo, o.tri);
+  else if (ta && !tb) dgemm_t<kTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo, o.tri);
+  else dgemm_t<kTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo, o.tri);
 }
 
 void dev_sgemm(int TA, int TB, int M, int N, int K, float alpha, const float *A, int lda, const float *B,
@@ -393,15 +453,15 @@ void dev_sgemm(int TA, int TB, int M, int N, int K, float alpha, const float *A,
   if (M <= 0 || N <= 0) return;
   if (alpha == 0.0f || K <= 0) { dev_gescal(M, N, beta, C, ldc, st); return; }
   const bool ta = TA != kNoTrans, tb = TB != kNoTrans;
-  if (N == 1 && o.allow_gemv && o.uplo == 0) {
+  if (N == 1 && o.allow_gemv && o.uplo == 0 && o.tri == 0) {
     gemv_launch<float>(TA, M, K, alpha, A, lda, B, tb ? ldb : 1, beta, C, st);
     return;
   }
   ProfScope ps(st, 2.0 * M * N * K);
-  if (!ta && !tb) sgemm_t<kNoTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo);
-  else if (!ta && tb) sgemm_t<kNoTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo);
-  else if (ta && !tb) sgemm_t<kTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo);
-  else sgemm_t<kTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo);
+  if (!ta && !tb) sgemm_t<kNoTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo, o.tri);
+  else if (!ta && tb) sgemm_t<kNoTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo, o.tri);
+  else if (ta && !tb) sgemm_t<kTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo, o.tri);
+  else sgemm_t<kTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo, o.tri);
 }
 
 unsigned gemm_status_read_and_clear() {

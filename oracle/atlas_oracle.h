@@ -7,7 +7,8 @@
  * calls it.
  *
  * Parity pin: the random generator, laswp, pivot order, Cholesky info and
- * the LU / Cholesky / GEMM / SYRK / TRSM results of this restatement are
+ * the LU / Cholesky / GEMM / SYRK / TRSM / TRMM / GEMV / TRSV results of this
+ * restatement are
  * checked against routines extracted from the reference's own basefiles (oracle/ref_build.sh builds them into
  * oracle/_ref/) and against the fixtures in tests/golden/ that were generated
  * from that build (tests/golden/make_golden.py).
@@ -113,6 +114,32 @@ int  ora_dposv(int Order, int Uplo, int N, int NRHS, double *A, int lda,
                double *B, int ldb);
 int  ora_sposv(int Order, int Uplo, int N, int NRHS, float *A, int lda,
                float *B, int ldb);
+
+/* --- TRMM, GEMV, TRSV --------------------------------------------------- */
+/* reference-BLAS trmm (AtlasBase/Antoine/atlrefblas.base:8406) and the cblas
+ * order mapping shared with TRSM (AtlasBase/Clint/cblas.base:587-692) */
+void ora_dtrmm(int Side, int Uplo, int TA, int Diag, int M, int N, double alpha,
+               const double *A, int lda, double *B, int ldb);
+void ora_strmm(int Side, int Uplo, int TA, int Diag, int M, int N, float alpha,
+               const float *A, int lda, float *B, int ldb);
+void ora_dcblas_trmm(int Order, int Side, int Uplo, int TA, int Diag, int M,
+                     int N, double alpha, const double *A, int lda, double *B,
+                     int ldb);
+void ora_scblas_trmm(int Order, int Side, int Uplo, int TA, int Diag, int M,
+                     int N, float alpha, const float *A, int lda, float *B,
+                     int ldb);
+/* cblas_gemv / cblas_trsv (AtlasBase/Clint/cblas-lvl2.base:21-93, 273-357),
+ * negative increments counted from the far end */
+void ora_dcblas_gemv(int Order, int TA, int M, int N, double alpha,
+                     const double *A, int lda, const double *X, int incX,
+                     double beta, double *Y, int incY);
+void ora_scblas_gemv(int Order, int TA, int M, int N, float alpha,
+                     const float *A, int lda, const float *X, int incX,
+                     float beta, float *Y, int incY);
+void ora_dcblas_trsv(int Order, int Uplo, int TA, int Diag, int N,
+                     const double *A, int lda, double *X, int incX);
+void ora_scblas_trsv(int Order, int Uplo, int TA, int Diag, int N,
+                     const float *A, int lda, float *X, int incX);
 
 /* --- tester residuals ---------------------------------------------------- */
 /* xdlutst residual (AtlasBase/Clint/atlas-tlp.base:1992-2058) for a

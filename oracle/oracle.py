@@ -45,6 +45,8 @@ _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="F_CONTIGUOUS")
 _sp = np.ctypeslib.ndpointer(dtype=np.float32, flags="F_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _i, _d, _f, _l = C.c_int, C.c_double, C.c_float, C.c_long
+_v1d = np.ctypeslib.ndpointer(dtype=np.float64, ndim=1, flags="C_CONTIGUOUS")
+_v1s = np.ctypeslib.ndpointer(dtype=np.float32, ndim=1, flags="C_CONTIGUOUS")
 
 
 def _declare(L):
@@ -91,6 +93,14 @@ def _declare(L):
         "ora_spotrs": (None, [_i, _i, _i, _i, _sp, _i, _sp, _i]),
         "ora_dposv": (_i, [_i, _i, _i, _i, _dp, _i, _dp, _i]),
         "ora_sposv": (_i, [_i, _i, _i, _i, _sp, _i, _sp, _i]),
+        "ora_dtrmm": (None, [_i, _i, _i, _i, _i, _i, _d, _dp, _i, _dp, _i]),
+        "ora_strmm": (None, [_i, _i, _i, _i, _i, _i, _f, _sp, _i, _sp, _i]),
+        "ora_dcblas_trmm": (None, [_i, _i, _i, _i, _i, _i, _i, _d, _dp, _i, _dp, _i]),
+        "ora_scblas_trmm": (None, [_i, _i, _i, _i, _i, _i, _i, _f, _sp, _i, _sp, _i]),
+        "ora_dcblas_gemv": (None, [_i, _i, _i, _i, _d, _dp, _i, _v1d, _i, _d, _v1d, _i]),
+        "ora_scblas_gemv": (None, [_i, _i, _i, _i, _f, _sp, _i, _v1s, _i, _f, _v1s, _i]),
+        "ora_dcblas_trsv": (None, [_i, _i, _i, _i, _i, _dp, _i, _v1d, _i]),
+        "ora_scblas_trsv": (None, [_i, _i, _i, _i, _i, _sp, _i, _v1s, _i]),
         "ora_set_threads": (_i, [_i]),
         "ora_get_threads": (_i, []),
     }
@@ -140,6 +150,25 @@ def syrk(Uplo, Trans, N, K, alpha, A, beta, C, order=ColMajor):
     f = lib().ora_dcblas_syrk if C.dtype == np.float64 else lib().ora_scblas_syrk
     f(order, Uplo, Trans, N, K, alpha, A, A.shape[0], beta, C, C.shape[0])
     return C
+
+
+def trmm(Side, Uplo, TA, Diag, M, N, alpha, A, B, order=ColMajor):
+    f = lib().ora_dcblas_trmm if B.dtype == np.float64 else lib().ora_scblas_trmm
+    f(order, Side, Uplo, TA, Diag, M, N, alpha, A, A.shape[0], B, B.shape[0])
+    return B
+
+
+def gemv(TA, M, N, alpha, A, x, incx, beta, y, incy, order=ColMajor):
+    """y <- alpha*op(A)*x + beta*y on 1-D strided storage (cblas_gemv)."""
+    f = lib().ora_dcblas_gemv if A.dtype == np.float64 else lib().ora_scblas_gemv
+    f(order, TA, M, N, alpha, A, A.shape[0], x, incx, beta, y, incy)
+    return y
+
+
+def trsv(Uplo, TA, Diag, N, A, x, incx, order=ColMajor):
+    f = lib().ora_dcblas_trsv if A.dtype == np.float64 else lib().ora_scblas_trsv
+    f(order, Uplo, TA, Diag, N, A, A.shape[0], x, incx)
+    return x
 
 
 def potrf(A, uplo=Lower, N=None, order=ColMajor):

@@ -6,7 +6,8 @@
 #  2. extracts, one routine per file, ATL_getrfC/getrfR/getf2/laswp/getrs and
 #     ATL_potrfU/potrfL/potrf/potrs (AtlasBase/Clint/atlas-lp.base),
 #     ATL_rand/gegen/epsilon (AtlasBase/Clint/atlas-tst.base) and the C
-#     reference BLAS they run on (gemm, trsm, syrk, ger, scal, swap, iamax from
+#     reference BLAS they run on (gemm, trsm, trmm, syrk, gemv, trsv, ger, scal,
+#     swap, iamax from
 #     AtlasBase/Antoine/atlrefblas.base);
 #  3. compiles them, double and single precision, with the stand-in headers in
 #     oracle/ref_shim/ into oracle/_ref/libatlref.so.
@@ -28,8 +29,10 @@ $X -b $R/Clint/atlas.base -o cblas.h rout=cblas.h
 for h in misc lvl3 level3 level1 level2 lvl2; do
    $X -b $R/Antoine/atlrefblas.base -o atlas_ref$h.h rout=atlas_ref$h.h type=none
 done
-RB="gemm gemmNN gemmNT gemmTN gemmTT trsm ger scal swap syrk syrkLN syrkLT syrkUN syrkUT"
-for s in L R; do for u in L U; do for t in N T; do for d in N U; do RB="$RB trsm$s$u$t$d"; done; done; done; done
+RB="gemm gemmNN gemmNT gemmTN gemmTT trsm trmm ger scal swap syrk syrkLN syrkLT syrkUN syrkUT"
+RB="$RB gemv gemvN gemvT trsv"
+for s in L R; do for u in L U; do for t in N T; do for d in N U; do RB="$RB trsm$s$u$t$d trmm$s$u$t$d"; done; done; done; done
+for u in L U; do for t in N T; do for d in N U; do RB="$RB trsv$u$t$d"; done; done; done
 for r in $RB; do
    $X -b $R/Antoine/atlrefblas.base -o ATL_dref$r.c rout=$r type=dble
    $X -b $R/Antoine/atlrefblas.base -o ATL_sref$r.c rout=$r type=real

@@ -28,6 +28,12 @@ void ATL_##P##getrs(const enum CBLAS_ORDER, const enum CBLAS_TRANSPOSE, const in
 void ATL_##P##gegen(const int, const int, T*, const int, const int); \
 void ATL_##P##refsyrk(const enum ATLAS_UPLO, const enum ATLAS_TRANS, const int, const int, const T, \
    const T*, const int, const T, T*, const int); \
+void ATL_##P##reftrmm(const enum ATLAS_SIDE, const enum ATLAS_UPLO, const enum ATLAS_TRANS, \
+   const enum ATLAS_DIAG, const int, const int, const T, const T*, const int, T*, const int); \
+void ATL_##P##refgemv(const enum ATLAS_TRANS, const int, const int, const T, const T*, const int, \
+   const T*, const int, const T, T*, const int); \
+void ATL_##P##reftrsv(const enum ATLAS_UPLO, const enum ATLAS_TRANS, const enum ATLAS_DIAG, const int, \
+   const T*, const int, T*, const int); \
 int  ATL_##P##potrf(const enum ATLAS_ORDER, const enum ATLAS_UPLO, const int, T*, const int); \
 void ATL_##P##potrs(const enum CBLAS_ORDER, const enum CBLAS_UPLO, const int, const int, const T*, \
    const int, T*, const int); \
@@ -108,6 +114,40 @@ void atlref_##P##syrk(int order, int u, int t, int N, int K, T al, const T *A, i
                     be, C, ldc); } \
 int  atlref_##P##potrf(int order, int u, int N, T *A, int lda) \
 { return ATL_##P##potrf((enum ATLAS_ORDER)order, (enum ATLAS_UPLO)u, N, A, lda); } \
+/* cblas order mappings of trmm (as trsm), gemv and trsv: AtlasBase/Clint/cblas.base \
+ * TRSM/TRMM section and AtlasBase/Clint/cblas-lvl2.base; negative increments start \
+ * at the far end as the cblas wrappers arrange */ \
+void atlref_##P##trmm(int order, int s, int u, int t, int d, int M, int N, T al, const T *A, int lda, \
+   T *B, int ldb) \
+{ \
+   if (order == CblasColMajor) \
+      ATL_##P##reftrmm((enum ATLAS_SIDE)s, (enum ATLAS_UPLO)u, (enum ATLAS_TRANS)t, (enum ATLAS_DIAG)d, \
+                       M, N, al, A, lda, B, ldb); \
+   else \
+      ATL_##P##reftrmm(s == CblasLeft ? AtlasRight : AtlasLeft, u == CblasUpper ? AtlasLower : AtlasUpper, \
+                       (enum ATLAS_TRANS)t, (enum ATLAS_DIAG)d, N, M, al, A, lda, B, ldb); \
+} \
+void atlref_##P##gemv(int order, int ta, int M, int N, T al, const T *A, int lda, const T *X, int incx, \
+   T be, T *Y, int incy) \
+{ \
+   const int lx = (ta == CblasNoTrans) ? N : M, ly = (ta == CblasNoTrans) ? M : N; \
+   if (incx < 0) X += (1 - lx) * incx; \
+   if (incy < 0) Y += (1 - ly) * incy; \
+   /* ATL_refgemv takes the dimensions of op(A): y has ly entries, x has lx */ \
+   if (order == CblasColMajor) \
+      ATL_##P##refgemv((enum ATLAS_TRANS)ta, ly, lx, al, A, lda, X, incx, be, Y, incy); \
+   else \
+      ATL_##P##refgemv(ta == CblasNoTrans ? AtlasTrans : AtlasNoTrans, ly, lx, al, A, lda, X, incx, be, Y, incy); \
+} \
+void atlref_##P##trsv(int order, int u, int t, int d, int N, const T *A, int lda, T *X, int incx) \
+{ \
+   if (incx < 0) X += (1 - N) * incx; \
+   if (order == CblasColMajor) \
+      ATL_##P##reftrsv((enum ATLAS_UPLO)u, (enum ATLAS_TRANS)t, (enum ATLAS_DIAG)d, N, A, lda, X, incx); \
+   else \
+      ATL_##P##reftrsv(u == CblasUpper ? AtlasLower : AtlasUpper, t == CblasNoTrans ? AtlasTrans : AtlasNoTrans, \
+                       (enum ATLAS_DIAG)d, N, A, lda, X, incx); \
+} \
 void atlref_##P##potrs(int order, int u, int N, int NRHS, const T *A, int lda, T *B, int ldb) \
 { ATL_##P##potrs((enum CBLAS_ORDER)order, (enum CBLAS_UPLO)u, N, NRHS, A, lda, B, ldb); }
 

@@ -23,6 +23,7 @@ OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "atlas_ref_fixtur
 dp = np.ctypeslib.ndpointer(np.float64, flags="F_CONTIGUOUS")
 sp = np.ctypeslib.ndpointer(np.float32, flags="F_CONTIGUOUS")
 ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+v1 = np.ctypeslib.ndpointer(np.float64, ndim=1, flags="C_CONTIGUOUS")
 I, D, F = C.c_int, C.c_double, C.c_float
 
 
@@ -46,6 +47,9 @@ def load():
     R.atlref_spotrf.argtypes = [I, I, I, sp, I]
     R.atlref_spotrf.restype = I
     R.atlref_dpotrs.argtypes = [I, I, I, I, dp, I, dp, I]
+    R.atlref_dtrmm.argtypes = [I, I, I, I, I, I, I, D, dp, I, dp, I]
+    R.atlref_dgemv.argtypes = [I, I, I, I, D, dp, I, v1, I, D, v1, I]
+    R.atlref_dtrsv.argtypes = [I, I, I, I, I, dp, I, v1, I]
     return R
 
 
@@ -203,6 +207,43 @@ def main():
         for uplo in (121, 122):
             F = A.copy(order="F")
             out[f"cholbad_{n}_{bad}_{uplo}_info"] = np.array(R.atlref_dpotrf(102, uplo, n, F, lda))
+    # reference trmm, all 16 cases and both orders (M x N = 37 x 29)
+    for order in (101, 102):
+        for side in (141, 142):
+            for uplo in (121, 122):
+                for ta in (111, 112):
+                    for diag in (131, 132):
+                        M, N = 37, 29
+                        na = M if side == 141 else N
+                        rows, cols = (M, N) if order == 102 else (N, M)
+                        A = gegen(R, na, na, na, na * na + 11)
+                        A += np.eye(na) * na
+                        B = gegen(R, rows, cols, rows, M * N + 3)
+                        R.atlref_dtrmm(order, side, uplo, ta, diag, M, N, 1.5, A, na, B, rows)
+                        out[f"trmm_{order}_{side}_{uplo}_{ta}_{diag}"] = B
+    # reference gemv (M x N = 33 x 21) with positive and negative increments
+    for order in (101, 102):
+        for ta in (111, 112):
+            for incx, incy in ((1, 1), (-2, 3), (2, -3)):
+                M, N = 33, 21
+                A = gegen(R, M, N, M, 7) if order == 102 else gegen(R, N, M, N, 7)
+                lx, ly = (N, M) if ta == 111 else (M, N)
+                x = gegen(R, lx * abs(incx), 1, lx * abs(incx), 8)[:, 0].copy()
+                y = gegen(R, ly * abs(incy), 1, ly * abs(incy), 9)[:, 0].copy()
+                R.atlref_dgemv(order, ta, M, N, 0.7, A, A.shape[0], x, incx, 0.3, y, incy)
+                out[f"gemv_{order}_{ta}_{incx}_{incy}"] = y
+    # reference trsv (N = 40) with unit and negative increments
+    for order in (101, 102):
+        for uplo in (121, 122):
+            for ta in (111, 112):
+                for diag in (131, 132):
+                    for incx in (1, -2):
+                        n = 40
+                        A = gegen(R, n, n, n, 5)
+                        A += np.eye(n) * n
+                        x = gegen(R, n * abs(incx), 1, n * abs(incx), 6)[:, 0].copy()
+                        R.atlref_dtrsv(order, uplo, ta, diag, n, A, n, x, incx)
+                        out[f"trsv_{order}_{uplo}_{ta}_{diag}_{incx}"] = x
     np.savez_compressed(OUT, **out)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")
 

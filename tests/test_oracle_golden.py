@@ -170,3 +170,54 @@ def test_spotrf_info(ora, golden):
         n, lda = int(n), int(lda)
         F = golden[f"chol_{n}_{lda}_a"].astype(np.float32, order="F")
         assert ora.potrf(F, uplo=ora.Lower, N=n) == int(golden[f"chol_{n}_{lda}_s_info"])
+
+
+def test_trmm_matches_reference_blas(ora, golden):
+    for order in (101, 102):
+        for side in (ora.Left, ora.Right):
+            for uplo in (ora.Upper, ora.Lower):
+                for ta in (ora.NoTrans, ora.Trans):
+                    for diag in (ora.NonUnit, ora.Unit):
+                        M, N = 37, 29
+                        na = M if side == ora.Left else N
+                        rows, cols = (M, N) if order == 102 else (N, M)
+                        A = ora.gegen(na, na, na * na + 11)
+                        A += np.eye(na) * na
+                        B = ora.gegen(rows, cols, M * N + 3)
+                        ora.trmm(side, uplo, ta, diag, M, N, 1.5, A, B, order=order)
+                        ref = golden[f"trmm_{order}_{side}_{uplo}_{ta}_{diag}"]
+                        assert np.abs(B - ref).max() <= 1e-12 * na, (order, side, uplo, ta, diag)
+
+
+def test_gemv_matches_reference_blas(ora, golden):
+    for order in (101, 102):
+        for ta in (ora.NoTrans, ora.Trans):
+            for incx, incy in ((1, 1), (-2, 3), (2, -3)):
+                M, N = 33, 21
+                A = ora.gegen(M, N, 7) if order == 102 else ora.gegen(N, M, 7)
+                lx, ly = (N, M) if ta == ora.NoTrans else (M, N)
+                x = ora.gegen(lx * abs(incx), 1, 8)[:, 0].copy()
+                y = ora.gegen(ly * abs(incy), 1, 9)[:, 0].copy()
+                y0 = y.copy()
+                ora.gemv(ta, M, N, 0.7, A, x, incx, 0.3, y, incy, order=order)
+                assert np.abs(y - golden[f"gemv_{order}_{ta}_{incx}_{incy}"]).max() <= 1e-14 * lx
+                # elements between the strided ones are not touched
+                if abs(incy) > 1:
+                    mask = np.ones(len(y), bool)
+                    mask[::abs(incy)] = False
+                    assert np.array_equal(y[mask], y0[mask])
+
+
+def test_trsv_matches_reference_blas(ora, golden):
+    for order in (101, 102):
+        for uplo in (ora.Upper, ora.Lower):
+            for ta in (ora.NoTrans, ora.Trans):
+                for diag in (ora.NonUnit, ora.Unit):
+                    for incx in (1, -2):
+                        n = 40
+                        A = ora.gegen(n, n, 5)
+                        A += np.eye(n) * n
+                        x = ora.gegen(n * abs(incx), 1, 6)[:, 0].copy()
+                        ora.trsv(uplo, ta, diag, n, A, x, incx, order=order)
+                        ref = golden[f"trsv_{order}_{uplo}_{ta}_{diag}_{incx}"]
+                        assert np.allclose(x, ref, rtol=1e-12, atol=1e-14), (order, uplo, ta, diag, incx)
