@@ -36,12 +36,15 @@ enum CBLAS_UPLO {CblasUpper=121, CblasLower=122};
 enum CBLAS_DIAG {CblasNonUnit=131, CblasUnit=132};
 enum CBLAS_SIDE {CblasLeft=141, CblasRight=142};
 #endif
-/* AtlasBase/Clint/atlas-clp.base:624-627 (clapack.h aliases) */
+/* AtlasBase/Clint/atlas-clp.base:624-630 (clapack.h aliases) */
 #ifndef ATLAS_ORDER
 #define ATLAS_ORDER CBLAS_ORDER
 #endif
 #ifndef ATLAS_UPLO
 #define ATLAS_UPLO CBLAS_UPLO
+#endif
+#ifndef ATLAS_DIAG
+#define ATLAS_DIAG CBLAS_DIAG
 #endif
 
 /* ---- error reporting: AtlasBase/Clint/cblas.base:14 (cblas_errprn), :42 (cblas_xerbla) */
@@ -139,6 +142,17 @@ int clapack_dposv(const enum ATLAS_ORDER Order, const enum ATLAS_UPLO Uplo, cons
 int clapack_sposv(const enum ATLAS_ORDER Order, const enum ATLAS_UPLO Uplo, const int N,
                   const int NRHS, float *A, const int lda, float *B, const int ldb);
 
+/* ---- LAPACK: AtlasBase/Clint/atlas-clp.base:411-452 (clapack_trtri, d and s) */
+int clapack_dtrtri(const enum ATLAS_ORDER Order, const enum ATLAS_UPLO Uplo,
+                   const enum ATLAS_DIAG Diag, const int N, double *A, const int lda);
+int clapack_strtri(const enum ATLAS_ORDER Order, const enum ATLAS_UPLO Uplo,
+                   const enum ATLAS_DIAG Diag, const int N, float *A, const int lda);
+/* ---- LAPACK: AtlasBase/Clint/atlas-clp.base:115-139 (clapack_getri, d and s) */
+int clapack_dgetri(const enum CBLAS_ORDER Order, const int N, double *A, const int lda,
+                   const int *ipiv);
+int clapack_sgetri(const enum CBLAS_ORDER Order, const int N, float *A, const int lda,
+                   const int *ipiv);
+
 /* ---- new methods (no reference counterpart: ATLAS has neither a
  *      mixed-precision solver nor an adjoint).  Column-major. */
 /* Split-precision DGEMM: cblas_dgemm's interface and checks, computed from
@@ -229,6 +243,10 @@ int atlg_dgemv_dev(int TA, int M, int N, double alpha, const double *A, int lda,
                    const double *X, int incX, double beta, double *Y, void *stream);
 int atlg_dtrsv_dev(int Uplo, int TA, int Diag, int N, const double *A, int lda, double *X,
                    void *stream);
+/* trtri returns its info (synchronizes once); getri reads the 0-based
+ * device pivots back to the host first */
+int atlg_dtrtri_dev(int Order, int Uplo, int Diag, int N, double *A, int lda, void *stream);
+int atlg_dgetri_dev(int N, double *A, int lda, const int *ipiv, void *stream);
 /* berr, ferr (NRHS entries), iters and status are host pointers; synchronizes */
 int atlg_dgesv_mixed_dev(int N, int NRHS, double *A, int lda, int *ipiv, const double *B,
                          int ldb, double *X, int ldx, double *berr, double *ferr, int *iters,

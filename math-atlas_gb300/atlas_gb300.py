@@ -33,6 +33,7 @@ EXPORTS = [
     "clapack_dposv", "clapack_sposv", "atlg_dsyrk_dev", "atlg_dpotrf_dev", "atlg_dpotrs_dev",
     "cblas_dtrmm", "cblas_strmm", "cblas_dgemv", "cblas_sgemv", "cblas_dtrsv", "cblas_strsv",
     "atlg_dtrmm_dev", "atlg_dgemv_dev", "atlg_dtrsv_dev",
+    "clapack_dtrtri", "clapack_strtri", "clapack_dgetri", "clapack_sgetri", "atlg_dtrtri_dev", "atlg_dgetri_dev",
 ]
 
 _lib = None
@@ -92,6 +93,12 @@ def _declare(L):
         "atlg_dtrmm_dev": (_i, [_i, _i, _i, _i, _i, _i, _d, _v, _i, _v, _i, _v]),
         "atlg_dgemv_dev": (_i, [_i, _i, _i, _d, _v, _i, _v, _i, _d, _v, _v]),
         "atlg_dtrsv_dev": (_i, [_i, _i, _i, _i, _v, _i, _v, _v]),
+        "clapack_dtrtri": (_i, [_i, _i, _i, _i, _dp, _i]),
+        "clapack_strtri": (_i, [_i, _i, _i, _i, _sp, _i]),
+        "clapack_dgetri": (_i, [_i, _i, _dp, _i, _ip]),
+        "clapack_sgetri": (_i, [_i, _i, _sp, _i, _ip]),
+        "atlg_dtrtri_dev": (_i, [_i, _i, _i, _i, _v, _i, _v]),
+        "atlg_dgetri_dev": (_i, [_i, _v, _i, _v, _v]),
         "atlg_num_sms": (_i, []),
         "atlg_stream": (_v, []),
         "atlg_status": (_u, []),
@@ -221,6 +228,22 @@ def clapack_dposv(order, uplo, N, NRHS, A, lda, B, ldb):
 
 def clapack_sposv(order, uplo, N, NRHS, A, lda, B, ldb):
     return lib().clapack_sposv(order, uplo, N, NRHS, A, lda, B, ldb)
+
+
+def clapack_dtrtri(order, uplo, diag, N, A, lda):
+    return lib().clapack_dtrtri(order, uplo, diag, N, A, lda)
+
+
+def clapack_strtri(order, uplo, diag, N, A, lda):
+    return lib().clapack_strtri(order, uplo, diag, N, A, lda)
+
+
+def clapack_dgetri(order, N, A, lda, ipiv):
+    return lib().clapack_dgetri(order, N, A, lda, ipiv)
+
+
+def clapack_sgetri(order, N, A, lda, ipiv):
+    return lib().clapack_sgetri(order, N, A, lda, ipiv)
 
 
 def dgemm_split(ta, tb, alpha, A, B, beta, Cm, nslices=7):

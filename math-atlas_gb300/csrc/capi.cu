@@ -13,7 +13,8 @@
 // TRSM/TRMM checks :611-677, SYRK :356-449), AtlasBase/Clint/cblas-lvl2.base
 // (GEMV :21-93, TRSV :273-357) and AtlasBase/Clint/atlas-clp.base
 // (clapack_gesv :62, clapack_getrf :140, clapack_getrs :218, clapack_posv
-// :266, clapack_potrf :320, clapack_potrs :363).
+// :266, clapack_potrf :320, clapack_potrs :363, clapack_getri :115,
+// clapack_trtri :411).
 #include <stdarg.h>
 #include <stdlib.h>
 #include <string.h>
@@ -25,6 +26,7 @@
 #include "context.cuh"
 #include "chol.cuh"
 #include "gemm.cuh"
+#include "getri.cuh"
 #include "lu.cuh"
 #include "mixed.cuh"
 #include "split.cuh"
@@ -671,6 +673,52 @@ void host_trsv(const char *rout, int Order, int Uplo, int TA, int Diag, int N, c
   check_status(rout);
 }
 
+// ------------------------------------------------------------ inverses
+// clapack_?trtri (AtlasBase/Clint/atlas-clp.base:411-452).  The reference
+// tests `if (ierr)` on an uninitialised ierr before calling ATL_trtri; the
+// inverse is computed here whenever the arguments are valid.
+template <typename T>
+int host_trtri(const char *rout, int Order, int Uplo, int Diag, int N, T *A, int lda) {
+  if (Order != CblasRowMajor && Order != CblasColMajor)
+    cblas_xerbla(1, rout, "Order must be %d or %d, but is set to %d\n", CblasRowMajor, CblasColMajor, Order);
+  if (Uplo != CblasUpper && Uplo != CblasLower)
+    cblas_xerbla(2, rout, "Uplo must be %d or %d, but is set to %d\n", CblasUpper, CblasLower, Uplo);
+  if (Diag != CblasUnit && Diag != CblasNonUnit)
+    cblas_xerbla(3, rout, "Diag must be %d or %d, but is set to %d\n", CblasNonUnit, CblasUnit, Diag);
+  if (N < 0) cblas_xerbla(4, rout, "N cannot be less than zero 0,; is set to %d.\n", N);
+  if (lda < N || lda < 1) cblas_xerbla(6, rout, "lda must be >= MAX(N,1): lda=%d N=%d\n", lda, N);
+  if (N == 0) return 0;
+  cudaStream_t st = ctx().stream;
+  int ldd;
+  T *dA = to_dev<T>(kBufA, A, N, N, lda, &ldd, st);
+  const int info = (sizeof(T) == 8) ? dev_dtrtri(Order, Uplo, Diag, N, (double *)dA, ldd, st)
+                                    : dev_strtri(Order, Uplo, Diag, N, (float *)dA, ldd, st);
+  if (info == 0) to_host<T>(A, lda, dA, ldd, N, N, st);
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  check_status(rout);
+  return info;
+}
+
+// clapack_?getri (AtlasBase/Clint/atlas-clp.base:115-139): the reference
+// checks no argument; N < 0 and lda < max(N,1) are reported here through
+// xerbla as parameters 2 and 4 instead of reading out of bounds.
+template <typename T>
+int host_getri(const char *rout, int Order, int N, T *A, int lda, const int *ipiv) {
+  if (N < 0) cblas_xerbla(2, rout, "N cannot be less than zero 0,; is set to %d.\n", N);
+  if (lda < N || lda < 1) cblas_xerbla(4, rout, "lda must be >= MAX(N,1): lda=%d N=%d\n", lda, N);
+  (void)Order;   // same computation on the same memory for both orders
+  if (N == 0) return 0;
+  cudaStream_t st = ctx().stream;
+  int ldd;
+  T *dA = to_dev<T>(kBufA, A, N, N, lda, &ldd, st);
+  const int info = (sizeof(T) == 8) ? dev_dgetri(N, (double *)dA, ldd, ipiv, st)
+                                    : dev_sgetri(N, (float *)dA, ldd, ipiv, st);
+  if (info == 0) to_host<T>(A, lda, dA, ldd, N, N, st);
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  check_status(rout);
+  return info;
+}
+
 // ------------------------------------------------------------- new methods
 int mixed_dev(int N, int NRHS, double *A, int lda, int *ipiv, const double *B, int ldb, double *X, int ldx,
               double *berr, double *ferr, int *iters, int *status, cudaStream_t st) {
@@ -809,6 +857,21 @@ void cblas_strsv(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const
                  const enum CBLAS_DIAG Diag, const int N, const float *A, const int lda, float *X,
                  const int incX) {
   host_trsv<float>("cblas_strsv", Order, Uplo, TA, Diag, N, A, lda, X, incX);
+}
+
+int clapack_dtrtri(const enum ATLAS_ORDER Order, const enum ATLAS_UPLO Uplo, const enum ATLAS_DIAG Diag,
+                   const int N, double *A, const int lda) {
+  return host_trtri<double>("clapack_dtrtri", Order, Uplo, Diag, N, A, lda);
+}
+int clapack_strtri(const enum ATLAS_ORDER Order, const enum ATLAS_UPLO Uplo, const enum ATLAS_DIAG Diag,
+                   const int N, float *A, const int lda) {
+  return host_trtri<float>("clapack_strtri", Order, Uplo, Diag, N, A, lda);
+}
+int clapack_dgetri(const enum CBLAS_ORDER Order, const int N, double *A, const int lda, const int *ipiv) {
+  return host_getri<double>("clapack_dgetri", Order, N, A, lda, ipiv);
+}
+int clapack_sgetri(const enum CBLAS_ORDER Order, const int N, float *A, const int lda, const int *ipiv) {
+  return host_getri<float>("clapack_sgetri", Order, N, A, lda, ipiv);
 }
 
 // Split-precision DGEMM (no reference counterpart; see split.cu): the
@@ -1063,6 +1126,19 @@ int atlg_dtrsv_dev(int Uplo, int TA, int Diag, int N, const double *A, int lda, 
   if (N < 0) return -1;
   dev_dtrsv(Uplo, TA, Diag, N, A, lda, X, stream_of(stream));
   return 0;
+}
+int atlg_dtrtri_dev(int Order, int Uplo, int Diag, int N, double *A, int lda, void *stream) {
+  if (N < 0 || lda < (N > 1 ? N : 1)) return -1;
+  return dev_dtrtri(Order, Uplo, Diag, N, A, lda, stream_of(stream));
+}
+int atlg_dgetri_dev(int N, double *A, int lda, const int *ipiv, void *stream) {
+  if (N < 0 || lda < (N > 1 ? N : 1)) return -1;
+  if (N == 0) return 0;
+  cudaStream_t st = stream_of(stream);
+  std::vector<int> hp(N);
+  ATLG_CHECK(cudaMemcpyAsync(hp.data(), ipiv, sizeof(int) * N, cudaMemcpyDeviceToHost, st));
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  return dev_dgetri(N, A, lda, hp.data(), st);
 }
 int atlg_dgetrs_dev(int Order, int Trans, int N, int NRHS, const double *A, int lda, const int *ipiv, double *B,
                     int ldb, void *stream) {

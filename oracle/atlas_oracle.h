@@ -141,6 +141,16 @@ void ora_dcblas_trsv(int Order, int Uplo, int TA, int Diag, int N,
 void ora_scblas_trsv(int Order, int Uplo, int TA, int Diag, int N,
                      const float *A, int lda, float *X, int incX);
 
+/* --- inverses -------------------------------------------------------------- */
+/* ATL_trtri (AtlasBase/Clint/atlas-lp.base:1718-2380): 0, or the 1-based index
+ * of the first exact zero on a non-unit diagonal (A untouched then). */
+int  ora_dtrtri(int Order, int Uplo, int Diag, int N, double *A, int lda);
+int  ora_strtri(int Order, int Uplo, int Diag, int N, float *A, int lda);
+/* clapack_getri / ATL_getriC (AtlasBase/Clint/atlas-clp.base:115-139,
+ * atlas-lp.base:104-199) on the factors and 0-based pivots of getrf */
+int  ora_dgetri(int Order, int N, double *A, int lda, const int *ipiv);
+int  ora_sgetri(int Order, int N, float *A, int lda, const int *ipiv);
+
 /* --- tester residuals ---------------------------------------------------- */
 /* xdlutst residual (AtlasBase/Clint/atlas-tlp.base:1992-2058) for a
  * column-major factorization held in LU/ipiv of the matrix gegen(M,N,lda,seed). */

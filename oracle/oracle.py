@@ -101,6 +101,10 @@ def _declare(L):
         "ora_scblas_gemv": (None, [_i, _i, _i, _i, _f, _sp, _i, _v1s, _i, _f, _v1s, _i]),
         "ora_dcblas_trsv": (None, [_i, _i, _i, _i, _i, _dp, _i, _v1d, _i]),
         "ora_scblas_trsv": (None, [_i, _i, _i, _i, _i, _sp, _i, _v1s, _i]),
+        "ora_dtrtri": (_i, [_i, _i, _i, _i, _dp, _i]),
+        "ora_strtri": (_i, [_i, _i, _i, _i, _sp, _i]),
+        "ora_dgetri": (_i, [_i, _i, _dp, _i, _ip]),
+        "ora_sgetri": (_i, [_i, _i, _sp, _i, _ip]),
         "ora_set_threads": (_i, [_i]),
         "ora_get_threads": (_i, []),
     }
@@ -169,6 +173,18 @@ def trsv(Uplo, TA, Diag, N, A, x, incx, order=ColMajor):
     f = lib().ora_dcblas_trsv if A.dtype == np.float64 else lib().ora_scblas_trsv
     f(order, Uplo, TA, Diag, N, A, A.shape[0], x, incx)
     return x
+
+
+def trtri(A, uplo, diag=NonUnit, N=None, order=ColMajor):
+    N = A.shape[1] if N is None else N
+    f = lib().ora_dtrtri if A.dtype == np.float64 else lib().ora_strtri
+    return f(order, uplo, diag, N, A, A.shape[0])
+
+
+def getri(A, ipiv, N=None, order=ColMajor):
+    N = A.shape[1] if N is None else N
+    f = lib().ora_dgetri if A.dtype == np.float64 else lib().ora_sgetri
+    return f(order, N, A, A.shape[0], np.ascontiguousarray(ipiv, dtype=np.int32))
 
 
 def potrf(A, uplo=Lower, N=None, order=ColMajor):

@@ -4,7 +4,8 @@
 #
 #  1. compiles the reference's basefile extractor (extract.c) with gcc;
 #  2. extracts, one routine per file, ATL_getrfC/getrfR/getf2/laswp/getrs and
-#     ATL_potrfU/potrfL/potrf/potrs (AtlasBase/Clint/atlas-lp.base),
+#     ATL_potrfU/potrfL/potrf/potrs, ATL_trtri* and ATL_getri*
+#     (AtlasBase/Clint/atlas-lp.base),
 #     ATL_rand/gegen/epsilon (AtlasBase/Clint/atlas-tst.base) and the C
 #     reference BLAS they run on (gemm, trsm, trmm, syrk, gemv, trsv, ger, scal,
 #     swap, iamax from
@@ -39,7 +40,8 @@ for r in $RB; do
 done
 $X -b $R/Antoine/atlrefblas.base -o ATL_idrefamax.c rout=amax type=dble
 $X -b $R/Antoine/atlrefblas.base -o ATL_isrefamax.c rout=amax type=real
-for r in ATL_getrfC ATL_getrfR ATL_getf2 ATL_laswp ATL_getrs ATL_potrfU ATL_potrfL ATL_potrf ATL_potrs; do
+for r in ATL_getrfC ATL_getrfR ATL_getf2 ATL_laswp ATL_getrs ATL_potrfU ATL_potrfL ATL_potrf ATL_potrs \
+         ATL_trtri ATL_trtriCU ATL_trtriCL ATL_trtriRU ATL_trtriRL ATL_getri ATL_getriC ATL_getriR; do
    $X -b $R/Clint/atlas-lp.base -o $r.c rout=$r 2>/dev/null
 done
 for r in ATL_rand ATL_gegen ATL_epsilon; do
@@ -50,6 +52,7 @@ OBJ=""
 for f in ATL_dref*.c ATL_idrefamax.c; do $CC $CF -DDREAL -c $f -o ${f%.c}.o; OBJ="$OBJ ${f%.c}.o"; done
 for f in ATL_sref*.c ATL_isrefamax.c; do $CC $CF -DSREAL -c $f -o ${f%.c}.o; OBJ="$OBJ ${f%.c}.o"; done
 for f in ATL_getrfC ATL_getrfR ATL_getf2 ATL_laswp ATL_getrs ATL_potrfU ATL_potrfL ATL_potrf ATL_potrs \
+         ATL_trtri ATL_trtriCU ATL_trtriCL ATL_trtriRU ATL_trtriRL ATL_getri ATL_getriC ATL_getriR \
          ATL_gegen ATL_epsilon; do
    $CC $CF -DDREAL -c $f.c -o d_$f.o
    $CC $CF -DSREAL -c $f.c -o s_$f.o

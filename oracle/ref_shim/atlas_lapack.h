@@ -32,6 +32,35 @@ void ATL_dpotrs(const enum CBLAS_ORDER, const enum CBLAS_UPLO, const int, const 
                 const int, double*, const int);
 void ATL_spotrs(const enum CBLAS_ORDER, const enum CBLAS_UPLO, const int, const int, const float*,
                 const int, float*, const int);
+#define ATL_trtri  Mjoin(PATL,trtri)
+#define ATL_trtriCU Mjoin(PATL,trtriCU)
+#define ATL_trtriCL Mjoin(PATL,trtriCL)
+#define ATL_trtriRU Mjoin(PATL,trtriRU)
+#define ATL_trtriRL Mjoin(PATL,trtriRL)
+#define ATL_getri  Mjoin(PATL,getri)
+#define ATL_getriC Mjoin(PATL,getriC)
+#define ATL_getriR Mjoin(PATL,getriR)
+int ATL_dtrtri(const enum ATLAS_ORDER, const enum ATLAS_UPLO, const enum ATLAS_DIAG, const int,
+               double*, const int);
+int ATL_strtri(const enum ATLAS_ORDER, const enum ATLAS_UPLO, const enum ATLAS_DIAG, const int,
+               float*, const int);
+int ATL_dtrtriCU(const enum ATLAS_DIAG, const int, double*, const int);
+int ATL_strtriCU(const enum ATLAS_DIAG, const int, float*, const int);
+int ATL_dtrtriCL(const enum ATLAS_DIAG, const int, double*, const int);
+int ATL_strtriCL(const enum ATLAS_DIAG, const int, float*, const int);
+int ATL_dtrtriRU(const enum ATLAS_DIAG, const int, double*, const int);
+int ATL_strtriRU(const enum ATLAS_DIAG, const int, float*, const int);
+int ATL_dtrtriRL(const enum ATLAS_DIAG, const int, double*, const int);
+int ATL_strtriRL(const enum ATLAS_DIAG, const int, float*, const int);
+int ATL_dgetri(const enum CBLAS_ORDER, const int, double*, const int, const int*, double*, int*);
+int ATL_sgetri(const enum CBLAS_ORDER, const int, float*, const int, const int*, float*, int*);
+int ATL_dgetriC(const int, double*, const int, const int*, double*, const int);
+int ATL_sgetriC(const int, float*, const int, const int*, float*, const int);
+int ATL_dgetriR(const int, double*, const int, const int*, double*, const int);
+int ATL_sgetriR(const int, float*, const int, const int*, float*, const int);
+/* blocking factor of the tuned build; the stand-in lives in ref_glue.c */
+int ATL_dlaGetB(int, int, int, int);
+int ATL_slaGetB(int, int, int, int);
 void ATL_dger(const int, const int, const double, const double*, const int, const double*,
               const int, double*, const int);
 void ATL_sger(const int, const int, const float, const float*, const int, const float*,

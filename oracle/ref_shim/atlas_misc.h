@@ -14,6 +14,8 @@
 #include "refshim_cblas.h"
 
 #define my_join(a_, b_) a_ ## b_
+#define my_str(x_) #x_
+#define Mstr(x_) my_str(x_)
 #define Mjoin(a_, b_) my_join(a_, b_)
 #define Mmin(x_, y_) (((x_) < (y_)) ? (x_) : (y_))
 #define Mmax(x_, y_) (((x_) > (y_)) ? (x_) : (y_))
@@ -26,6 +28,7 @@
    #define TREAL
    #define TYPE double
    #define PRE d
+   #define ATLAS_PRE d
    #define PATL ATL_d
    #define PATLU ATL_d
    #define ATL_MulBySize(x_) ((x_) << 3)
@@ -33,6 +36,7 @@
    #define TREAL
    #define TYPE float
    #define PRE s
+   #define ATLAS_PRE s
    #define PATL ATL_s
    #define PATLU ATL_s
    #define ATL_MulBySize(x_) ((x_) << 2)

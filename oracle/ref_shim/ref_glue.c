@@ -148,6 +148,24 @@ void atlref_##P##trsv(int order, int u, int t, int d, int N, const T *A, int lda
       ATL_##P##reftrsv(u == CblasUpper ? AtlasLower : AtlasUpper, t == CblasNoTrans ? AtlasTrans : AtlasNoTrans, \
                        (enum ATLAS_DIAG)d, N, A, lda, X, incx); \
 } \
+/* stand-in for the tuned blocking factor: 64 columns */ \
+int ATL_##P##laGetB(int M, int N, int K, int hint) { (void)M; (void)N; (void)K; (void)hint; return 64; } \
+int  ATL_##P##trtri(const enum ATLAS_ORDER, const enum ATLAS_UPLO, const enum ATLAS_DIAG, const int, T*, \
+   const int); \
+int  ATL_##P##getri(const enum CBLAS_ORDER, const int, T*, const int, const int*, T*, int*); \
+int  atlref_##P##trtri(int order, int u, int d, int N, T *A, int lda) \
+{ return ATL_##P##trtri((enum ATLAS_ORDER)order, (enum ATLAS_UPLO)u, (enum ATLAS_DIAG)d, N, A, lda); } \
+/* clapack_getri's workspace: laGetB * N entries (AtlasBase/Clint/atlas-clp.base:115-139) */ \
+int  atlref_##P##getri(int order, int N, T *A, int lda, const int *ipiv) \
+{ \
+   int lwrk = ATL_##P##laGetB(N, 0, N, 0), ierr; \
+   T *w; \
+   lwrk = (lwrk <= N) ? lwrk * N : N * N; \
+   w = (T*)malloc(sizeof(T) * (size_t)(lwrk > 0 ? lwrk : 1)); \
+   ierr = ATL_##P##getri((enum CBLAS_ORDER)order, N, A, lda, ipiv, w, &lwrk); \
+   free(w); \
+   return ierr; \
+} \
 void atlref_##P##potrs(int order, int u, int N, int NRHS, const T *A, int lda, T *B, int ldb) \
 { ATL_##P##potrs((enum CBLAS_ORDER)order, (enum CBLAS_UPLO)u, N, NRHS, A, lda, B, ldb); }
 

@@ -1,0 +1,7 @@
+/* Stand-in for the tuned build's sipgen_view.h: the blocking constants
+ * the extracted getri routines name.  TEST INFRASTRUCTURE ONLY. */
+#ifndef REFSHIM_SIPGEN_VIEW_H
+#define REFSHIM_SIPGEN_VIEW_H
+#define ATL_VWipgen_100LCMMN 4
+#define ATL_VWipgen_98KB 64
+#endif

@@ -50,6 +50,10 @@ def load():
     R.atlref_dtrmm.argtypes = [I, I, I, I, I, I, I, D, dp, I, dp, I]
     R.atlref_dgemv.argtypes = [I, I, I, I, D, dp, I, v1, I, D, v1, I]
     R.atlref_dtrsv.argtypes = [I, I, I, I, I, dp, I, v1, I]
+    R.atlref_dtrtri.argtypes = [I, I, I, I, dp, I]
+    R.atlref_dtrtri.restype = I
+    R.atlref_dgetri.argtypes = [I, I, dp, I, ip]
+    R.atlref_dgetri.restype = I
     return R
 
 
@@ -244,6 +248,31 @@ def main():
                         x = gegen(R, n * abs(incx), 1, n * abs(incx), 6)[:, 0].copy()
                         R.atlref_dtrsv(order, uplo, ta, diag, n, A, n, x, incx)
                         out[f"trsv_{order}_{uplo}_{ta}_{diag}_{incx}"] = x
+    # triangular inverse, both triangles, orders and diagonals
+    for uplo in (121, 122):
+        for order in (101, 102):
+            for diag in (131, 132):
+                for n in (1, 2, 3, 4, 5, 50):
+                    T = gegen(R, n, n, n, 3 + n)
+                    T += np.eye(n) * n
+                    info = R.atlref_dtrtri(order, uplo, diag, n, T, n)
+                    out[f"trtri_{uplo}_{order}_{diag}_{n}"] = T
+                    out[f"trtri_{uplo}_{order}_{diag}_{n}_info"] = np.array(info)
+    for (n, z) in ((10, 0), (50, 37), (130, 129)):
+        T = gegen(R, n, n, n, 3 + n)
+        T += np.eye(n) * n
+        T[z, z] = 0.0
+        out[f"trtri_sing_{n}_{z}_info"] = np.array(R.atlref_dtrtri(102, 121, 131, n, T, n))
+    # inverse from the LU factors
+    for n in (1, 2, 3, 5, 17, 64, 65, 100):
+        for order in (101, 102):
+            A = gegen(R, n, n, n, n * n + n)
+            piv = np.zeros(n, dtype=np.int32)
+            R.atlref_dgetrf(order, n, n, A, n, piv)
+            out[f"getri_{n}_{order}_lu"] = A.copy()
+            out[f"getri_{n}_{order}_piv"] = piv.copy()
+            out[f"getri_{n}_{order}_info"] = np.array(R.atlref_dgetri(order, n, A, n, piv))
+            out[f"getri_{n}_{order}_inv"] = A
     np.savez_compressed(OUT, **out)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")
 

@@ -221,3 +221,40 @@ def test_trsv_matches_reference_blas(ora, golden):
                         ora.trsv(uplo, ta, diag, n, A, x, incx, order=order)
                         ref = golden[f"trsv_{order}_{uplo}_{ta}_{diag}_{incx}"]
                         assert np.allclose(x, ref, rtol=1e-12, atol=1e-14), (order, uplo, ta, diag, incx)
+
+
+def test_trtri_matches_reference(ora, golden):
+    for uplo in (ora.Upper, ora.Lower):
+        for order in (101, 102):
+            for diag in (ora.NonUnit, ora.Unit):
+                for n in (1, 2, 3, 4, 5, 50):
+                    T = ora.gegen(n, n, 3 + n)
+                    T += np.eye(n) * n
+                    key = f"trtri_{uplo}_{order}_{diag}_{n}"
+                    assert ora.trtri(T, uplo, diag, order=order) == int(golden[key + "_info"]) == 0
+                    ref = golden[key]
+                    if order == 102 and n <= 4:   # the unrolled column-major cases
+                        assert np.array_equal(T, ref), key
+                    assert np.abs(T - ref).max() <= 1e-14 * n * max(1.0, np.abs(ref).max()), key
+
+
+def test_trtri_singular_info(ora, golden):
+    for (n, z) in ((10, 0), (50, 37), (130, 129)):
+        T = ora.gegen(n, n, 3 + n)
+        T += np.eye(n) * n
+        T[z, z] = 0.0
+        T0 = T.copy(order="F")
+        assert ora.trtri(T, ora.Upper) == int(golden[f"trtri_sing_{n}_{z}_info"]) == z + 1
+        assert np.array_equal(T, T0)
+
+
+def test_getri_matches_reference(ora, golden):
+    for n in (1, 2, 3, 5, 17, 64, 65, 100):
+        for order in (101, 102):
+            key = f"getri_{n}_{order}"
+            A = golden[key + "_lu"].copy(order="F")
+            assert ora.getri(A, golden[key + "_piv"], order=order) == int(golden[key + "_info"]) == 0
+            ref = golden[key + "_inv"]
+            if order == 102 and n <= 5:
+                assert np.array_equal(A, ref), key
+            assert np.abs(A - ref).max() <= 1e-13 * n * max(1.0, np.abs(ref).max()), key
