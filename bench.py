@@ -220,6 +220,7 @@ def measure_forms(G, O, torch, n=16384, kappas=(1e2, 1e6, 1e10), nslices=8):
         torch.exp2(torch.randint(-16, 17, (n, n), device=dev, generator=g).double())
     Cm = torch.zeros(n, n, device=dev, dtype=torch.float64)
     s = torch.cuda.ExternalStream(st)
+    torch.cuda.synchronize()      # the library stream does not wait for torch's stream
     ts = []
     for rep in range(3):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -303,9 +304,91 @@ def measure_next(G, O, torch, n=16384):
     t0 = time.perf_counter()
     O.potrf(Ah, uplo=O.Lower)
     tc = time.perf_counter() - t0
-    row["cpu_baseline"] = {"value": nc ** 3 / 3.0 / tc / 1e12, "unit": "TFLOP/s", "cores": 1, "kind": "port",
-                           "sample": f"oracle recursive potrfL n={nc} (reference-BLAS trsm/syrk, one thread)"}
+    thr = O.get_threads()
+    row["cpu_baseline"] = {"value": nc ** 3 / 3.0 / tc / 1e12, "unit": "TFLOP/s", "cores": thr, "kind": "port",
+                           "sample": f"oracle recursive potrfL n={nc} (restated reference trsm/syrk; the syrk "
+                                     "loops are serial, the gemm inside trsm uses the OpenMP threads)"}
     out["dposv_cholesky_n16384"] = row
+
+    # TRMM Left/Upper/NoTrans/NonUnit, 8192 x 8192: n^3 flops, event-timed
+    nt = 8192
+    g = torch.Generator(device="cuda").manual_seed(13)
+    A = torch.rand(nt, nt, device="cuda", dtype=torch.float64, generator=g) - 0.5
+    B0 = torch.rand(nt, nt, device="cuda", dtype=torch.float64, generator=g) - 0.5
+    B = torch.empty_like(B0)
+    s = torch.cuda.ExternalStream(st)
+    ms = []
+    for rep in range(3):
+        B.copy_(B0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        L.atlg_dtrmm_dev(141, 121, 111, 131, nt, nt, 1.0, C.c_void_p(A.data_ptr()), nt, C.c_void_p(B.data_ptr()),
+                         nt, st)
+        e1.record(s)
+        torch.cuda.synchronize()
+        if rep:
+            ms.append(e0.elapsed_time(e1))
+    # column-major views: the torch tensors hold A^T and B^T row-major
+    Bc = B.T
+    ref = torch.triu(A.T) @ B0.T
+    trmm_err = float((Bc - ref).abs().max() / ref.abs().max())
+    row = {"n": nt, "case": "Left/Upper/NoTrans/NonUnit, M=N=8192", "ms": min(ms),
+           "tflops": nt ** 3 / (min(ms) * 1e-3) / 1e12, "max_rel_err_vs_torch_fp64": trmm_err,
+           "timing": "CUDA events on the library stream around one cblas_dtrmm-equivalent device call "
+                     "(workspace copy of B included), best of 2 after one warm-up"}
+    ncpu = 1024
+    Ah = np.asfortranarray(A[:ncpu, :ncpu].cpu().numpy())
+    Bh = np.asfortranarray(B0[:ncpu, :ncpu].cpu().numpy())
+    t0 = time.perf_counter()
+    O.trmm(O.Left, O.Upper, O.NoTrans, O.NonUnit, ncpu, ncpu, 1.0, Ah, Bh)
+    tc = time.perf_counter() - t0
+    row["cpu_baseline"] = {"value": ncpu ** 3 / tc / 1e12, "unit": "TFLOP/s", "cores": 1, "kind": "port",
+                           "sample": f"oracle trmm M=N={ncpu} (reference-BLAS loop order, one thread)"}
+    out["dtrmm_n8192"] = row
+    del A, B, B0, ref, Bc
+    torch.cuda.empty_cache()
+
+    # getri: inverse from the dgetrf factors at 8192, 4/3 n^3 flops
+    ng = 8192
+    A0 = torch.rand(ng, ng, device="cuda", dtype=torch.float64, generator=g) - 0.5
+    A = A0.clone()
+    piv = torch.zeros(ng, dtype=torch.int32, device="cuda")
+    inf = torch.zeros(4, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()      # the library stream does not wait for torch's stream
+    L.atlg_dgetrf_dev(ng, ng, C.c_void_p(A.data_ptr()), ng, C.c_void_p(piv.data_ptr()),
+                      C.c_void_p(inf.data_ptr()), st)
+    torch.cuda.synchronize()
+    F = A.clone()
+    ts = []
+    for rep in range(3):
+        A.copy_(F)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        info = L.atlg_dgetri_dev(ng, C.c_void_p(A.data_ptr()), ng, C.c_void_p(piv.data_ptr()), st)
+        torch.cuda.synchronize()
+        if rep:
+            ts.append(time.perf_counter() - t0)
+    X = A.T                       # column-major inverse
+    M0 = A0.T
+    n1 = lambda Z: float(Z.abs().sum(dim=0).max())
+    resid = n1(X @ M0 - torch.eye(ng, device="cuda", dtype=torch.float64)) / (n1(X) * n1(M0) * ng *
+                                                                               np.finfo(float).eps)
+    row = {"n": ng, "ms": min(ts) * 1e3, "tflops": 4.0 / 3.0 * ng ** 3 / min(ts) / 1e12, "info": info,
+           "inverse_residual": resid,
+           "timing": "wall clock around atlg_dgetri_dev on the dgetrf factors (reads the pivots to the host, "
+                     "one info sync in trtri), best of 2 after one warm-up"}
+    nc = 1024
+    Ah = np.asfortranarray(A0[:nc, :nc].cpu().numpy())
+    info_c, ipiv_c = O.getrf(Ah)
+    t0 = time.perf_counter()
+    O.getri(Ah, ipiv_c)
+    tc = time.perf_counter() - t0
+    row["cpu_baseline"] = {"value": 4.0 / 3.0 * nc ** 3 / tc / 1e12, "unit": "TFLOP/s", "cores": thr, "kind": "port",
+                           "sample": f"oracle getri n={nc} (restated ATL_getriC on the oracle's trsm/gemm)"}
+    out["dgetri_n8192"] = row
+    del A, A0, F, X, M0
+    torch.cuda.empty_cache()
     return out
 
 
@@ -471,6 +554,8 @@ def run_case(args):
     sgetrf -- FP32 LU (FFMA trailing update) at n
     mixed  -- mixed-precision dgesv at n on A = G/sqrt(n) + 4I, run twice
     potrf  -- FP64 Cholesky (Lower) at n on a diagonally dominant SPD matrix
+    trmm   -- FP64 TRMM Left/Upper/NoTrans at M = N = n
+    getri  -- FP64 inverse from the dgetrf factors at n
     Prints one JSON line with the device time of the last run."""
     import ctypes as C
     import torch
@@ -485,6 +570,7 @@ def run_case(args):
         A = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g)
         B = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g)
         Cm = torch.zeros(n, n, device="cuda", dtype=torch.float64)
+        torch.cuda.synchronize()
         for _ in range(2):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(s)
@@ -497,12 +583,40 @@ def run_case(args):
         S = torch.randn(n, n, device="cuda", dtype=torch.float32, generator=g)
         piv = torch.zeros(n, dtype=torch.int32, device="cuda")
         inf = torch.zeros(4, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(s)
         L.atlg_sgetrf_dev(n, n, S.data_ptr(), n, piv.data_ptr(), inf.data_ptr(), st)
         e1.record(s)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
+    elif args.case == "trmm":
+        A = torch.rand(n, n, device="cuda", dtype=torch.float64, generator=g)
+        B = torch.rand(n, n, device="cuda", dtype=torch.float64, generator=g)
+        torch.cuda.synchronize()
+        for _ in range(2):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            L.atlg_dtrmm_dev(141, 121, 111, 131, n, n, 1.0, C.c_void_p(A.data_ptr()), n, C.c_void_p(B.data_ptr()),
+                             n, st)
+            e1.record(s)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+    elif args.case == "getri":
+        A0 = torch.rand(n, n, device="cuda", dtype=torch.float64, generator=g) - 0.5
+        piv = torch.zeros(n, dtype=torch.int32, device="cuda")
+        inf = torch.zeros(4, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        L.atlg_dgetrf_dev(n, n, C.c_void_p(A0.data_ptr()), n, C.c_void_p(piv.data_ptr()),
+                          C.c_void_p(inf.data_ptr()), st)
+        A = torch.empty_like(A0)
+        for _ in range(2):
+            A.copy_(A0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            L.atlg_dgetri_dev(n, C.c_void_p(A.data_ptr()), n, C.c_void_p(piv.data_ptr()), st)
+            torch.cuda.synchronize()
+            ms = (time.perf_counter() - t0) * 1e3
     elif args.case == "potrf":
         A0 = spd_device(torch, n, 11)
         A = torch.empty_like(A0)
@@ -541,7 +655,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=8192)
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
-    ap.add_argument("--case", choices=["split", "sgetrf", "mixed", "potrf"], default=None,
+    ap.add_argument("--case", choices=["split", "sgetrf", "mixed", "potrf", "trmm", "getri"], default=None,
                     help="run one kernel workload for a profiling capture instead of the benchmark")
     ap.add_argument("--skip-extras", action="store_true",
                     help="omit the n=16384 mixed-dgesv and split-DGEMM measurements")

@@ -181,7 +181,12 @@ int dgesv_adjoint(const int n, const int nrhs, const double *LU, const int lda,
 
 /* ---- device-pointer variants (no reference counterpart: the reference has
  *      no device memory; these are the same operations on GPU-resident data,
- *      column-major, used by callers that keep matrices in HBM) */
+ *      column-major, used by callers that keep matrices in HBM).
+ *      Ordering: work runs on `stream` (NULL: the library's own stream,
+ *      atlg_stream(), created non-blocking).  A non-blocking stream does not
+ *      wait for the legacy default stream or any other stream, so data written
+ *      on another stream must be ordered before the call by the caller (an
+ *      event wait or a device synchronize). */
 int      atlg_num_sms(void);
 void    *atlg_stream(void);
 unsigned atlg_status(void);   /* device wait-timeout flags since the last call, cleared */

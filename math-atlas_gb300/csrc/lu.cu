@@ -93,7 +93,10 @@ struct PanelRows {
   }
 };
 
-// Candidate records in global scratch, double buffered by column parity:
+// Candidate records in global scratch, double buffered by column parity.
+// Other CTAs write them between grid barriers, so every read after a barrier
+// goes to L2 (__ldcg): an L1 line from the same buffer two columns earlier
+// would otherwise be stale.
 // rec[(par*G + b)*RS + c] holds CTA b's candidate row (c < NB), then its
 // |a| (c = NB, negative: no candidate) and its row index (c = NB+1, exact in
 // T for any matrix this library can hold).  One record per CTA, so a
@@ -176,15 +179,15 @@ __global__ void __launch_bounds__(PT)
     // ---- global winner (identical in every CTA) ----
     if (gather_all) {
       // one round trip: every record (value, index, row) and row j
-      for (int e = threadIdx.x; e < G * RS; e += PT) gath[e] = rp[e];
-      for (int c = threadIdx.x; c < jb; c += PT) J[c] = jrow[par * NB + c];
+      for (int e = threadIdx.x; e < G * RS; e += PT) gath[e] = __ldcg(rp + e);
+      for (int c = threadIdx.x; c < jb; c += PT) J[c] = __ldcg(jrow + par * NB + c);
       __syncthreads();
     }
     if (threadIdx.x < 32) {
       T best = T(-1);
       int bb = 0x7fffffff;
       for (int b = threadIdx.x; b < G; b += 32) {
-        const T v = gather_all ? gath[b * RS + NB] : rp[(size_t)b * RS + NB];
+        const T v = gather_all ? gath[b * RS + NB] : __ldcg(rp + (size_t)b * RS + NB);
         if (v > best) { best = v; bb = b; }
       }
       for (int o = 16; o > 0; o >>= 1) {
@@ -194,7 +197,7 @@ __global__ void __launch_bounds__(PT)
       }
       if (threadIdx.x == 0) {
         int p = -1;
-        if (bb < G && best > T(0)) p = (int)(gather_all ? gath[bb * RS + NB + 1] : rp[(size_t)bb * RS + NB + 1]);
+        if (bb < G && best > T(0)) p = (int)(gather_all ? gath[bb * RS + NB + 1] : __ldcg(rp + (size_t)bb * RS + NB + 1));
         s_zero = (p < 0);
         s_p = (p < 0) ? j : p;
         s_piv = best;
@@ -215,8 +218,8 @@ __global__ void __launch_bounds__(PT)
         if (gather_all) {
           P[c] = gath[wb * RS + c];
         } else {
-          P[c] = rp[(size_t)wb * RS + c];
-          J[c] = jrow[par * NB + c];
+          P[c] = __ldcg(rp + (size_t)wb * RS + c);
+          J[c] = __ldcg(jrow + par * NB + c);
         }
       }
       __syncthreads();

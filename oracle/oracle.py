@@ -253,3 +253,7 @@ def backward_error(A, x, b):
 
 def set_threads(n):
     return lib().ora_set_threads(n)
+
+
+def get_threads():
+    return lib().ora_get_threads()

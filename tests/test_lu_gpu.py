@@ -156,3 +156,37 @@ def test_dgetrs_one_rhs_lookback_trsv(gb, ora, n, trans):
     ora.lib().ora_dgetrs(102, trans, n, 1, A, n, ipiv, bo, n)
     assert np.allclose(bg, bo, rtol=1e-9, atol=1e-9 * np.abs(bo).max())
     assert gb.status() == 0
+
+
+def test_dgetrf_sizes_in_sequence(gb):
+    """A smaller factorization followed by larger ones in one process: the
+    panel's candidate records are reused across columns and calls, and every
+    pivot must still satisfy ipiv[j] >= j with a small LU residual."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    L = gb.lib()
+    eps = np.finfo(float).eps
+    n1 = lambda Z: float(Z.abs().sum(dim=0).max())
+    for n in (4096, 6144, 2048, 8192):
+        g = torch.Generator(device="cuda").manual_seed(13)
+        A0 = torch.rand(n, n, device="cuda", dtype=torch.float64, generator=g) - 0.5
+        A = A0.clone()
+        piv = torch.zeros(n, dtype=torch.int32, device="cuda")
+        info = torch.zeros(4, dtype=torch.int32, device="cuda")
+        # the library stream does not wait for torch's stream
+        torch.cuda.synchronize()
+        L.atlg_dgetrf_dev(n, n, C.c_void_p(A.data_ptr()), n, C.c_void_p(piv.data_ptr()),
+                          C.c_void_p(info.data_ptr()), None)
+        torch.cuda.synchronize()
+        assert int(info[0]) == 0 and gb.status() == 0
+        p = piv.cpu().numpy()
+        assert (p >= np.arange(n)).all() and (p < n).all(), n
+        perm = np.arange(n)
+        for i in range(n):
+            perm[[i, p[i]]] = perm[[p[i], i]]
+        F = A.T
+        Lm = torch.tril(F, -1) + torch.eye(n, device="cuda", dtype=torch.float64)
+        resid = n1(A0.T[torch.from_numpy(perm).cuda()] - Lm @ torch.triu(F)) / (n1(A0.T) * n * eps)
+        assert resid <= 1.0, (n, resid)
+        del A, A0, Lm, F
+        torch.cuda.empty_cache()
