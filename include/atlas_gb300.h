@@ -228,6 +228,10 @@ int atlg_dlaswp_dev(int N, double *A, int lda, int K1, int K2, const int *ipiv, 
  * race: serialise them. */
 int atlg_dlaswp_noalloc(int N, double *A, int lda, int K1, int K2, const int *ipiv, int inci,
                         int nrows, void *stream);
+/* LU panel implementation: 1 (default) factors panels that fit one thread-
+ * block cluster's shared memory with the cluster kernel, 0 always uses the
+ * cooperative-grid kernel; both give bit-identical factors and pivots */
+void atlg_panel_cluster(int on);
 /* column-major LU; info written to device memory */
 int atlg_dgetrf_dev(int M, int N, double *A, int lda, int *ipiv, int *info, void *stream);
 int atlg_sgetrf_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void *stream);

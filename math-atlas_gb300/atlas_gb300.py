@@ -34,6 +34,7 @@ EXPORTS = [
     "cblas_dtrmm", "cblas_strmm", "cblas_dgemv", "cblas_sgemv", "cblas_dtrsv", "cblas_strsv",
     "atlg_dtrmm_dev", "atlg_dgemv_dev", "atlg_dtrsv_dev",
     "clapack_dtrtri", "clapack_strtri", "clapack_dgetri", "clapack_sgetri", "atlg_dtrtri_dev", "atlg_dgetri_dev",
+    "atlg_panel_cluster",
 ]
 
 _lib = None
@@ -99,6 +100,7 @@ def _declare(L):
         "clapack_sgetri": (_i, [_i, _i, _sp, _i, _ip]),
         "atlg_dtrtri_dev": (_i, [_i, _i, _i, _i, _v, _i, _v]),
         "atlg_dgetri_dev": (_i, [_i, _v, _i, _v, _v]),
+        "atlg_panel_cluster": (None, [_i]),
         "atlg_num_sms": (_i, []),
         "atlg_stream": (_v, []),
         "atlg_status": (_u, []),

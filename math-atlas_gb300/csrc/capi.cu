@@ -1071,6 +1071,7 @@ int atlg_dlaswp_dev(int N, double *A, int lda, int K1, int K2, const int *ipiv, 
   dev_dlaswp(N, A, lda, K1, K2, ipiv, inci, nrows, stream_of(stream));
   return 0;
 }
+void atlg_panel_cluster(int on) { set_panel_cluster(on != 0); }
 int atlg_dgetrf_dev(int M, int N, double *A, int lda, int *ipiv, int *info, void *stream) {
   if (M < 0 || N < 0 || lda < (M > 1 ? M : 1)) return -1;
   dev_dgetrf(M, N, A, lda, ipiv, info, stream_of(stream));

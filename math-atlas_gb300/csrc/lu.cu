@@ -26,6 +26,8 @@
 // pivot search are within rounding of each other; the factors agree to
 // rounding (different but equally stable summation order).
 #include <float.h>
+
+#include <cooperative_groups.h>
 #include <mutex>
 #include <vector>
 
@@ -35,6 +37,8 @@
 #include "lu.cuh"
 #include "tf32.cuh"
 #include "trsm.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace atlg {
 
@@ -129,6 +133,51 @@ __device__ void stage_candidate(const PanelRows<T, SM> &A, int j, int jb, int r0
     for (int c = threadIdx.x; c < jb; c += PT) r[c] = A.at(ci, c);
   if (j >= r0 && j < r1)
     for (int c = threadIdx.x; c < jb; c += PT) jrow[par * NB + c] = A.at(j, c);
+}
+
+// One warp: the panel's jb interchanges (row j <-> row piv_local[j], panel-
+// relative, in order) as one permutation of at most 2*NB rows, written as
+// perm = {count, dst[2NB], src[2NB]} for apply_perm_kernel.
+__device__ void reduce_interchanges(const int *piv_local, int jb, int *perm) {
+  __shared__ int rows[2 * NB], content[2 * NB];
+  __shared__ int cnt;
+  const int lane = threadIdx.x & 31;
+  for (int t = lane; t < jb; t += 32) { rows[t] = t; content[t] = t; }
+  if (lane == 0) cnt = jb;
+  __syncwarp();
+  for (int j = 0; j < jb; ++j) {
+    const int p = piv_local[j];
+    int slot;
+    if (p < jb) {
+      slot = p;
+    } else {
+      const int n = cnt;
+      int found = -1;
+      for (int base = jb; base < n; base += 32) {
+        const int t = base + lane;
+        const unsigned m = __ballot_sync(0xffffffffu, t < n && rows[t] == p);
+        if (m) { found = base + __ffs(m) - 1; break; }
+      }
+      if (found < 0) {
+        found = n;
+        if (lane == 0) { rows[n] = p; content[n] = p; cnt = n + 1; }
+      }
+      slot = found;
+    }
+    __syncwarp();
+    if (lane == 0 && slot != j) {
+      const int t = content[j];
+      content[j] = content[slot];
+      content[slot] = t;
+    }
+    __syncwarp();
+  }
+  const int n = cnt;
+  for (int t = lane; t < n; t += 32) {
+    perm[1 + t] = rows[t];
+    perm[1 + 2 * NB + t] = content[t];
+  }
+  if (lane == 0) perm[0] = n;
 }
 
 template <typename T, bool SM>
@@ -272,47 +321,165 @@ __global__ void __launch_bounds__(PT)
       }
   }
   // ---- CTA 0: reduce the NB interchanges to a permutation of rows ----
-  if (blockIdx.x == 0 && threadIdx.x < 32) {
-    __shared__ int rows[2 * NB], content[2 * NB];
-    __shared__ int cnt;
-    const int lane = threadIdx.x;
-    for (int t = lane; t < jb; t += 32) { rows[t] = t; content[t] = t; }
-    if (lane == 0) cnt = jb;
-    __syncwarp();
-    for (int j = 0; j < jb; ++j) {
-      const int p = piv_local[j];
-      int slot;
-      if (p < jb) {
-        slot = p;
-      } else {
-        const int n = cnt;
-        int found = -1;
-        for (int base = jb; base < n; base += 32) {
-          const int t = base + lane;
-          const unsigned m = __ballot_sync(0xffffffffu, t < n && rows[t] == p);
-          if (m) { found = base + __ffs(m) - 1; break; }
-        }
-        if (found < 0) {
-          found = n;
-          if (lane == 0) { rows[n] = p; content[n] = p; cnt = n + 1; }
-        }
-        slot = found;
-      }
-      __syncwarp();
-      if (lane == 0 && slot != j) {
-        const int t = content[j];
-        content[j] = content[slot];
-        content[slot] = t;
-      }
-      __syncwarp();
+  if (blockIdx.x == 0 && threadIdx.x < 32) reduce_interchanges(piv_local, jb, perm);
+}
+
+// ---------------------------------------------------------------------------
+// Cluster panel: the same factorization as panel_kernel (identical arithmetic
+// per element, so identical pivots and factors) for panels whose rows fit the
+// shared memory of one thread-block cluster (up to 16 CTAs on one GPC).  The
+// candidate exchange goes through distributed shared memory and the per-column
+// barrier is the cluster's hardware barrier instead of a grid barrier over L2.
+// Per column j: cluster barrier; every CTA reads the CN published candidates
+// (|a|, row) and picks the winner; reads the winner's row and row j from
+// their CTAs; eliminates in its own rows while finding its first-max for
+// column j+1; publishes that candidate (double buffered by column parity, so
+// a CTA never overwrites what a slower CTA still reads).
+template <typename T>
+struct ClusterSlots {
+  T crow[2][NB];   // this CTA's candidate row
+  T jrow[2][NB];   // row j, by the CTA that owns it
+  T cval[2];       // candidate |a| (negative: none)
+  int cidx[2];     // candidate row (panel-relative)
+};
+
+template <typename T>
+__global__ void __launch_bounds__(PT)
+    panel_cluster_kernel(T *Ag, int lda, int M, int jb, int koff, int *ipiv, int *info, int *perm) {
+  extern __shared__ __align__(16) unsigned char panel_dyn[];
+  __shared__ ClusterSlots<T> slot;
+  __shared__ BlockArgmax<T> sh;
+  __shared__ T P[NB], J[NB];
+  __shared__ int s_p, s_zero, s_win, s_ci;
+  __shared__ int piv_local[NB];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int CN = (int)cluster.num_blocks();
+  const int me = (int)cluster.block_rank();
+  const int tid = threadIdx.x;
+  const int chunk = (M + CN - 1) / CN;
+  const int r0 = me * chunk;
+  const int r1 = (r0 + chunk < M) ? r0 + chunk : M;
+  const int nr = r1 - r0;
+  T *sa = reinterpret_cast<T *>(panel_dyn);   // own rows, column-major, chunk rows
+#define AT(i_, c_) sa[((i_) - r0) + (size_t)(c_) * chunk]
+  if (nr > 0)
+    for (int e = tid; e < nr * jb; e += PT) {
+      const int i = e % nr, c = e / nr;
+      sa[i + (size_t)c * chunk] = Ag[(r0 + i) + (size_t)c * lda];
     }
-    const int n = cnt;
-    for (int t = lane; t < n; t += 32) {
-      perm[1 + t] = rows[t];
-      perm[1 + 2 * NB + t] = content[t];
+  __syncthreads();
+
+  // publish the candidate for column jn (after its values are final)
+  auto publish = [&](T best, int bi, int jn) {
+    block_argmax(best, bi, sh);
+    const int par = jn & 1;
+    if (tid == 0) {
+      slot.cval[par] = best;
+      slot.cidx[par] = best >= T(0) ? bi : -1;
+      s_ci = best >= T(0) ? bi : -1;
     }
-    if (lane == 0) perm[0] = n;
+    __syncthreads();
+    const int ci = s_ci;
+    if (ci >= 0 && tid < jb) slot.crow[par][tid] = AT(ci, tid);
+    if (jn >= r0 && jn < r1 && tid >= 128 && tid - 128 < jb) slot.jrow[par][tid - 128] = AT(jn, tid - 128);
+  };
+
+  {
+    T best = T(-1);
+    int bi = 0x7fffffff;
+    for (int i = r0 + tid; i < r1; i += PT) {
+      T a = AT(i, 0);
+      a = a < T(0) ? -a : a;
+      if (a > best) { best = a; bi = i; }
+    }
+    publish(best, bi, 0);
   }
+
+  for (int j = 0; j < jb; ++j) {
+    const int par = j & 1;
+    cluster.sync();
+    // ---- global winner (identical in every CTA) ----
+    if (tid < 32) {
+      T v = T(-1);
+      int b = 0x7fffffff, idx = -1;
+      if (tid < CN) {
+        const ClusterSlots<T> *rs = cluster.map_shared_rank(&slot, tid);
+        v = rs->cval[par];
+        idx = rs->cidx[par];
+        b = tid;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const T ov = __shfl_down_sync(0xffffffffu, v, o);
+        const int ob = __shfl_down_sync(0xffffffffu, b, o);
+        const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+        if (ov > v || (ov == v && ob < b)) { v = ov; b = ob; idx = oi; }
+      }
+      if (tid == 0) {
+        const int p = (b < CN && v > T(0)) ? idx : -1;
+        s_zero = (p < 0);
+        s_p = (p < 0) ? j : p;
+        s_win = b;
+      }
+    }
+    __syncthreads();
+    const int p = s_p;
+    const bool zero = s_zero != 0;
+    if (me == 0 && tid == 0) {
+      ipiv[j] = koff + p;
+      piv_local[j] = p;
+      if (zero && *info == 0) *info = koff + j + 1;
+    }
+    T best = T(-1);
+    int bi = 0x7fffffff;
+    if (!zero) {
+      const int wb = s_win, owner = j / chunk;
+      if (tid < jb) P[tid] = cluster.map_shared_rank(&slot, wb)->crow[par][tid];
+      else if (tid >= 128 && tid - 128 < jb) J[tid - 128] = cluster.map_shared_rank(&slot, owner)->jrow[par][tid - 128];
+      __syncthreads();
+      const T pv = P[j];
+      const T apv = pv < T(0) ? -pv : pv;
+      const bool use_rcp = apv > Lim<T>::safmin();
+      const T rcp = T(1) / pv;
+      const int lo = r0 > j ? r0 : j;
+      for (int i = lo + tid; i < r1; i += PT) {
+        if (i == j) {                       // row j <- pivot row
+          for (int c = 0; c < jb; ++c) AT(j, c) = P[c];
+          continue;
+        }
+        const T src = (i == p) ? J[j] : AT(i, j);
+        const T l = use_rcp ? src * rcp : src / pv;
+        AT(i, j) = l;
+        if (i == p) {                       // row p <- old row j, eliminated
+          for (int c = 0; c < j; ++c) AT(p, c) = J[c];
+          for (int c = j + 1; c < jb; ++c) AT(p, c) = J[c] - l * P[c];
+        } else {
+#pragma unroll 4
+          for (int c = j + 1; c < jb; ++c) AT(i, c) -= l * P[c];
+        }
+        if (j + 1 < jb) {
+          T a = AT(i, j + 1);
+          a = a < T(0) ? -a : a;
+          if (a > best) { best = a; bi = i; }
+        }
+      }
+    } else if (j + 1 < jb) {
+      const int lo = r0 > j + 1 ? r0 : j + 1;
+      for (int i = lo + tid; i < r1; i += PT) {
+        T a = AT(i, j + 1);
+        a = a < T(0) ? -a : a;
+        if (a > best) { best = a; bi = i; }
+      }
+    }
+    if (j + 1 < jb) publish(best, bi, j + 1);
+  }
+  cluster.sync();   // every remote read is done before any CTA leaves
+  if (nr > 0)
+    for (int e = tid; e < nr * jb; e += PT) {
+      const int i = e % nr, c = e / nr;
+      Ag[(r0 + i) + (size_t)c * lda] = sa[i + (size_t)c * chunk];
+    }
+#undef AT
+  if (me == 0 && tid < 32) reduce_interchanges(piv_local, jb, perm);
 }
 
 // Apply a row permutation (perm: count, dst[], src[] relative to row k) to
@@ -476,6 +643,48 @@ static void trailing_update(bool tc, int m, int n, int jb, const T *L21, const T
   gemm_any<T>(m, n, jb, L21, lda, U12 + (size_t)boff * lda, lda, C + (size_t)boff * lda, lda, st);
 }
 
+// Largest cluster (16, else 8 CTAs) the panel kernel can be launched with at
+// the full shared-memory size; 0 when clusters are unavailable.
+constexpr size_t kClusterSmemMax = 220 * 1024;
+static bool g_panel_cluster = true;
+
+template <typename T>
+static int cluster_panel_size() {
+  static std::once_flag once;
+  static int size = 0;
+  std::call_once(once, [] {
+    auto k = panel_cluster_kernel<T>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kClusterSmemMax) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return;
+    }
+    const int sizes[2] = {16, 8};
+    for (int q = 0; q < 2; ++q) {
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      cfg.gridDim = dim3(sizes[q]);
+      cfg.blockDim = dim3(PT);
+      cfg.dynamicSmemBytes = kClusterSmemMax;
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = sizes[q];
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int n = 0;
+      if (cudaOccupancyMaxActiveClusters(&n, (const void *)k, &cfg) == cudaSuccess && n > 0) {
+        size = sizes[q];
+        break;
+      }
+      (void)cudaGetLastError();
+    }
+  });
+  return size;
+}
+
+void set_panel_cluster(bool on) { g_panel_cluster = on; }
+
 template <typename T>
 static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaStream_t st, bool tc = false) {
   ATLG_CHECK(cudaMemsetAsync(info, 0, sizeof(int), st));
@@ -512,6 +721,8 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
   cudaStream_t side = c.side_stream();
   cudaEvent_t ev_ready = c.sync_event(0), ev_side = c.sync_event(1);
   bool side_pending = false;
+  const int cn = g_panel_cluster ? cluster_panel_size<T>() : 0;
+  bool used_cluster = false;
 
   for (int k = 0; k < MN; k += NB) {
     const int jb = (MN - k < NB) ? MN - k : NB;
@@ -520,12 +731,38 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     int *ipk = ipiv + k;
     int koff = k;
     void *args[] = {&Ap, (void *)&lda, &Mp, (void *)&jb, &koff, &ipk, &info, &rec, &jrow, &bar, &perm};
-    // the CTA's rows of the panel live in shared memory when they fit
-    const size_t tile = sizeof(T) * (size_t)((Mp + G - 1) / G) * jb;
-    if (tile <= kPanelSmemMax)
-      ATLG_CHECK(cudaLaunchCooperativeKernel((const void *)panel_kernel<T, true>, dim3(G), dim3(PT), args, tile, st));
-    else
-      ATLG_CHECK(cudaLaunchCooperativeKernel((const void *)panel_kernel<T, false>, dim3(G), dim3(PT), args, 0, st));
+    // one cluster when the panel fits its shared memory (panels only shrink,
+    // so the grid path below is never needed after it)
+    const size_t ctile = cn ? sizeof(T) * (size_t)((Mp + cn - 1) / cn) * NB : 0;
+    if (cn && ctile <= kClusterSmemMax) {
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      cfg.gridDim = dim3(cn);
+      cfg.blockDim = dim3(PT);
+      cfg.dynamicSmemBytes = ctile;
+      cfg.stream = st;
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = cn;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      ATLG_CHECK(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T>, Ap, lda, Mp, jb, koff, ipk, info, perm));
+      used_cluster = true;
+    } else {
+      if (used_cluster) {   // the grid barrier counts every earlier column
+        const unsigned base = (unsigned)koff * (unsigned)G;
+        ATLG_CHECK(cudaMemcpyAsync(bar, &base, sizeof(unsigned), cudaMemcpyHostToDevice, st));
+        ATLG_CHECK(cudaStreamSynchronize(st));
+        used_cluster = false;
+      }
+      // the CTA's rows of the panel live in shared memory when they fit
+      const size_t tile = sizeof(T) * (size_t)((Mp + G - 1) / G) * jb;
+      if (tile <= kPanelSmemMax)
+        ATLG_CHECK(cudaLaunchCooperativeKernel((const void *)panel_kernel<T, true>, dim3(G), dim3(PT), args, tile, st));
+      else
+        ATLG_CHECK(cudaLaunchCooperativeKernel((const void *)panel_kernel<T, false>, dim3(G), dim3(PT), args, 0, st));
+    }
     note_launch();
     // the interchanges touch every other column: the side update must be done
     if (side_pending) {

@@ -4,6 +4,10 @@
 
 namespace atlg {
 
+// false forces the cooperative-grid panel (the cluster panel is the default
+// where the panel fits one cluster's shared memory); results are identical.
+void set_panel_cluster(bool on);
+
 // Column-major LU with partial pivoting of the M x N matrix A (device).
 // ipiv (device, min(M,N) ints, 0-based, global row indices) and info
 // (device int: 0, or the 1-based index of the first exactly-zero pivot).

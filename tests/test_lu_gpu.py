@@ -190,3 +190,27 @@ def test_dgetrf_sizes_in_sequence(gb):
         assert resid <= 1.0, (n, resid)
         del A, A0, Lm, F
         torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_cluster_panel_matches_grid_panel(gb, ora, dtype):
+    """The cluster panel (distributed shared memory, hardware cluster barrier)
+    and the cooperative-grid panel do the same arithmetic: bit-identical
+    pivots and factors, for panels on both sides of the cluster's capacity."""
+    L = gb.lib()
+    sizes = (700, 3000, 7100) if dtype == np.float64 else (700, 5000, 15000)
+    try:
+        for n in sizes:
+            A0 = ora.gegen(n, n, n * n + n, dtype=dtype)
+            out = []
+            for on in (1, 0):
+                L.atlg_panel_cluster(on)
+                A = A0.copy(order="F")
+                piv = np.zeros(n, dtype=np.int32)
+                f = gb.clapack_dgetrf if dtype == np.float64 else gb.clapack_sgetrf
+                assert f(102, n, n, A, n, piv) == 0
+                out.append((A, piv))
+            assert np.array_equal(out[0][1], out[1][1]), n
+            assert np.array_equal(out[0][0], out[1][0]), n
+    finally:
+        L.atlg_panel_cluster(1)
