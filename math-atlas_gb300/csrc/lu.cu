@@ -327,156 +327,306 @@ __global__ void __launch_bounds__(PT)
 // ---------------------------------------------------------------------------
 // Cluster panel: the same factorization as panel_kernel (identical arithmetic
 // per element, so identical pivots and factors) for panels whose rows fit the
-// shared memory of one thread-block cluster (up to 16 CTAs on one GPC).  The
-// candidate exchange goes through distributed shared memory and the per-column
-// barrier is the cluster's hardware barrier instead of a grid barrier over L2.
-// Per column j: cluster barrier; every CTA reads the CN published candidates
-// (|a|, row) and picks the winner; reads the winner's row and row j from
-// their CTAs; eliminates in its own rows while finding its first-max for
-// column j+1; publishes that candidate (double buffered by column parity, so
-// a CTA never overwrites what a slower CTA still reads).
-template <typename T>
-struct ClusterSlots {
-  T crow[2][NB];   // this CTA's candidate row
-  T jrow[2][NB];   // row j, by the CTA that owns it
-  T cval[2];       // candidate |a| (negative: none)
-  int cidx[2];     // candidate row (panel-relative)
-};
+// shared memory of one thread-block cluster (up to 16 CTAs on one GPC).
+// Per column j: each CTA keeps its first-max candidate row (and the owner of
+// row j that row) in its own shared memory and pushes only the candidate's
+// |a| and row index into every CTA; one hardware cluster barrier; each warp
+// then picks the winner from its own CTA's copy of the candidates; the CTA
+// pulls the winner's row and row j with 16-byte distributed-shared-memory
+// loads and eliminates in its rows (batched loads ahead of the stores)
+// before it reduces its first-max of column j+1.  Two CTA barriers and one
+// cluster barrier per column.  Everything a CTA publishes is
+// double buffered by column parity: column j+1 is published only after the
+// barrier of column j, which every CTA reaches after reading column j.
+constexpr int kClusterMax = 16;
 
 template <typename T>
-__global__ void __launch_bounds__(PT)
+struct ClusterSlots {
+  __align__(16) T crow[2][NB];   // own candidate row
+  __align__(16) T jrow[2][NB];   // row j, in the CTA that owns it
+  T cval[2][kClusterMax];        // pushed by every CTA: candidate |a| (< 0: none)
+  int cidx[2][kClusterMax];      //                      candidate row
+};
+
+template <typename T> struct Vec16;
+template <> struct Vec16<float> { using type = float4; };
+template <> struct Vec16<double> { using type = double2; };
+
+// (larger |a|, then lower source) wins; every lane ends with the winner
+template <typename T>
+__device__ __forceinline__ void warp_winner(T &v, int &b, int &idx) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const T ov = __shfl_xor_sync(0xffffffffu, v, o);
+    const int ob = __shfl_xor_sync(0xffffffffu, b, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+    if (ov > v || (ov == v && ob < b)) { v = ov; b = ob; idx = oi; }
+  }
+}
+
+constexpr int CT = 512;         // threads per cluster-panel CTA (16 warps)
+
+// Row stride of the cluster panel's shared-memory tile: NB plus one 16-byte
+// vector, an odd number of vectors, so 16-byte accesses to consecutive rows
+// hit distinct banks.
+template <typename T> __host__ __device__ constexpr int cl_rs() { return NB + 16 / (int)sizeof(T); }
+
+// Vector update of one row's columns [cb, jb) (cb >= 1): a -= l * P.
+template <typename T>
+__device__ __forceinline__ void row_axpy(T *row, const T *P, T l, int cb, int jb) {
+  using V = typename Vec16<T>::type;
+  constexpr int VE = 16 / (int)sizeof(T);
+  const int nvj = (jb + VE - 1) / VE;
+  int q = cb / VE;
+  V *rv = reinterpret_cast<V *>(row);
+  const V *pvec = reinterpret_cast<const V *>(P);
+  if (q < nvj && (cb % VE != 0 || (q + 1) * VE > jb)) {   // first vector, masked
+    V a0 = rv[q];
+    const V p0 = pvec[q];
+    T *x0 = reinterpret_cast<T *>(&a0);
+    const T *y0 = reinterpret_cast<const T *>(&p0);
+#pragma unroll
+    for (int e = 0; e < VE; ++e)
+      if (q * VE + e >= cb && q * VE + e < jb) x0[e] -= l * y0[e];
+    rv[q] = a0;
+    ++q;
+  }
+  const int qend = jb / VE;
+  for (; q + 1 < qend; q += 2) {
+    V a0 = rv[q], a1 = rv[q + 1];
+    const V p0 = pvec[q], p1 = pvec[q + 1];
+    T *x0 = reinterpret_cast<T *>(&a0);
+    T *x1 = reinterpret_cast<T *>(&a1);
+    const T *y0 = reinterpret_cast<const T *>(&p0);
+    const T *y1 = reinterpret_cast<const T *>(&p1);
+#pragma unroll
+    for (int e = 0; e < VE; ++e) {
+      x0[e] -= l * y0[e];
+      x1[e] -= l * y1[e];
+    }
+    rv[q] = a0;
+    rv[q + 1] = a1;
+  }
+  if (q < qend) {
+    V a0 = rv[q];
+    const V p0 = pvec[q];
+    T *x0 = reinterpret_cast<T *>(&a0);
+    const T *y0 = reinterpret_cast<const T *>(&p0);
+#pragma unroll
+    for (int e = 0; e < VE; ++e) x0[e] -= l * y0[e];
+    rv[q] = a0;
+    ++q;
+  }
+  if (q < nvj) {   // partial last vector
+    V a0 = rv[q];
+    const V p0 = pvec[q];
+    T *x0 = reinterpret_cast<T *>(&a0);
+    const T *y0 = reinterpret_cast<const T *>(&p0);
+#pragma unroll
+    for (int e = 0; e < VE; ++e)
+      if (q * VE + e < jb) x0[e] -= l * y0[e];
+    rv[q] = a0;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(CT)
     panel_cluster_kernel(T *Ag, int lda, int M, int jb, int koff, int *ipiv, int *info, int *perm) {
+  using V = typename Vec16<T>::type;
+  constexpr int VE = 16 / (int)sizeof(T);        // elements per 16-byte vector
+  constexpr int NV = NB / VE;                    // vectors per row
+  constexpr int RS = cl_rs<T>();
+  constexpr int NW = CT / 32;
   extern __shared__ __align__(16) unsigned char panel_dyn[];
   __shared__ ClusterSlots<T> slot;
-  __shared__ BlockArgmax<T> sh;
-  __shared__ T P[NB], J[NB];
-  __shared__ int s_p, s_zero, s_win, s_ci;
+  // pivot row and row j, double buffered by column parity: a thread still in
+  // the previous column's phase 2 may read one while the next is pulled
+  __shared__ __align__(16) T Pb[2][NB];
+  __shared__ __align__(16) T Jb[2][NB];
+  __shared__ T wv[NW];
+  __shared__ int wi[NW];
   __shared__ int piv_local[NB];
   cg::cluster_group cluster = cg::this_cluster();
   const int CN = (int)cluster.num_blocks();
   const int me = (int)cluster.block_rank();
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int chunk = (M + CN - 1) / CN;
   const int r0 = me * chunk;
   const int r1 = (r0 + chunk < M) ? r0 + chunk : M;
   const int nr = r1 - r0;
-  T *sa = reinterpret_cast<T *>(panel_dyn);   // own rows, column-major, chunk rows
-#define AT(i_, c_) sa[((i_) - r0) + (size_t)(c_) * chunk]
+  const int nvj = (jb + VE - 1) / VE;            // vectors holding the jb columns
+  T *sa = reinterpret_cast<T *>(panel_dyn);      // own rows, row-major, stride RS
+#define AT(i_, c_) sa[(size_t)((i_) - r0) * RS + (c_)]
   if (nr > 0)
-    for (int e = tid; e < nr * jb; e += PT) {
+    for (int e = tid; e < nr * jb; e += CT) {
       const int i = e % nr, c = e / nr;
-      sa[i + (size_t)c * chunk] = Ag[(r0 + i) + (size_t)c * lda];
+      sa[(size_t)i * RS + c] = Ag[(r0 + i) + (size_t)c * lda];
     }
-  __syncthreads();
+  cluster.sync();   // every CTA of the cluster is running before the first push
 
-  // publish the candidate for column jn (after its values are final)
-  auto publish = [&](T best, int bi, int jn) {
-    block_argmax(best, bi, sh);
-    const int par = jn & 1;
-    if (tid == 0) {
-      slot.cval[par] = best;
-      slot.cidx[par] = best >= T(0) ? bi : -1;
-      s_ci = best >= T(0) ? bi : -1;
+  // Reduce the per-thread candidates (rows ci already complete) to the CTA's
+  // first-max; keep its row and row jn locally, push |a| and row to all.
+  auto publish = [&](T best, int bi, int jn) -> int {
+    for (int o = 16; o > 0; o >>= 1) {
+      const T ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi && ov >= T(0))) { best = ov; bi = oi; }
     }
+    if (lane == 0) { wv[w] = best; wi[w] = bi; }
     __syncthreads();
-    const int ci = s_ci;
-    if (ci >= 0 && tid < jb) slot.crow[par][tid] = AT(ci, tid);
-    if (jn >= r0 && jn < r1 && tid >= 128 && tid - 128 < jb) slot.jrow[par][tid - 128] = AT(jn, tid - 128);
+    best = lane < NW ? wv[lane] : T(-1);
+    bi = lane < NW ? wi[lane] : 0x7fffffff;
+    for (int o = 16; o > 0; o >>= 1) {
+      const T ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi && ov >= T(0))) { best = ov; bi = oi; }
+    }
+    return best >= T(0) ? bi : -1;
+  };
+  auto push = [&](T best, int ci, int jn) {
+    const int par = jn & 1;
+    if (ci >= 0 && tid < nvj)
+      reinterpret_cast<V *>(slot.crow[par])[tid] = reinterpret_cast<const V *>(&AT(ci, 0))[tid];
+    if (jn >= r0 && jn < r1 && tid >= 64 && tid - 64 < nvj)
+      reinterpret_cast<V *>(slot.jrow[par])[tid - 64] = reinterpret_cast<const V *>(&AT(jn, 0))[tid - 64];
+    if (tid < CN) {
+      ClusterSlots<T> *rs = cluster.map_shared_rank(&slot, tid);
+      rs->cval[par][me] = best;
+      rs->cidx[par][me] = ci;
+    }
   };
 
   {
     T best = T(-1);
     int bi = 0x7fffffff;
-    for (int i = r0 + tid; i < r1; i += PT) {
+    for (int i = r0 + tid; i < r1; i += CT) {
       T a = AT(i, 0);
       a = a < T(0) ? -a : a;
       if (a > best) { best = a; bi = i; }
     }
-    publish(best, bi, 0);
+    const int ci = publish(best, bi, 0);
+    T cv = T(-1);
+    if (ci >= 0) { cv = AT(ci, 0); cv = cv < T(0) ? -cv : cv; }
+    push(cv, ci, 0);
   }
 
   for (int j = 0; j < jb; ++j) {
     const int par = j & 1;
-    cluster.sync();
-    // ---- global winner (identical in every CTA) ----
-    if (tid < 32) {
-      T v = T(-1);
-      int b = 0x7fffffff, idx = -1;
-      if (tid < CN) {
-        const ClusterSlots<T> *rs = cluster.map_shared_rank(&slot, tid);
-        v = rs->cval[par];
-        idx = rs->cidx[par];
-        b = tid;
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        const T ov = __shfl_down_sync(0xffffffffu, v, o);
-        const int ob = __shfl_down_sync(0xffffffffu, b, o);
-        const int oi = __shfl_down_sync(0xffffffffu, idx, o);
-        if (ov > v || (ov == v && ob < b)) { v = ov; b = ob; idx = oi; }
-      }
-      if (tid == 0) {
-        const int p = (b < CN && v > T(0)) ? idx : -1;
-        s_zero = (p < 0);
-        s_p = (p < 0) ? j : p;
-        s_win = b;
-      }
-    }
-    __syncthreads();
-    const int p = s_p;
-    const bool zero = s_zero != 0;
+    if (j == 0) cluster.sync();
+    else cluster.barrier_wait();
+    // ---- global winner, computed by every warp from its own CTA's slots ----
+    T v = T(-1);
+    int b = 0x7fffffff, idx = -1;
+    if (lane < CN) { v = slot.cval[par][lane]; idx = slot.cidx[par][lane]; b = lane; }
+    warp_winner(v, b, idx);
+    const bool zero = !(b < CN && v > T(0));
+    const int p = zero ? j : idx;
     if (me == 0 && tid == 0) {
       ipiv[j] = koff + p;
       piv_local[j] = p;
       if (zero && *info == 0) *info = koff + j + 1;
     }
+    const bool last = (j + 1 >= jb);
     T best = T(-1);
     int bi = 0x7fffffff;
     if (!zero) {
-      const int wb = s_win, owner = j / chunk;
-      if (tid < jb) P[tid] = cluster.map_shared_rank(&slot, wb)->crow[par][tid];
-      else if (tid >= 128 && tid - 128 < jb) J[tid - 128] = cluster.map_shared_rank(&slot, owner)->jrow[par][tid - 128];
-      __syncthreads();
-      const T pv = P[j];
+      // the winner's row and row j, pulled once per CTA
+      T *Ps = Pb[par];
+      T *Js = Jb[par];
+      if (tid < 2 * NV) {
+        if (tid < NV)
+          reinterpret_cast<V *>(Ps)[tid] = reinterpret_cast<const V *>(cluster.map_shared_rank(slot.crow[par], b))[tid];
+        else
+          reinterpret_cast<V *>(Js)[tid - NV] =
+              reinterpret_cast<const V *>(cluster.map_shared_rank(slot.jrow[par], j / chunk))[tid - NV];
+      }
+      __syncthreads();   // also: every thread is done with the previous column's phase 2
+      const T pv = Ps[j];
       const T apv = pv < T(0) ? -pv : pv;
       const bool use_rcp = apv > Lim<T>::safmin();
       const T rcp = T(1) / pv;
       const int lo = r0 > j ? r0 : j;
-      for (int i = lo + tid; i < r1; i += PT) {
+      // phase 1: multipliers and column j+1 of every own row (rows j and p
+      // completely), with the first-max of column j+1
+      for (int i = lo + tid; i < r1; i += CT) {
+        T *row = &AT(i, 0);
         if (i == j) {                       // row j <- pivot row
-          for (int c = 0; c < jb; ++c) AT(j, c) = P[c];
+          for (int q = 0; q < nvj; ++q) reinterpret_cast<V *>(row)[q] = reinterpret_cast<const V *>(Ps)[q];
           continue;
         }
-        const T src = (i == p) ? J[j] : AT(i, j);
-        const T l = use_rcp ? src * rcp : src / pv;
-        AT(i, j) = l;
         if (i == p) {                       // row p <- old row j, eliminated
-          for (int c = 0; c < j; ++c) AT(p, c) = J[c];
-          for (int c = j + 1; c < jb; ++c) AT(p, c) = J[c] - l * P[c];
+          const T l = use_rcp ? Js[j] * rcp : Js[j] / pv;
+          for (int c = 0; c < j; ++c) row[c] = Js[c];
+          row[j] = l;
+          for (int c = j + 1; c < jb; ++c) row[c] = Js[c] - l * Ps[c];
         } else {
-#pragma unroll 4
-          for (int c = j + 1; c < jb; ++c) AT(i, c) -= l * P[c];
+          const T src = row[j];
+          const T l = use_rcp ? src * rcp : src / pv;
+          row[j] = l;
+          if (!last) row[j + 1] -= l * Ps[j + 1];
         }
-        if (j + 1 < jb) {
-          T a = AT(i, j + 1);
+        if (!last) {
+          T a = row[j + 1];
           a = a < T(0) ? -a : a;
           if (a > best) { best = a; bi = i; }
         }
       }
-    } else if (j + 1 < jb) {
+      if (!last) {
+        const int ci = publish(best, bi, j + 1);
+        // complete the rows other CTAs may read: the candidate and row j+1
+        const bool own_next = (j + 1 >= r0 && j + 1 < r1);
+        if (tid < 32) {
+          const int r = tid < 16 ? ci : (own_next ? j + 1 : -1);
+          if (r >= 0 && r != p && r != j && (tid < 16 || r != ci)) {
+            // 16 lanes per row, one vector each, over the columns j+2 .. jb-1
+            for (int q = (tid & 15) + (j + 2) / VE; q < nvj; q += 16) {
+              T *row = &AT(r, 0);
+              const T l = row[j];
+              V a0 = reinterpret_cast<V *>(row)[q];
+              const V p0 = reinterpret_cast<const V *>(Ps)[q];
+              T *x0 = reinterpret_cast<T *>(&a0);
+              const T *y0 = reinterpret_cast<const T *>(&p0);
+#pragma unroll
+              for (int e = 0; e < VE; ++e)
+                if (q * VE + e >= j + 2 && q * VE + e < jb) x0[e] -= l * y0[e];
+              reinterpret_cast<V *>(row)[q] = a0;
+            }
+          }
+        }
+        __syncthreads();
+        T cv = T(-1);
+        if (ci >= 0) { cv = AT(ci, j + 1); cv = cv < T(0) ? -cv : cv; }
+        push(cv, ci, j + 1);
+        cluster.barrier_arrive();
+        // phase 2 (overlaps the barrier): columns j+2.. of the other rows
+        if (j + 2 < jb) {
+          for (int i = lo + tid; i < r1; i += CT) {
+            if (i == j || i == p || i == ci || i == j + 1) continue;
+            T *row = &AT(i, 0);
+            row_axpy<T>(row, Ps, row[j], j + 2, jb);
+          }
+        }
+      }
+    } else if (!last) {
       const int lo = r0 > j + 1 ? r0 : j + 1;
-      for (int i = lo + tid; i < r1; i += PT) {
+      for (int i = lo + tid; i < r1; i += CT) {
         T a = AT(i, j + 1);
         a = a < T(0) ? -a : a;
         if (a > best) { best = a; bi = i; }
       }
+      const int ci = publish(best, bi, j + 1);
+      __syncthreads();
+      T cv = T(-1);
+      if (ci >= 0) { cv = AT(ci, j + 1); cv = cv < T(0) ? -cv : cv; }
+      push(cv, ci, j + 1);
+      cluster.barrier_arrive();
     }
-    if (j + 1 < jb) publish(best, bi, j + 1);
+    if (last) break;
   }
-  cluster.sync();   // every remote read is done before any CTA leaves
+  cluster.sync();   // no CTA leaves while another may still read or push to it
   if (nr > 0)
-    for (int e = tid; e < nr * jb; e += PT) {
+    for (int e = tid; e < nr * jb; e += CT) {
       const int i = e % nr, c = e / nr;
-      Ag[(r0 + i) + (size_t)c * lda] = sa[i + (size_t)c * chunk];
+      Ag[(r0 + i) + (size_t)c * lda] = sa[(size_t)i * RS + c];
     }
 #undef AT
   if (me == 0 && tid < 32) reduce_interchanges(piv_local, jb, perm);
@@ -664,7 +814,7 @@ static int cluster_panel_size() {
       cudaLaunchConfig_t cfg = {};
       cudaLaunchAttribute at[1];
       cfg.gridDim = dim3(sizes[q]);
-      cfg.blockDim = dim3(PT);
+      cfg.blockDim = dim3(CT);
       cfg.dynamicSmemBytes = kClusterSmemMax;
       at[0].id = cudaLaunchAttributeClusterDimension;
       at[0].val.clusterDim.x = sizes[q];
@@ -733,12 +883,12 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     void *args[] = {&Ap, (void *)&lda, &Mp, (void *)&jb, &koff, &ipk, &info, &rec, &jrow, &bar, &perm};
     // one cluster when the panel fits its shared memory (panels only shrink,
     // so the grid path below is never needed after it)
-    const size_t ctile = cn ? sizeof(T) * (size_t)((Mp + cn - 1) / cn) * NB : 0;
+    const size_t ctile = cn ? sizeof(T) * (size_t)((Mp + cn - 1) / cn) * cl_rs<T>() : 0;
     if (cn && ctile <= kClusterSmemMax) {
       cudaLaunchConfig_t cfg = {};
       cudaLaunchAttribute at[1];
       cfg.gridDim = dim3(cn);
-      cfg.blockDim = dim3(PT);
+      cfg.blockDim = dim3(CT);
       cfg.dynamicSmemBytes = ctile;
       cfg.stream = st;
       at[0].id = cudaLaunchAttributeClusterDimension;
