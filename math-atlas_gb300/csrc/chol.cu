@@ -115,14 +115,18 @@ void dev_ssyreflect(int n, float *C, int ldc, cudaStream_t st) { syreflect_impl<
 
 // Factor the nb x nb diagonal block at A (nb <= 64) in shared memory, as
 // L L^T (Lower) or U^T U (Upper, handled as the transpose).  One barrier per
-// column: step j reads the pivot, every thread forms 1/sqrt redundantly and
-// applies the rank-1 update with the scaled column computed on the fly;
-// column j itself is scaled in step j+1, when nothing reads it any more.
-// Four threads share a row.  On a non-positive pivot j the block keeps that
-// value, *info gets koff + j + 1 and the factorization stops.
+// column: step j applies the rank-1 update with the scaled column computed on
+// the fly (column j itself is scaled in step j+1, when nothing reads it any
+// more).  The square root and reciprocal of each pivot are computed once, by
+// the thread that finishes that diagonal entry, and read from shared memory
+// (FP64 division and square root are expensive on GB300's FP64 pipe).  Four
+// threads share a row.  On a non-positive pivot j the block keeps that value,
+// *info gets koff + j + 1 and the factorization stops.
 template <typename T>
 __global__ void __launch_bounds__(256) potf2_kernel(int nb, int uplo, T *A, int lda, int koff, int *info) {
   __shared__ T a[CB][CB + 1];
+  __shared__ T s_sq[3], s_rc[3];   // by step mod 3: step j reads j and j-1, writes j+1
+  __shared__ int s_ok[3];
   const int tid = threadIdx.x;
   const int row = tid >> 2, q = tid & 3;
   for (int e = tid; e < nb * nb; e += 256) {
@@ -130,25 +134,34 @@ __global__ void __launch_bounds__(256) potf2_kernel(int nb, int uplo, T *A, int 
     if (i >= k) a[i][k] = (uplo == kLower) ? A[i + (size_t)k * lda] : A[k + (size_t)i * lda];
   }
   __syncthreads();
+  auto pivot = [&](int j) {   // one thread: pivot j's square root and reciprocal
+    const T ajj = a[j][j];
+    const int ok = ajj > T(0);
+    const T sj = ok ? sqrt(ajj) : T(0);
+    s_sq[j % 3] = sj;
+    s_rc[j % 3] = ok ? T(1) / sj : T(0);
+    s_ok[j % 3] = ok;
+  };
+  if (tid == 0) pivot(0);
+  __syncthreads();
   int fail = 0;
-  T s_prev = T(0), r_prev = T(0);
   for (int j = 0; j < nb; ++j) {
-    const T ajj = a[j][j];   // same value in every thread: the loop exits uniformly
+    const int b = j % 3, bp = (j + 2) % 3;
     if (j > 0 && q == 0) {   // finish column j-1
-      if (row == j - 1) a[row][row] = s_prev;
-      else if (row > j - 1 && row < nb) a[row][j - 1] *= r_prev;
+      if (row == j - 1) a[row][row] = s_sq[bp];
+      else if (row > j - 1 && row < nb) a[row][j - 1] *= s_rc[bp];
     }
-    if (!(ajj > T(0))) { fail = j + 1; break; }
-    const T sj = sqrt(ajj), r = T(1) / sj;
+    if (!s_ok[b]) { fail = j + 1; break; }   // same in every thread
+    const T r = s_rc[b];
     if (row > j && row < nb) {
       const T lij = a[row][j] * r;
       for (int k = j + 1 + q; k <= row; k += 4) a[row][k] -= lij * (a[k][j] * r);
+      // the thread that just finished a[j+1][j+1] prepares the next pivot
+      if (row == j + 1 && q == 0) pivot(j + 1);
     }
-    s_prev = sj;
-    r_prev = r;
     __syncthreads();
   }
-  if (!fail && q == 0 && row == nb - 1) a[row][row] = s_prev;
+  if (!fail && q == 0 && row == nb - 1) a[row][row] = s_sq[(nb - 1) % 3];
   __syncthreads();
   // write back the processed columns (the failing pivot column as it stands)
   const int done = fail ? fail : nb;

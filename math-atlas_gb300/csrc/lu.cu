@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(PT)
   __shared__ BlockArgmax<T> sh;
   __shared__ T P[NB], J[NB];
   __shared__ int s_idx, s_p, s_zero;
-  __shared__ T s_piv;
+  __shared__ T s_piv, s_rcp;
   __shared__ int piv_local[NB];
   constexpr int LB = SM ? 1 : 2048;
   __shared__ T lbuf[LB];
@@ -270,12 +270,13 @@ __global__ void __launch_bounds__(PT)
           P[c] = __ldcg(rp + (size_t)wb * RS + c);
           J[c] = __ldcg(jrow + par * NB + c);
         }
+        if (c == j) s_rcp = T(1) / P[c];   // once per CTA: FP64 division is costly
       }
       __syncthreads();
       const T pv = P[j];
       const T apv = pv < T(0) ? -pv : pv;
       const bool use_rcp = apv > Lim<T>::safmin();
-      const T rcp = T(1) / pv;
+      const T rcp = s_rcp;
       // pass 1: multipliers (column j) and the two swapped rows' L parts
       const int lo = r0 > j ? r0 : j;
       for (int i = lo + threadIdx.x; i < r1; i += PT) {
@@ -442,6 +443,7 @@ __global__ void __launch_bounds__(CT)
   // the previous column's phase 2 may read one while the next is pulled
   __shared__ __align__(16) T Pb[2][NB];
   __shared__ __align__(16) T Jb[2][NB];
+  __shared__ T s_rcp[2];
   __shared__ T wv[NW];
   __shared__ int wi[NW];
   __shared__ int piv_local[NB];
@@ -533,9 +535,18 @@ __global__ void __launch_bounds__(CT)
       T *Ps = Pb[par];
       T *Js = Jb[par];
       if (tid < 2 * NV) {
-        if (tid < NV)
-          reinterpret_cast<V *>(Ps)[tid] = reinterpret_cast<const V *>(cluster.map_shared_rank(slot.crow[par], b))[tid];
-        else
+        if (tid < NV) {
+          const V pvec = reinterpret_cast<const V *>(cluster.map_shared_rank(slot.crow[par], b))[tid];
+          reinterpret_cast<V *>(Ps)[tid] = pvec;
+          if (tid == j / VE) {   // once per CTA: FP64 division is costly
+            const T *pe = reinterpret_cast<const T *>(&pvec);
+            T pj = pe[0];
+#pragma unroll
+            for (int e = 1; e < VE; ++e)
+              if (tid * VE + e == j) pj = pe[e];
+            s_rcp[par] = T(1) / pj;
+          }
+        } else
           reinterpret_cast<V *>(Js)[tid - NV] =
               reinterpret_cast<const V *>(cluster.map_shared_rank(slot.jrow[par], j / chunk))[tid - NV];
       }
@@ -543,7 +554,7 @@ __global__ void __launch_bounds__(CT)
       const T pv = Ps[j];
       const T apv = pv < T(0) ? -pv : pv;
       const bool use_rcp = apv > Lim<T>::safmin();
-      const T rcp = T(1) / pv;
+      const T rcp = s_rcp[par];
       const int lo = r0 > j ? r0 : j;
       // phase 1: multipliers and column j+1 of every own row (rows j and p
       // completely), with the first-max of column j+1
