@@ -159,8 +159,8 @@ def run_reference(args):
 
 # ------------------------------------------------------------- other forms
 def measure_forms(G, O, torch, n=16384, kappas=(1e2, 1e6, 1e10), nslices=8):
-    """The two other FP64-accuracy forms at n=16384 (SURVEY configs 3 and 4):
-    mixed-precision dgesv on A = U diag(s) V^T (U, V from Householder QR of
+    """The other FP64-accuracy forms at n=16384: mixed-precision dgesv and the
+    split-DGEMM LU dgesv on A = U diag(s) V^T (U, V from Householder QR of
     seeded Gaussian matrices, s geometric 1..1/kappa) against the plain FP64
     dgesv on the same matrix, and the split-precision DGEMM on
     uniform[-1,1]*2^e operands (e in [-16,16]) against the double-double
@@ -177,6 +177,7 @@ def measure_forms(G, O, torch, n=16384, kappas=(1e2, 1e6, 1e10), nslices=8):
     piv = torch.zeros(n, dtype=torch.int32, device=dev)
     info_d = torch.zeros(4, dtype=torch.int32, device=dev)
     rows = []
+    srows = []
     plain_t = None
     for kappa in kappas:
         sv = torch.logspace(0, -np.log10(kappa), n, device=dev, dtype=torch.float64)
@@ -208,8 +209,26 @@ def measure_forms(G, O, torch, n=16384, kappas=(1e2, 1e6, 1e10), nslices=8):
             row["forward_vs_plain_fp64"] = float((X - xb).abs().max() / xb.abs().max())
         row["speedup_vs_plain_fp64"] = plain_t / min(ts)
         rows.append(row)
+        # split-DGEMM form: FP64 LU with tensor-core (integer-slice) updates
+        ts2 = []
+        for rep in range(2):
+            A.copy_(Acm)
+            xs = b.clone()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sinfo = L.atlg_dgetrf_split_dev(n, A.data_ptr(), n, piv.data_ptr(), 8, st)
+            L.atlg_dgetrs_dev(102, 111, n, 1, A.data_ptr(), n, piv.data_ptr(), xs.data_ptr(), n, st)
+            torch.cuda.synchronize()
+            ts2.append(time.perf_counter() - t0)
+        Am = Acm.T                                  # the column-major matrix
+        r = b - Am @ xs
+        sberr = float(r.abs().max() / (Am.abs().sum(dim=1).max() * xs.abs().max() + b.abs().max()))
+        srows.append({"kappa": kappa, "ms": min(ts2) * 1e3, "tflops": dgesv_flops(n) / min(ts2) / 1e12,
+                      "info": sinfo, "backward_error": sberr, "n_eps": n * np.finfo(float).eps,
+                      "speedup_vs_plain_fp64": plain_t / min(ts2)})
         del A, Acm
     out["mixed_dgesv_n16384"] = rows
+    out["split_lu_dgesv_n16384"] = srows
     out["plain_dgesv_n16384"] = {"ms": plain_t * 1e3, "tflops": dgesv_flops(n) / plain_t / 1e12}
     del U, V
     torch.cuda.empty_cache()
@@ -556,6 +575,7 @@ def run_case(args):
     potrf  -- FP64 Cholesky (Lower) at n on a diagonally dominant SPD matrix
     trmm   -- FP64 TRMM Left/Upper/NoTrans at M = N = n
     getri  -- FP64 inverse from the dgetrf factors at n
+    splitlu -- FP64 LU with split-DGEMM (tensor-core) trailing updates at n
     Prints one JSON line with the device time of the last run."""
     import ctypes as C
     import torch
@@ -590,6 +610,17 @@ def run_case(args):
         e1.record(s)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
+    elif args.case == "splitlu":
+        A0 = torch.rand(n, n, device="cuda", dtype=torch.float64, generator=g) - 0.5
+        A = torch.empty_like(A0)
+        piv = torch.zeros(n, dtype=torch.int32, device="cuda")
+        for _ in range(2):
+            A.copy_(A0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            L.atlg_dgetrf_split_dev(n, C.c_void_p(A.data_ptr()), n, C.c_void_p(piv.data_ptr()), 8, st)
+            torch.cuda.synchronize()
+            ms = (time.perf_counter() - t0) * 1e3
     elif args.case == "trmm":
         A = torch.rand(n, n, device="cuda", dtype=torch.float64, generator=g)
         B = torch.rand(n, n, device="cuda", dtype=torch.float64, generator=g)
@@ -655,7 +686,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=8192)
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
-    ap.add_argument("--case", choices=["split", "sgetrf", "mixed", "potrf", "trmm", "getri"], default=None,
+    ap.add_argument("--case", choices=["split", "sgetrf", "mixed", "potrf", "trmm", "getri", "splitlu"], default=None,
                     help="run one kernel workload for a profiling capture instead of the benchmark")
     ap.add_argument("--skip-extras", action="store_true",
                     help="omit the n=16384 mixed-dgesv and split-DGEMM measurements")

@@ -28,6 +28,7 @@
 #include "gemm.cuh"
 #include "getri.cuh"
 #include "lu.cuh"
+#include "lu_split.cuh"
 #include "mixed.cuh"
 #include "split.cuh"
 #include "tf32.cuh"
@@ -874,6 +875,34 @@ int clapack_sgetri(const enum CBLAS_ORDER Order, const int N, float *A, const in
   return host_getri<float>("clapack_sgetri", Order, N, A, lda, ipiv);
 }
 
+// Split-DGEMM form of dgesv (no reference counterpart; see lu_split.cu):
+// clapack_dgesv's ColMajor interface and checks; the LU's trailing updates run
+// on the split-precision DGEMM with 8 slices, the solve is the FP64 getrs.
+int dgesv_split(const int N, const int NRHS, double *A, const int lda, int *ipiv, double *B, const int ldb) {
+  const char *rout = "dgesv_split";
+  if (N < 0) cblas_xerbla(1, rout, "N cannot be less than zero 0,; is set to %d.\n", N);
+  if (NRHS < 0) cblas_xerbla(2, rout, "NRHS cannot be less than zero 0,; is set to %d.\n", NRHS);
+  if (lda < N || lda < 1) cblas_xerbla(4, rout, "lda must be >= MAX(N,1): lda=%d N=%d\n", lda, N);
+  if (ldb < N || ldb < 1) cblas_xerbla(7, rout, "ldb must be >= MAX(N,1): ldb=%d N=%d\n", ldb, N);
+  if (N == 0) return 0;
+  cudaStream_t st = ctx().stream;
+  int ldd;
+  double *dA = to_dev<double>(kBufA, A, N, N, lda, &ldd, st);
+  int *dpiv = static_cast<int *>(ctx().buffer(kBufPiv, sizeof(int) * (size_t)N));
+  const int info = dev_dgetrf_split(N, dA, ldd, dpiv, 8, st);
+  to_host<double>(A, lda, dA, ldd, N, N, st);
+  ATLG_CHECK(cudaMemcpyAsync(ipiv, dpiv, sizeof(int) * N, cudaMemcpyDeviceToHost, st));
+  if (info == 0 && NRHS > 0) {
+    int ldd_b;
+    double *dB = to_dev<double>(kBufB, B, N, NRHS, ldb, &ldd_b, st);
+    dev_dgetrs(kColMajor, kNoTrans, N, NRHS, dA, ldd, dpiv, dB, ldd_b, st);
+    to_host<double>(B, ldb, dB, ldd_b, N, NRHS, st);
+  }
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  check_status(rout);
+  return info;
+}
+
 // Split-precision DGEMM (no reference counterpart; see split.cu): the
 // cblas_dgemm interface and checks, plus the number of 7-bit slices per
 // operand (1..8; 7 gives about 49 bits of each row/column's largest entry).
@@ -1140,6 +1169,10 @@ int atlg_dgetri_dev(int N, double *A, int lda, const int *ipiv, void *stream) {
   ATLG_CHECK(cudaMemcpyAsync(hp.data(), ipiv, sizeof(int) * N, cudaMemcpyDeviceToHost, st));
   ATLG_CHECK(cudaStreamSynchronize(st));
   return dev_dgetri(N, A, lda, hp.data(), st);
+}
+int atlg_dgetrf_split_dev(int N, double *A, int lda, int *ipiv, int nslices, void *stream) {
+  if (N < 0 || lda < (N > 1 ? N : 1) || nslices < 1 || nslices > 8) return -1;
+  return dev_dgetrf_split(N, A, lda, ipiv, nslices, stream_of(stream));
 }
 int atlg_dgetrs_dev(int Order, int Trans, int N, int NRHS, const double *A, int lda, const int *ipiv, double *B,
                     int ldb, void *stream) {

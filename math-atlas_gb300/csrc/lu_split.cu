@@ -1,0 +1,82 @@
+// lu_split.cu -- FP64 LU whose trailing updates run on the split-precision
+// DGEMM (integer slices on tcgen05 tensor cores, split.cu): the "split-DGEMM
+// form" of dgesv.  No reference counterpart: ATLAS has one LU, in FP64 on the
+// FP64 pipe (ATL_getrfC, AtlasBase/Clint/atlas-lp.base:1210-1617); this
+// factorization computes the same partial-pivoting LU with the O(n^3) part of
+// the work moved to the tensor pipe.
+//
+// Outer blocks of NB2 = 512 columns, right-looking:
+//  1. the (n-k) x 512 block column is factored by the FP64 LU (lu.cu: 64-wide
+//     panels, look-ahead, DFMA updates inside the block column);
+//  2. its interchanges are applied to the columns left and right of it;
+//  3. U12 = L11^-1 A12 as inv(L11) (unit lower, trtri in FP64) times A12 on
+//     the split DGEMM;
+//  4. A22 -= L21 U12 on the split DGEMM with K = 512.
+// With 8 slices each split product is accurate to about 3e-16 of
+// sum |a||b| (the FP64 GEMM's own error bound is of that order), so the
+// factorization is FP64-accurate at any condition number.  Pivots can differ
+// from the plain FP64 LU where two candidates are within rounding.
+#include "common.cuh"
+#include "context.cuh"
+#include "getri.cuh"
+#include "lu.cuh"
+#include "lu_split.cuh"
+#include "split.cuh"
+
+namespace atlg {
+
+constexpr int NB2 = 512;
+
+__global__ void add_offset_kernel(int *ipiv, int n, int off) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) ipiv[i] += off;
+}
+
+// W = the unit lower triangle of the kb x kb block at A (zeros above).
+__global__ void unit_lower_kernel(int kb, const double *A, int lda, double *W, int ldw) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int j = blockIdx.y; j < kb; j += gridDim.y)
+    if (i < kb) W[i + (size_t)j * ldw] = (i > j) ? A[i + (size_t)j * lda] : (i == j ? 1.0 : 0.0);
+}
+
+int dev_dgetrf_split(int n, double *A, int lda, int *ipiv, int nslices, cudaStream_t st) {
+  if (n <= 0) return 0;
+  Context &c = ctx();
+  int *dinfo = static_cast<int *>(c.buffer(kBufX2, 64));
+  int info = 0;
+  for (int k = 0; k < n; k += NB2) {
+    const int kb = (n - k < NB2) ? n - k : NB2;
+    const int m = n - k, r = n - k - kb;
+    double *Akk = A + k + (size_t)k * lda;
+    dev_dgetrf(m, kb, Akk, lda, ipiv + k, dinfo, st);   // pivots relative to row k
+    int hinfo = 0;
+    ATLG_CHECK(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+    // interchanges on the rows k.. of the columns left and right of the block
+    if (k > 0) dev_dlaswp(k, A + k, lda, 0, kb, ipiv + k, 1, m, st);
+    if (r > 0) dev_dlaswp(r, A + k + (size_t)(k + kb) * lda, lda, 0, kb, ipiv + k, 1, m, st);
+    add_offset_kernel<<<(kb + 255) / 256, 256, 0, st>>>(ipiv + k, kb, k);
+    note_launch();
+    ATLG_CHECK(cudaGetLastError());
+    ATLG_CHECK(cudaStreamSynchronize(st));
+    if (hinfo > 0 && info == 0) info = k + hinfo;
+    if (r <= 0) continue;
+    double *A12 = A + k + (size_t)(k + kb) * lda;
+    // U12 = inv(L11) A12, through a workspace
+    const int ldw = (kb + 1) & ~1;
+    double *W = static_cast<double *>(c.buffer(kBufX0, sizeof(double) * (size_t)ldw * kb));
+    double *T = static_cast<double *>(c.buffer(kBufX1, sizeof(double) * (size_t)ldw * r));
+    unit_lower_kernel<<<dim3((kb + 255) / 256, kb), 256, 0, st>>>(kb, Akk, lda, W, ldw);
+    note_launch();
+    ATLG_CHECK(cudaGetLastError());
+    dev_dtrtri(kColMajor, kLower, kUnit, kb, W, ldw, st);
+    dev_dgemm_split(kNoTrans, kNoTrans, kb, r, kb, 1.0, W, ldw, A12, lda, 0.0, T, ldw, nslices, st);
+    ATLG_CHECK(cudaMemcpy2DAsync(A12, sizeof(double) * lda, T, sizeof(double) * ldw, sizeof(double) * kb, r,
+                                 cudaMemcpyDeviceToDevice, st));
+    // A22 -= L21 U12
+    dev_dgemm_split(kNoTrans, kNoTrans, r, r, kb, -1.0, Akk + kb, lda, A12, lda, 1.0,
+                    A + (k + kb) + (size_t)(k + kb) * lda, lda, nslices, st);
+  }
+  return info;
+}
+
+}  // namespace atlg

@@ -1,0 +1,13 @@
+// lu_split.cuh -- FP64 LU with split-precision (tensor-core) trailing updates.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace atlg {
+
+// Column-major n x n partial-pivoting LU in place (0-based absolute pivots);
+// returns 0 or the 1-based index of the first zero pivot.  nslices: 7-bit
+// slices per operand of the split products (8 for FP64 accuracy).
+// Synchronizes once per 512 columns (the block column's info).
+int dev_dgetrf_split(int n, double *A, int lda, int *ipiv, int nslices, cudaStream_t st);
+
+}  // namespace atlg

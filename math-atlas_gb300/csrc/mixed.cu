@@ -25,6 +25,7 @@
 #include "context.cuh"
 #include "gemm.cuh"
 #include "lu.cuh"
+#include "lu_split.cuh"
 #include "mixed.cuh"
 
 namespace atlg {
@@ -225,10 +226,8 @@ int dev_dgesv_mixed(int n, int nrhs, double *A, int lda, int *ipiv, const double
     double *F = static_cast<double *>(c.buffer(kBufW6, sizeof(double) * (size_t)ldf * n));
     copy_d_kernel<<<grid_for((long)n * n), 256, 0, st>>>(n, n, A, lda, F, ldf);
     note_launch();
-    dev_dgetrf(n, n, F, ldf, ipiv, dinfo, st);
-    int i64 = 0;
-    ATLG_CHECK(cudaMemcpyAsync(&i64, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
-    ATLG_CHECK(cudaStreamSynchronize(st));
+    // FP64-accurate LU with its O(n^3) updates on the tensor pipe (lu_split.cu)
+    const int i64 = dev_dgetrf_split(n, F, ldf, ipiv, 8, st);
     if (i64 != 0) {
       res->status = 2;
       copy_d_kernel<<<grid_for((long)n * n), 256, 0, st>>>(n, n, F, ldf, A, lda);

@@ -1,7 +1,7 @@
 """Mixed-precision dgesv (FP32 LU + FP64 iterative refinement, FP64
 fallback) through the C ABI.  A = U diag(s) V^T with U, V from Householder QR
 of seeded Gaussian matrices and s geometric from 1 to 1/kappa; b Gaussian.
-Accuracy is judged against the FP64 oracle solve: normwise backward error
+Accuracy is measured against the FP64 oracle solve: normwise backward error
 <= n*eps (double-double residual), forward error comparable to the FP64
 LU's."""
 import numpy as np
