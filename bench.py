@@ -216,7 +216,7 @@ def measure_forms(G, O, torch, n=16384, kappas=(1e2, 1e6, 1e10), nslices=8):
             xs = b.clone()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            sinfo = L.atlg_dgetrf_split_dev(n, A.data_ptr(), n, piv.data_ptr(), 8, st)
+            sinfo = L.atlg_dgetrf_split_dev(n, A.data_ptr(), n, piv.data_ptr(), 8, 1024, st)
             L.atlg_dgetrs_dev(102, 111, n, 1, A.data_ptr(), n, piv.data_ptr(), xs.data_ptr(), n, st)
             torch.cuda.synchronize()
             ts2.append(time.perf_counter() - t0)
@@ -618,7 +618,7 @@ def run_case(args):
             A.copy_(A0)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            L.atlg_dgetrf_split_dev(n, C.c_void_p(A.data_ptr()), n, C.c_void_p(piv.data_ptr()), 8, st)
+            L.atlg_dgetrf_split_dev(n, C.c_void_p(A.data_ptr()), n, C.c_void_p(piv.data_ptr()), 8, 1024, st)
             torch.cuda.synchronize()
             ms = (time.perf_counter() - t0) * 1e3
     elif args.case == "trmm":

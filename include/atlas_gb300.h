@@ -175,7 +175,7 @@ int dgesv_mixed(const int N, const int NRHS, double *A, const int lda, int *ipiv
                 const double *B, const int ldb, double *X, const int ldx, double *berr,
                 double *ferr, int *iters, int *status);
 /* Split-DGEMM form of dgesv: clapack_dgesv's ColMajor interface; the LU's
- * trailing updates (outer blocks of 512 columns) run on the split-precision
+ * trailing updates (outer blocks of 1024 columns) run on the split-precision
  * DGEMM with 8 slices, FP64-accurate at any condition number; the solve is the
  * FP64 getrs.  Returns 0 or the first zero pivot (1-based). */
 int dgesv_split(const int N, const int NRHS, double *A, const int lda, int *ipiv,
@@ -243,9 +243,11 @@ void atlg_panel_cluster(int on);
 /* column-major LU; info written to device memory */
 int atlg_dgetrf_dev(int M, int N, double *A, int lda, int *ipiv, int *info, void *stream);
 int atlg_sgetrf_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void *stream);
-/* the split-DGEMM LU on device data (0-based device pivots); returns info;
- * synchronizes once per 512 columns */
-int atlg_dgetrf_split_dev(int N, double *A, int lda, int *ipiv, int nslices, void *stream);
+/* the split-DGEMM LU on device data (0-based device pivots), nslices 1..8,
+ * outer block nb (rounded down to a multiple of 256; 1024 in dgesv_split);
+ * returns info; synchronizes once per outer block */
+int atlg_dgetrf_split_dev(int N, double *A, int lda, int *ipiv, int nslices, int nb,
+                          void *stream);
 int atlg_dgetrs_dev(int Order, int Trans, int N, int NRHS, const double *A, int lda,
                     const int *ipiv, double *B, int ldb, void *stream);
 /* column-major SYRK / Cholesky on device data (Uplo, Trans, Order take the

@@ -102,7 +102,7 @@ def _declare(L):
         "atlg_dgetri_dev": (_i, [_i, _v, _i, _v, _v]),
         "atlg_panel_cluster": (None, [_i]),
         "dgesv_split": (_i, [_i, _i, _dp, _i, _ip, _dp, _i]),
-        "atlg_dgetrf_split_dev": (_i, [_i, _v, _i, _v, _i, _v]),
+        "atlg_dgetrf_split_dev": (_i, [_i, _v, _i, _v, _i, _i, _v]),
         "atlg_num_sms": (_i, []),
         "atlg_stream": (_v, []),
         "atlg_status": (_u, []),

@@ -889,7 +889,7 @@ int dgesv_split(const int N, const int NRHS, double *A, const int lda, int *ipiv
   int ldd;
   double *dA = to_dev<double>(kBufA, A, N, N, lda, &ldd, st);
   int *dpiv = static_cast<int *>(ctx().buffer(kBufPiv, sizeof(int) * (size_t)N));
-  const int info = dev_dgetrf_split(N, dA, ldd, dpiv, 8, st);
+  const int info = dev_dgetrf_split(N, dA, ldd, dpiv, 8, 1024, st);
   to_host<double>(A, lda, dA, ldd, N, N, st);
   ATLG_CHECK(cudaMemcpyAsync(ipiv, dpiv, sizeof(int) * N, cudaMemcpyDeviceToHost, st));
   if (info == 0 && NRHS > 0) {
@@ -1170,9 +1170,9 @@ int atlg_dgetri_dev(int N, double *A, int lda, const int *ipiv, void *stream) {
   ATLG_CHECK(cudaStreamSynchronize(st));
   return dev_dgetri(N, A, lda, hp.data(), st);
 }
-int atlg_dgetrf_split_dev(int N, double *A, int lda, int *ipiv, int nslices, void *stream) {
-  if (N < 0 || lda < (N > 1 ? N : 1) || nslices < 1 || nslices > 8) return -1;
-  return dev_dgetrf_split(N, A, lda, ipiv, nslices, stream_of(stream));
+int atlg_dgetrf_split_dev(int N, double *A, int lda, int *ipiv, int nslices, int nb, void *stream) {
+  if (N < 0 || lda < (N > 1 ? N : 1) || nslices < 1 || nslices > 8 || nb < 256) return -1;
+  return dev_dgetrf_split(N, A, lda, ipiv, nslices, nb, stream_of(stream));
 }
 int atlg_dgetrs_dev(int Order, int Trans, int N, int NRHS, const double *A, int lda, const int *ipiv, double *B,
                     int ldb, void *stream) {

@@ -84,6 +84,15 @@ cudaStream_t Context::side_stream() {
   return side;
 }
 
+cudaStream_t Context::outer_stream() {
+  if (!outer) {
+    int lo = 0, hi = 0;
+    ATLG_CHECK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    ATLG_CHECK(cudaStreamCreateWithPriority(&outer, cudaStreamNonBlocking, lo));
+  }
+  return outer;
+}
+
 cudaEvent_t Context::sync_event(int i) {
   if (!sync_ev[i]) ATLG_CHECK(cudaEventCreateWithFlags(&sync_ev[i], cudaEventDisableTiming));
   return sync_ev[i];

@@ -5,13 +5,18 @@
 // factorization computes the same partial-pivoting LU with the O(n^3) part of
 // the work moved to the tensor pipe.
 //
-// Outer blocks of NB2 = 512 columns, right-looking:
-//  1. the (n-k) x 512 block column is factored by the FP64 LU (lu.cu: 64-wide
+// Outer blocks of nb columns (a multiple of 256; 1024 by default), right-
+// looking, with look-ahead:
+//  1. the (n-k) x nb block column is factored by the FP64 LU (lu.cu: 64-wide
 //     panels, look-ahead, DFMA updates inside the block column);
 //  2. its interchanges are applied to the columns left and right of it;
 //  3. U12 = L11^-1 A12 as inv(L11) (unit lower, trtri in FP64) times A12 on
 //     the split DGEMM;
-//  4. A22 -= L21 U12 on the split DGEMM with K = 512.
+//  4. A22 -= L21 U12 on the split DGEMM with K = nb, sliced once: the next
+//     block column's tiles on the caller's stream, the rest on a second
+//     low-priority stream, so the FP64 factorization of the next block column
+//     (FP64 pipe) overlaps the bulk of the update (tensor pipe); the next
+//     interchanges wait for it.
 // With 8 slices each split product is accurate to about 3e-16 of
 // sum |a||b| (the FP64 GEMM's own error bound is of that order), so the
 // factorization is FP64-accurate at any condition number.  Pivots can differ
@@ -25,7 +30,6 @@
 
 namespace atlg {
 
-constexpr int NB2 = 512;
 
 __global__ void add_offset_kernel(int *ipiv, int n, int off) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -39,18 +43,28 @@ __global__ void unit_lower_kernel(int kb, const double *A, int lda, double *W, i
     if (i < kb) W[i + (size_t)j * ldw] = (i > j) ? A[i + (size_t)j * lda] : (i == j ? 1.0 : 0.0);
 }
 
-int dev_dgetrf_split(int n, double *A, int lda, int *ipiv, int nslices, cudaStream_t st) {
+int dev_dgetrf_split(int n, double *A, int lda, int *ipiv, int nslices, int nb, cudaStream_t st) {
   if (n <= 0) return 0;
+  const int NB2 = (nb >= kSplitTileN) ? (nb / kSplitTileN) * kSplitTileN : 512;
   Context &c = ctx();
   int *dinfo = static_cast<int *>(c.buffer(kBufX2, 64));
+  cudaStream_t outer = c.outer_stream();
+  cudaEvent_t ev_ready = c.sync_event(2), ev_done = c.sync_event(3);
+  bool outer_pending = false;
   int info = 0;
   for (int k = 0; k < n; k += NB2) {
     const int kb = (n - k < NB2) ? n - k : NB2;
     const int m = n - k, r = n - k - kb;
     double *Akk = A + k + (size_t)k * lda;
+    // the block column was brought up to date by the previous step's first
+    // update; the rest of that update may still run on the outer stream
     dev_dgetrf(m, kb, Akk, lda, ipiv + k, dinfo, st);   // pivots relative to row k
     int hinfo = 0;
     ATLG_CHECK(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (outer_pending) {   // the interchanges touch every column
+      ATLG_CHECK(cudaStreamWaitEvent(st, ev_done, 0));
+      outer_pending = false;
+    }
     // interchanges on the rows k.. of the columns left and right of the block
     if (k > 0) dev_dlaswp(k, A + k, lda, 0, kb, ipiv + k, 1, m, st);
     if (r > 0) dev_dlaswp(r, A + k + (size_t)(k + kb) * lda, lda, 0, kb, ipiv + k, 1, m, st);
@@ -61,6 +75,7 @@ int dev_dgetrf_split(int n, double *A, int lda, int *ipiv, int nslices, cudaStre
     if (hinfo > 0 && info == 0) info = k + hinfo;
     if (r <= 0) continue;
     double *A12 = A + k + (size_t)(k + kb) * lda;
+    double *A22 = A + (k + kb) + (size_t)(k + kb) * lda;
     // U12 = inv(L11) A12, through a workspace
     const int ldw = (kb + 1) & ~1;
     double *W = static_cast<double *>(c.buffer(kBufX0, sizeof(double) * (size_t)ldw * kb));
@@ -72,10 +87,22 @@ int dev_dgetrf_split(int n, double *A, int lda, int *ipiv, int nslices, cudaStre
     dev_dgemm_split(kNoTrans, kNoTrans, kb, r, kb, 1.0, W, ldw, A12, lda, 0.0, T, ldw, nslices, st);
     ATLG_CHECK(cudaMemcpy2DAsync(A12, sizeof(double) * lda, T, sizeof(double) * ldw, sizeof(double) * kb, r,
                                  cudaMemcpyDeviceToDevice, st));
-    // A22 -= L21 U12
-    dev_dgemm_split(kNoTrans, kNoTrans, r, r, kb, -1.0, Akk + kb, lda, A12, lda, 1.0,
-                    A + (k + kb) + (size_t)(k + kb) * lda, lda, nslices, st);
+    // A22 -= L21 U12 from one slicing: the next block column first (so the
+    // next factorization can start), the rest on the outer stream
+    SplitPlan plan;
+    dev_dgemm_split_prepare(kNoTrans, kNoTrans, r, r, kb, Akk + kb, lda, A12, lda, nslices, &plan, st);
+    const int tnext = (r > NB2 ? NB2 : r) / kSplitTileN + ((r > NB2 ? NB2 : r) % kSplitTileN ? 1 : 0);
+    dev_dgemm_split_run(plan, 0, tnext, -1.0, 1.0, A22, lda, st);
+    const int tall = (r + kSplitTileN - 1) / kSplitTileN;
+    if (tnext < tall) {
+      ATLG_CHECK(cudaEventRecord(ev_ready, st));
+      ATLG_CHECK(cudaStreamWaitEvent(outer, ev_ready, 0));
+      dev_dgemm_split_run(plan, tnext, tall, -1.0, 1.0, A22, lda, outer);
+      ATLG_CHECK(cudaEventRecord(ev_done, outer));
+      outer_pending = true;
+    }
   }
+  if (outer_pending) ATLG_CHECK(cudaStreamWaitEvent(st, ev_done, 0));
   return info;
 }
 

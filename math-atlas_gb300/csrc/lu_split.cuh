@@ -6,8 +6,10 @@ namespace atlg {
 
 // Column-major n x n partial-pivoting LU in place (0-based absolute pivots);
 // returns 0 or the 1-based index of the first zero pivot.  nslices: 7-bit
-// slices per operand of the split products (8 for FP64 accuracy).
-// Synchronizes once per 512 columns (the block column's info).
-int dev_dgetrf_split(int n, double *A, int lda, int *ipiv, int nslices, cudaStream_t st);
+// slices per operand of the split products (8 for FP64 accuracy); nb: the
+// outer block width (rounded down to a multiple of 256; the K of the split
+// products).
+// Synchronizes once per outer block (the block column's info).
+int dev_dgetrf_split(int n, double *A, int lda, int *ipiv, int nslices, int nb, cudaStream_t st);
 
 }  // namespace atlg

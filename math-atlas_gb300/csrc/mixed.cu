@@ -227,7 +227,7 @@ int dev_dgesv_mixed(int n, int nrhs, double *A, int lda, int *ipiv, const double
     copy_d_kernel<<<grid_for((long)n * n), 256, 0, st>>>(n, n, A, lda, F, ldf);
     note_launch();
     // FP64-accurate LU with its O(n^3) updates on the tensor pipe (lu_split.cu)
-    const int i64 = dev_dgetrf_split(n, F, ldf, ipiv, 8, st);
+    const int i64 = dev_dgetrf_split(n, F, ldf, ipiv, 8, 1024, st);
     if (i64 != 0) {
       res->status = 2;
       copy_d_kernel<<<grid_for((long)n * n), 256, 0, st>>>(n, n, F, ldf, A, lda);

@@ -128,13 +128,6 @@ __global__ void __launch_bounds__(256) slice_kernel(int R, int Kd, int Rp, int K
 }
 
 // ------------------------------------------------------------ tensor cores
-struct SplitArgs {
-  int M, N, Mp, Np, Kp, s;
-  double alpha, beta;
-  double *C;
-  int ldc;
-  const int *exA, *exB;
-};
 
 __device__ __forceinline__ bool wait_or_abort(uint64_t *bar, unsigned parity, volatile int *abort_flag) {
   for (unsigned i = 0; i < kMbarPollLimit; ++i) {
@@ -162,7 +155,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1)
   __shared__ double colscale[TN];
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * TM, n0 = blockIdx.y * TN;
+  const int m0 = blockIdx.x * TM, n0 = (blockIdx.y + p.nt0) * TN;
   const int nkb = p.Kp / KB;
   const int nchunk = (nkb + KCHUNK_BLOCKS - 1) / KCHUNK_BLOCKS;
 
@@ -312,8 +305,10 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1)
 // ---------------------------------------------------------------- host side
 static int ceil_to(int x, int m) { return (x + m - 1) / m * m; }
 
-static void split_one(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda, const double *B,
-                      int ldb, double beta, double *C, int ldc, int s, cudaStream_t st) {
+// Exponents and slices of both operands (into the split slots) and the
+// tensor maps over them; K <= 16384 (one exact int32 accumulation).
+void dev_dgemm_split_prepare(int TA, int TB, int M, int N, int K, const double *A, int lda, const double *B, int ldb,
+                             int s, SplitPlan *plan, cudaStream_t st) {
   Context &c = ctx();
   const int Mp = ceil_to(M, TM), Np = ceil_to(N, TN), Kp = ceil_to(K, KB);
   __half *As = static_cast<__half *>(c.buffer(kBufS0, sizeof(__half) * (size_t)s * Mp * Kp));
@@ -329,21 +324,38 @@ static void split_one(int TA, int TB, int M, int N, int K, double alpha, const d
   slice_kernel<<<dim3(Kp / 32, Mp / 32), 256, 0, st>>>(M, K, Mp, Kp, s, A, ars, aks, exA, As);
   slice_kernel<<<dim3(Kp / 32, Np / 32), 256, 0, st>>>(N, K, Np, Kp, s, B, brs, bks, exB, Bs);
   note_launch(4);
-  CUtensorMap tA, tB;
-  if (!encode_tmap_2d(&tA, As, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, Kp, (uint64_t)s * Mp, Kp, KB, TM,
+  if (!encode_tmap_2d(&plan->tA, As, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, Kp, (uint64_t)s * Mp, Kp, KB, TM,
                       CU_TENSOR_MAP_SWIZZLE_128B) ||
-      !encode_tmap_2d(&tB, Bs, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, Kp, (uint64_t)s * Np, Kp, KB, TN,
+      !encode_tmap_2d(&plan->tB, Bs, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, Kp, (uint64_t)s * Np, Kp, KB, TN,
                       CU_TENSOR_MAP_SWIZZLE_128B)) {
     fprintf(stderr, "atlas_gb300: split dgemm: tensor map encoding failed\n");
     abort();
   }
-  SplitArgs a;
-  a.M = M; a.N = N; a.Mp = Mp; a.Np = Np; a.Kp = Kp; a.s = s;
-  a.alpha = alpha; a.beta = beta; a.C = C; a.ldc = ldc; a.exA = exA; a.exB = exB;
+  SplitArgs &a = plan->a;
+  a.M = M; a.N = N; a.Mp = Mp; a.Np = Np; a.Kp = Kp; a.s = s; a.nt0 = 0;
+  a.exA = exA; a.exB = exB;
+}
+
+// C[:, col range] = alpha*op(A)op(B) + beta*C for the output column tiles
+// [t0, t1) of a prepared product (tiles of 256 columns; t1 clipped).
+void dev_dgemm_split_run(const SplitPlan &plan, int t0, int t1, double alpha, double beta, double *C, int ldc,
+                         cudaStream_t st) {
+  const int nt = plan.a.Np / TN;
+  if (t1 > nt) t1 = nt;
+  if (t0 >= t1) return;
+  SplitArgs a = plan.a;
+  a.alpha = alpha; a.beta = beta; a.C = C; a.ldc = ldc; a.nt0 = t0;
   ATLG_CHECK(cudaFuncSetAttribute(ozaki_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPLIT_SMEM));
-  ozaki_tc_kernel<<<dim3(Mp / TM, Np / TN), SPLIT_THREADS, SPLIT_SMEM, st>>>(tA, tB, a);
+  ozaki_tc_kernel<<<dim3(a.Mp / TM, t1 - t0), SPLIT_THREADS, SPLIT_SMEM, st>>>(plan.tA, plan.tB, a);
   note_launch();
   ATLG_CHECK(cudaGetLastError());
+}
+
+static void split_one(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda, const double *B,
+                      int ldb, double beta, double *C, int ldc, int s, cudaStream_t st) {
+  SplitPlan plan;
+  dev_dgemm_split_prepare(TA, TB, M, N, K, A, lda, B, ldb, s, &plan, st);
+  dev_dgemm_split_run(plan, 0, plan.a.Np / TN, alpha, beta, C, ldc, st);
 }
 
 void dev_dgemm_split(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda, const double *B,

@@ -1,5 +1,6 @@
 // split.cuh -- split-precision (integer-slice, tensor-core) DGEMM.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace atlg {
@@ -8,6 +9,27 @@ namespace atlg {
 // from `nslices` (1..8) 7-bit slices per operand on tcgen05 tensor cores.
 void dev_dgemm_split(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda, const double *B,
                      int ldb, double beta, double *C, int ldc, int nslices, cudaStream_t st);
+// The same product in two steps, so one slicing can feed launches on several
+// streams: prepare slices both operands (K <= 16384) into the library's split
+// slots (one prepared product at a time); run computes the output column
+// tiles [t0, t1) (256 columns each).
+struct SplitArgs {
+  int M, N, Mp, Np, Kp, s;
+  int nt0;                 // first output column tile of a launch
+  double alpha, beta;
+  double *C;
+  int ldc;
+  const int *exA, *exB;
+};
+struct SplitPlan {
+  CUtensorMap tA, tB;
+  SplitArgs a;
+};
+constexpr int kSplitTileN = 256;
+void dev_dgemm_split_prepare(int TA, int TB, int M, int N, int K, const double *A, int lda, const double *B, int ldb,
+                             int s, SplitPlan *plan, cudaStream_t st);
+void dev_dgemm_split_run(const SplitPlan &plan, int t0, int t1, double alpha, double beta, double *C, int ldc,
+                         cudaStream_t st);
 unsigned split_status_read_and_clear();
 
 }  // namespace atlg
