@@ -240,6 +240,9 @@ int atlg_dlaswp_noalloc(int N, double *A, int lda, int K1, int K2, const int *ip
  * block cluster's shared memory with the cluster kernel, 0 always uses the
  * cooperative-grid kernel; both give bit-identical factors and pivots */
 void atlg_panel_cluster(int on);
+/* CTAs of the cooperative-grid LU panel (0: the default, a quarter of the SMs
+ * when the factorization overlaps its updates); results do not depend on it */
+void atlg_panel_grid(int ctas);
 /* column-major LU; info written to device memory */
 int atlg_dgetrf_dev(int M, int N, double *A, int lda, int *ipiv, int *info, void *stream);
 int atlg_sgetrf_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void *stream);

@@ -1101,6 +1101,7 @@ int atlg_dlaswp_dev(int N, double *A, int lda, int K1, int K2, const int *ipiv, 
   return 0;
 }
 void atlg_panel_cluster(int on) { set_panel_cluster(on != 0); }
+void atlg_panel_grid(int ctas) { set_panel_grid(ctas); }
 int atlg_dgetrf_dev(int M, int N, double *A, int lda, int *ipiv, int *info, void *stream) {
   if (M < 0 || N < 0 || lda < (M > 1 ? M : 1)) return -1;
   dev_dgetrf(M, N, A, lda, ipiv, info, stream_of(stream));

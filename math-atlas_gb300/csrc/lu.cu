@@ -845,6 +845,8 @@ static int cluster_panel_size() {
 }
 
 void set_panel_cluster(bool on) { g_panel_cluster = on; }
+static int g_panel_grid = 0;   // CTAs of the grid panel; 0: the default below
+void set_panel_grid(int ctas) { g_panel_grid = ctas > 0 ? ctas : 0; }
 
 template <typename T>
 static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaStream_t st, bool tc = false) {
@@ -865,6 +867,7 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     while (G < c.num_sms && ((size_t)((M + G - 1) / G) * NB * sizeof(T)) > kPanelSmemMax) G += 1;
     (void)need;
   }
+  if (g_panel_grid > 0) G = g_panel_grid < c.num_sms ? g_panel_grid : c.num_sms;
   // at least a few rows per CTA for the tallest panel
   if (G > (M + 7) / 8) G = (M + 7) / 8;
   if (G < 1) G = 1;

@@ -7,6 +7,9 @@ namespace atlg {
 // false forces the cooperative-grid panel (the cluster panel is the default
 // where the panel fits one cluster's shared memory); results are identical.
 void set_panel_cluster(bool on);
+// CTAs of the cooperative-grid panel (0: a quarter of the SMs with look-ahead,
+// more when the row slices would not fit shared memory).
+void set_panel_grid(int ctas);
 
 // Column-major LU with partial pivoting of the M x N matrix A (device).
 // ipiv (device, min(M,N) ints, 0-based, global row indices) and info

@@ -8,7 +8,8 @@
 // Outer blocks of nb columns (a multiple of 256; 1024 by default), right-
 // looking, with look-ahead:
 //  1. the (n-k) x nb block column is factored by the FP64 LU (lu.cu: 64-wide
-//     panels, look-ahead, DFMA updates inside the block column);
+//     panels, look-ahead, DFMA updates inside the block column; wider than
+//     1024 columns, by this same method with 1024-column blocks);
 //  2. its interchanges are applied to the columns left and right of it;
 //  3. U12 = L11^-1 A12 as inv(L11) (unit lower, trtri in FP64) times A12 on
 //     the split DGEMM;
@@ -43,24 +44,40 @@ __global__ void unit_lower_kernel(int kb, const double *A, int lda, double *W, i
     if (i < kb) W[i + (size_t)j * ldw] = (i > j) ? A[i + (size_t)j * lda] : (i == j ? 1.0 : 0.0);
 }
 
-int dev_dgetrf_split(int n, double *A, int lda, int *ipiv, int nslices, int nb, cudaStream_t st) {
-  if (n <= 0) return 0;
-  const int NB2 = (nb >= kSplitTileN) ? (nb / kSplitTileN) * kSplitTileN : 512;
+// Widest block column handed to the FP64 LU; wider ones are factored
+// recursively with blocks of this width.  Measured at n=16384 (outer 1024):
+// leaves of 256 (K = 256 split products on narrow outputs) are slower than
+// DFMA updates inside a 1024-wide leaf (530 vs 482 ms).
+constexpr int kInnerNb = 1024;
+
+// M x N (M >= N) partial-pivoting LU of A in place; pivots relative to row 0
+// of A; returns 0 or the first zero pivot (1-based).  Outer blocks of nb
+// columns; a block column wider than kInnerNb is itself factored by this
+// routine with kInnerNb blocks (no look-ahead there), a narrower one by the
+// FP64 LU.  With lookahead, each trailing update is sliced once into the
+// second slot set, its first block of columns is computed on st and the rest
+// on the library's outer stream, overlapping the next block column.
+static int split_lu(int M, int N, double *A, int lda, int *ipiv, int nslices, int nb, bool lookahead,
+                    cudaStream_t st) {
   Context &c = ctx();
+  const int NB2 = (nb >= kSplitTileN) ? (nb / kSplitTileN) * kSplitTileN : kInnerNb;
   int *dinfo = static_cast<int *>(c.buffer(kBufX2, 64));
   cudaStream_t outer = c.outer_stream();
   cudaEvent_t ev_ready = c.sync_event(2), ev_done = c.sync_event(3);
   bool outer_pending = false;
   int info = 0;
-  for (int k = 0; k < n; k += NB2) {
-    const int kb = (n - k < NB2) ? n - k : NB2;
-    const int m = n - k, r = n - k - kb;
+  for (int k = 0; k < N; k += NB2) {
+    const int kb = (N - k < NB2) ? N - k : NB2;
+    const int m = M - k, r = N - k - kb;
     double *Akk = A + k + (size_t)k * lda;
-    // the block column was brought up to date by the previous step's first
-    // update; the rest of that update may still run on the outer stream
-    dev_dgetrf(m, kb, Akk, lda, ipiv + k, dinfo, st);   // pivots relative to row k
-    int hinfo = 0;
-    ATLG_CHECK(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+    int binfo = 0;
+    bool leaf = kb <= kInnerNb;
+    if (!leaf) {
+      binfo = split_lu(m, kb, Akk, lda, ipiv + k, nslices, kInnerNb, false, st);   // relative to row k
+    } else {
+      dev_dgetrf(m, kb, Akk, lda, ipiv + k, dinfo, st);                       // relative to row k
+      ATLG_CHECK(cudaMemcpyAsync(&binfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+    }
     if (outer_pending) {   // the interchanges touch every column
       ATLG_CHECK(cudaStreamWaitEvent(st, ev_done, 0));
       outer_pending = false;
@@ -71,8 +88,8 @@ int dev_dgetrf_split(int n, double *A, int lda, int *ipiv, int nslices, int nb, 
     add_offset_kernel<<<(kb + 255) / 256, 256, 0, st>>>(ipiv + k, kb, k);
     note_launch();
     ATLG_CHECK(cudaGetLastError());
-    ATLG_CHECK(cudaStreamSynchronize(st));
-    if (hinfo > 0 && info == 0) info = k + hinfo;
+    if (leaf) ATLG_CHECK(cudaStreamSynchronize(st));   // binfo has arrived
+    if (binfo > 0 && info == 0) info = k + binfo;
     if (r <= 0) continue;
     double *A12 = A + k + (size_t)(k + kb) * lda;
     double *A22 = A + (k + kb) + (size_t)(k + kb) * lda;
@@ -87,11 +104,15 @@ int dev_dgetrf_split(int n, double *A, int lda, int *ipiv, int nslices, int nb, 
     dev_dgemm_split(kNoTrans, kNoTrans, kb, r, kb, 1.0, W, ldw, A12, lda, 0.0, T, ldw, nslices, st);
     ATLG_CHECK(cudaMemcpy2DAsync(A12, sizeof(double) * lda, T, sizeof(double) * ldw, sizeof(double) * kb, r,
                                  cudaMemcpyDeviceToDevice, st));
-    // A22 -= L21 U12 from one slicing: the next block column first (so the
-    // next factorization can start), the rest on the outer stream
+    // A22 -= L21 U12
+    if (!lookahead) {
+      dev_dgemm_split(kNoTrans, kNoTrans, m - kb, r, kb, -1.0, Akk + kb, lda, A12, lda, 1.0, A22, lda, nslices, st);
+      continue;
+    }
     SplitPlan plan;
-    dev_dgemm_split_prepare(kNoTrans, kNoTrans, r, r, kb, Akk + kb, lda, A12, lda, nslices, &plan, st);
-    const int tnext = (r > NB2 ? NB2 : r) / kSplitTileN + ((r > NB2 ? NB2 : r) % kSplitTileN ? 1 : 0);
+    dev_dgemm_split_prepare(kNoTrans, kNoTrans, m - kb, r, kb, Akk + kb, lda, A12, lda, nslices, &plan, st, 1);
+    const int first = r < NB2 ? r : NB2;
+    const int tnext = (first + kSplitTileN - 1) / kSplitTileN;
     dev_dgemm_split_run(plan, 0, tnext, -1.0, 1.0, A22, lda, st);
     const int tall = (r + kSplitTileN - 1) / kSplitTileN;
     if (tnext < tall) {
@@ -104,6 +125,11 @@ int dev_dgetrf_split(int n, double *A, int lda, int *ipiv, int nslices, int nb, 
   }
   if (outer_pending) ATLG_CHECK(cudaStreamWaitEvent(st, ev_done, 0));
   return info;
+}
+
+int dev_dgetrf_split(int n, double *A, int lda, int *ipiv, int nslices, int nb, cudaStream_t st) {
+  if (n <= 0) return 0;
+  return split_lu(n, n, A, lda, ipiv, nslices, nb, true, st);
 }
 
 }  // namespace atlg

@@ -308,12 +308,13 @@ static int ceil_to(int x, int m) { return (x + m - 1) / m * m; }
 // Exponents and slices of both operands (into the split slots) and the
 // tensor maps over them; K <= 16384 (one exact int32 accumulation).
 void dev_dgemm_split_prepare(int TA, int TB, int M, int N, int K, const double *A, int lda, const double *B, int ldb,
-                             int s, SplitPlan *plan, cudaStream_t st) {
+                             int s, SplitPlan *plan, cudaStream_t st, int slot_set) {
   Context &c = ctx();
   const int Mp = ceil_to(M, TM), Np = ceil_to(N, TN), Kp = ceil_to(K, KB);
-  __half *As = static_cast<__half *>(c.buffer(kBufS0, sizeof(__half) * (size_t)s * Mp * Kp));
-  __half *Bs = static_cast<__half *>(c.buffer(kBufS1, sizeof(__half) * (size_t)s * Np * Kp));
-  int *ex = static_cast<int *>(c.buffer(kBufS2, sizeof(int) * (size_t)(Mp + Np)));
+  const int sa = slot_set ? kBufS3 : kBufS0, sb = slot_set ? kBufS4 : kBufS1, se = slot_set ? kBufS5 : kBufS2;
+  __half *As = static_cast<__half *>(c.buffer(sa, sizeof(__half) * (size_t)s * Mp * Kp));
+  __half *Bs = static_cast<__half *>(c.buffer(sb, sizeof(__half) * (size_t)s * Np * Kp));
+  int *ex = static_cast<int *>(c.buffer(se, sizeof(int) * (size_t)(Mp + Np)));
   int *exA = ex, *exB = ex + Mp;
   // op(A)(i,k): TA==N -> A[i + k lda];  TA==T -> A[k + i lda]
   const long ars = (TA == kNoTrans) ? 1 : lda, aks = (TA == kNoTrans) ? lda : 1;

@@ -10,9 +10,10 @@ namespace atlg {
 void dev_dgemm_split(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda, const double *B,
                      int ldb, double beta, double *C, int ldc, int nslices, cudaStream_t st);
 // The same product in two steps, so one slicing can feed launches on several
-// streams: prepare slices both operands (K <= 16384) into the library's split
-// slots (one prepared product at a time); run computes the output column
-// tiles [t0, t1) (256 columns each).
+// streams: prepare slices both operands (K <= 16384) into one of two sets of
+// the library's split slots (one prepared product per set at a time; set 0
+// is also the one dev_dgemm_split uses); run computes the output column tiles
+// [t0, t1) (256 columns each).
 struct SplitArgs {
   int M, N, Mp, Np, Kp, s;
   int nt0;                 // first output column tile of a launch
@@ -27,7 +28,7 @@ struct SplitPlan {
 };
 constexpr int kSplitTileN = 256;
 void dev_dgemm_split_prepare(int TA, int TB, int M, int N, int K, const double *A, int lda, const double *B, int ldb,
-                             int s, SplitPlan *plan, cudaStream_t st);
+                             int s, SplitPlan *plan, cudaStream_t st, int slot_set = 0);
 void dev_dgemm_split_run(const SplitPlan &plan, int t0, int t1, double alpha, double beta, double *C, int ldc,
                          cudaStream_t st);
 unsigned split_status_read_and_clear();
