@@ -587,18 +587,23 @@ def run_case(args):
     g = torch.Generator(device="cuda").manual_seed(1)
     ms = None
     if args.case == "split":
-        A = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g)
-        B = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g)
+        # n x n x k product (k defaults to n); with --k the LU trailing-update
+        # form C -= A B (beta = 1, 8 slices)
+        k = args.k or n
+        A = torch.randn(n, k, device="cuda", dtype=torch.float64, generator=g)
+        B = torch.randn(k, n, device="cuda", dtype=torch.float64, generator=g)
         Cm = torch.zeros(n, n, device="cuda", dtype=torch.float64)
+        alpha, beta, ns = (-1.0, 1.0, 8) if args.k else (1.0, 0.0, 7)
         torch.cuda.synchronize()
-        for _ in range(2):
+        for _ in range(3):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(s)
-            L.atlg_dgemm_split_dev(111, 111, n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0, Cm.data_ptr(), n,
-                                   7, st)
+            L.atlg_dgemm_split_dev(111, 111, n, n, k, alpha, A.data_ptr(), n, B.data_ptr(), k, beta,
+                                   Cm.data_ptr(), n, ns, st)
             e1.record(s)
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1)
+        print(json.dumps({"case": "split", "n": n, "k": k, "ms": ms, "tflops_fp64_equiv": 2.0 * n * n * k / ms / 1e9}))
     elif args.case == "sgetrf":
         S = torch.randn(n, n, device="cuda", dtype=torch.float32, generator=g)
         piv = torch.zeros(n, dtype=torch.int32, device="cuda")
@@ -610,7 +615,28 @@ def run_case(args):
         e1.record(s)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
+    elif args.case == "dgetrf":
+        if args.pw:
+            L.atlg_panel_width(args.pw)
+        A0 = torch.rand(n, n, device="cuda", dtype=torch.float64, generator=g) - 0.5
+        A = torch.empty_like(A0)
+        piv = torch.zeros(n, dtype=torch.int32, device="cuda")
+        inf = torch.zeros(4, dtype=torch.int32, device="cuda")
+        for _ in range(2):
+            A.copy_(A0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            L.atlg_dgetrf_dev(n, n, C.c_void_p(A.data_ptr()), n, C.c_void_p(piv.data_ptr()),
+                              C.c_void_p(inf.data_ptr()), st)
+            e1.record(s)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
     elif args.case == "splitlu":
+        if args.leaf:
+            L.atlg_split_lu_leaf(args.leaf)
+        if args.pw:
+            L.atlg_panel_width(args.pw)
         A0 = torch.rand(n, n, device="cuda", dtype=torch.float64, generator=g) - 0.5
         A = torch.empty_like(A0)
         piv = torch.zeros(n, dtype=torch.int32, device="cuda")
@@ -685,8 +711,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=8192)
+    ap.add_argument("--k", type=int, default=0, help="inner dimension of --case split (0: n)")
+    ap.add_argument("--leaf", type=int, default=0, help="FP64 leaf width of --case splitlu (0: default)")
+    ap.add_argument("--pw", type=int, default=0, help="FP64 LU panel width for --case splitlu/dgetrf (0: default)")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
-    ap.add_argument("--case", choices=["split", "sgetrf", "mixed", "potrf", "trmm", "getri", "splitlu"], default=None,
+    ap.add_argument("--case", choices=["split", "sgetrf", "dgetrf", "mixed", "potrf", "trmm", "getri", "splitlu"], default=None,
                     help="run one kernel workload for a profiling capture instead of the benchmark")
     ap.add_argument("--skip-extras", action="store_true",
                     help="omit the n=16384 mixed-dgesv and split-DGEMM measurements")

@@ -243,6 +243,10 @@ void atlg_panel_cluster(int on);
 /* CTAs of the cooperative-grid LU panel (0: the default, a quarter of the SMs
  * when the factorization overlaps its updates); results do not depend on it */
 void atlg_panel_grid(int ctas);
+/* panel width of the FP64 LU (8..64, rounded down to a multiple of 8; other
+ * values: the default); pivots and factors agree with the default to
+ * rounding */
+void atlg_panel_width(int w);
 /* column-major LU; info written to device memory */
 int atlg_dgetrf_dev(int M, int N, double *A, int lda, int *ipiv, int *info, void *stream);
 int atlg_sgetrf_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void *stream);
@@ -251,6 +255,10 @@ int atlg_sgetrf_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void 
  * returns info; synchronizes once per outer block */
 int atlg_dgetrf_split_dev(int N, double *A, int lda, int *ipiv, int nslices, int nb,
                           void *stream);
+/* widest block column the split LU hands to the FP64 LU (rounded down to a
+ * multiple of 256; 0: the default 1024); narrower leaves move more of the
+ * block column's own updates onto split products */
+void atlg_split_lu_leaf(int nb);
 int atlg_dgetrs_dev(int Order, int Trans, int N, int NRHS, const double *A, int lda,
                     const int *ipiv, double *B, int ldb, void *stream);
 /* column-major SYRK / Cholesky on device data (Uplo, Trans, Order take the

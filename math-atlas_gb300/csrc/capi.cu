@@ -1102,6 +1102,8 @@ int atlg_dlaswp_dev(int N, double *A, int lda, int K1, int K2, const int *ipiv, 
 }
 void atlg_panel_cluster(int on) { set_panel_cluster(on != 0); }
 void atlg_panel_grid(int ctas) { set_panel_grid(ctas); }
+void atlg_split_lu_leaf(int nb) { set_split_lu_leaf(nb); }
+void atlg_panel_width(int w) { set_panel_width_f64(w); }
 int atlg_dgetrf_dev(int M, int N, double *A, int lda, int *ipiv, int *info, void *stream) {
   if (M < 0 || N < 0 || lda < (M > 1 ? M : 1)) return -1;
   dev_dgetrf(M, N, A, lda, ipiv, info, stream_of(stream));

@@ -99,6 +99,9 @@ __device__ __forceinline__ void tma_load_2d(void *smem_dst, const CUtensorMap *m
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap *map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
+// *p += v in L2 (round to nearest), no value returned: the issuing thread
+// does not wait for it.
+__device__ __forceinline__ void red_add_f64(double *p, double v) { (void)atomicAdd(p, v); }
 
 // cp.async with zero fill: copies `src_bytes` (0 or the full size) and
 // fills the rest of the destination with zeros.

@@ -52,31 +52,56 @@ template <typename T> struct Lim;
 template <> struct Lim<double> { __device__ static double safmin() { return DBL_MIN; } };
 template <> struct Lim<float>  { __device__ static float safmin() { return FLT_MIN; } };
 
-template <typename T>
+// Pivot search on integer keys.  For x not NaN, the bit pattern of |x| read
+// as a signed integer orders exactly as |x| does; NaN maps to -1, below every
+// candidate, so it never wins (as `|x| > best` never holds for NaN).  GB300
+// runs FP64 compares on its narrow FP64 pipe, so the reductions of the
+// search compare keys on the integer pipe instead; the winner is the same.
+template <typename T> struct PivKey;
+template <> struct PivKey<double> {
+  using K = long long;
+  __device__ static K key(double x) {
+    const K b = __double_as_longlong(x) & 0x7fffffffffffffffLL;
+    return b > 0x7ff0000000000000LL ? K(-1) : b;
+  }
+  __device__ static double as_t(K k) { return __longlong_as_double(k); }
+  __device__ static K from_t(double v) { return __double_as_longlong(v); }
+};
+template <> struct PivKey<float> {
+  using K = int;
+  __device__ static K key(float x) {
+    const K b = __float_as_int(x) & 0x7fffffff;
+    return b > 0x7f800000 ? K(-1) : b;
+  }
+  __device__ static float as_t(K k) { return __int_as_float(k); }
+  __device__ static K from_t(float v) { return __float_as_int(v); }
+};
+
+template <typename K>
 struct BlockArgmax {
-  T v[PT / 32];
+  K v[PT / 32];
   int i[PT / 32];
 };
 
-// first-max reduction over the block: (val, idx) with larger val winning,
-// lower idx winning ties; val < 0 marks "no candidate".
-template <typename T>
-__device__ void block_argmax(T &val, int &idx, BlockArgmax<T> &sh) {
+// first-max reduction over the block: (key, idx) with the larger key
+// winning, lower idx winning ties; key < 0 marks "no candidate".
+template <typename K>
+__device__ void block_argmax(K &val, int &idx, BlockArgmax<K> &sh) {
   for (int o = 16; o > 0; o >>= 1) {
-    const T ov = __shfl_down_sync(0xffffffffu, val, o);
+    const K ov = __shfl_down_sync(0xffffffffu, val, o);
     const int oi = __shfl_down_sync(0xffffffffu, idx, o);
-    if (ov > val || (ov == val && oi < idx && ov >= T(0))) { val = ov; idx = oi; }
+    if (ov > val || (ov == val && oi < idx && ov >= K(0))) { val = ov; idx = oi; }
   }
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (lane == 0) { sh.v[w] = val; sh.i[w] = idx; }
   __syncthreads();
   if (w == 0) {
-    val = lane < PT / 32 ? sh.v[lane] : T(-1);
+    val = lane < PT / 32 ? sh.v[lane] : K(-1);
     idx = lane < PT / 32 ? sh.i[lane] : 0x7fffffff;
     for (int o = 16; o > 0; o >>= 1) {
-      const T ov = __shfl_down_sync(0xffffffffu, val, o);
+      const K ov = __shfl_down_sync(0xffffffffu, val, o);
       const int oi = __shfl_down_sync(0xffffffffu, idx, o);
-      if (ov > val || (ov == val && oi < idx && ov >= T(0))) { val = ov; idx = oi; }
+      if (ov > val || (ov == val && oi < idx && ov >= K(0))) { val = ov; idx = oi; }
     }
   }
   __syncthreads();
@@ -101,31 +126,32 @@ struct PanelRows {
 // Other CTAs write them between grid barriers, so every read after a barrier
 // goes to L2 (__ldcg): an L1 line from the same buffer two columns earlier
 // would otherwise be stale.
-// rec[(par*G + b)*RS + c] holds CTA b's candidate row (c < NB), then its
-// |a| (c = NB, negative: no candidate) and its row index (c = NB+1, exact in
-// T for any matrix this library can hold).  One record per CTA, so a
+// rec[(par*G + b)*RS + c] holds CTA b's candidate row (c < NB), then the
+// pivot key of its |a| (c = NB, its bits stored in a T; negative: no
+// candidate) and its row index (c = NB+1, exact in T for any matrix this
+// library can hold).  One record per CTA, so a
 // reader gets value, index and row of every candidate from one place.
 template <typename T> __host__ __device__ constexpr int rec_stride() { return sizeof(T) == 8 ? NB + 2 : NB + 4; }
 
 // Local candidate for column j among own rows [max(r0,j), r1); stage it.
 template <typename T, bool SM>
 __device__ void stage_candidate(const PanelRows<T, SM> &A, int j, int jb, int r0, int r1, int par, int G, T *rec,
-                                T *jrow, BlockArgmax<T> &sh, int *s_idx) {
+                                T *jrow, BlockArgmax<typename PivKey<T>::K> &sh, int *s_idx) {
+  using K = typename PivKey<T>::K;
   constexpr int RS = rec_stride<T>();
-  T best = T(-1);
+  K best = K(-1);
   int bi = 0x7fffffff;
   const int lo = r0 > j ? r0 : j;
   for (int i = lo + threadIdx.x; i < r1; i += PT) {      // ascending rows per thread
-    T a = A.at(i, j);
-    a = a < T(0) ? -a : a;
+    const K a = PivKey<T>::key(A.at(i, j));
     if (a > best) { best = a; bi = i; }
   }
   block_argmax(best, bi, sh);
   T *r = rec + ((size_t)par * G + blockIdx.x) * RS;
   if (threadIdx.x == 0) {
-    r[NB] = best;
-    r[NB + 1] = best >= T(0) ? (T)bi : T(-1);
-    *s_idx = best >= T(0) ? bi : -1;
+    r[NB] = PivKey<T>::as_t(best);
+    r[NB + 1] = best >= K(0) ? (T)bi : T(-1);
+    *s_idx = best >= K(0) ? bi : -1;
   }
   __syncthreads();
   const int ci = *s_idx;
@@ -184,11 +210,12 @@ template <typename T, bool SM>
 __global__ void __launch_bounds__(PT)
     panel_kernel(T *Ag, int lda, int M, int jb, int koff, int *ipiv, int *info, T *rec, T *jrow, unsigned *bar,
                  int *perm) {
+  using K = typename PivKey<T>::K;
   extern __shared__ __align__(16) unsigned char panel_dyn[];
-  __shared__ BlockArgmax<T> sh;
+  __shared__ BlockArgmax<K> sh;
   __shared__ T P[NB], J[NB];
-  __shared__ int s_idx, s_p, s_zero;
-  __shared__ T s_piv, s_rcp;
+  __shared__ int s_idx, s_p, s_zero, s_use_rcp;
+  __shared__ T s_rcp;
   __shared__ int piv_local[NB];
   constexpr int LB = SM ? 1 : 2048;
   __shared__ T lbuf[LB];
@@ -233,23 +260,22 @@ __global__ void __launch_bounds__(PT)
       __syncthreads();
     }
     if (threadIdx.x < 32) {
-      T best = T(-1);
+      K best = K(-1);
       int bb = 0x7fffffff;
       for (int b = threadIdx.x; b < G; b += 32) {
-        const T v = gather_all ? gath[b * RS + NB] : __ldcg(rp + (size_t)b * RS + NB);
+        const K v = PivKey<T>::from_t(gather_all ? gath[b * RS + NB] : __ldcg(rp + (size_t)b * RS + NB));
         if (v > best) { best = v; bb = b; }
       }
       for (int o = 16; o > 0; o >>= 1) {
-        const T ov = __shfl_down_sync(0xffffffffu, best, o);
+        const K ov = __shfl_down_sync(0xffffffffu, best, o);
         const int ob = __shfl_down_sync(0xffffffffu, bb, o);
         if (ov > best || (ov == best && ob < bb)) { best = ov; bb = ob; }
       }
       if (threadIdx.x == 0) {
         int p = -1;
-        if (bb < G && best > T(0)) p = (int)(gather_all ? gath[bb * RS + NB + 1] : __ldcg(rp + (size_t)bb * RS + NB + 1));
+        if (bb < G && best > K(0)) p = (int)(gather_all ? gath[bb * RS + NB + 1] : __ldcg(rp + (size_t)bb * RS + NB + 1));
         s_zero = (p < 0);
         s_p = (p < 0) ? j : p;
-        s_piv = best;
         s_idx = bb;
       }
     }
@@ -270,12 +296,15 @@ __global__ void __launch_bounds__(PT)
           P[c] = __ldcg(rp + (size_t)wb * RS + c);
           J[c] = __ldcg(jrow + par * NB + c);
         }
-        if (c == j) s_rcp = T(1) / P[c];   // once per CTA: FP64 division is costly
+        if (c == j) {   // once per CTA: FP64 division (and compare) is costly
+          const T pj = P[c];
+          s_rcp = T(1) / pj;
+          s_use_rcp = (pj < T(0) ? -pj : pj) > Lim<T>::safmin();
+        }
       }
       __syncthreads();
       const T pv = P[j];
-      const T apv = pv < T(0) ? -pv : pv;
-      const bool use_rcp = apv > Lim<T>::safmin();
+      const bool use_rcp = s_use_rcp != 0;
       const T rcp = s_rcp;
       // pass 1: multipliers (column j) and the two swapped rows' L parts
       const int lo = r0 > j ? r0 : j;
@@ -345,7 +374,7 @@ template <typename T>
 struct ClusterSlots {
   __align__(16) T crow[2][NB];   // own candidate row
   __align__(16) T jrow[2][NB];   // row j, in the CTA that owns it
-  T cval[2][kClusterMax];        // pushed by every CTA: candidate |a| (< 0: none)
+  typename PivKey<T>::K cval[2][kClusterMax];   // pushed by every CTA: key of candidate |a| (< 0: none)
   int cidx[2][kClusterMax];      //                      candidate row
 };
 
@@ -353,11 +382,11 @@ template <typename T> struct Vec16;
 template <> struct Vec16<float> { using type = float4; };
 template <> struct Vec16<double> { using type = double2; };
 
-// (larger |a|, then lower source) wins; every lane ends with the winner
-template <typename T>
-__device__ __forceinline__ void warp_winner(T &v, int &b, int &idx) {
+// (larger key, then lower source) wins; every lane ends with the winner
+template <typename K>
+__device__ __forceinline__ void warp_winner(K &v, int &b, int &idx) {
   for (int o = 16; o > 0; o >>= 1) {
-    const T ov = __shfl_xor_sync(0xffffffffu, v, o);
+    const K ov = __shfl_xor_sync(0xffffffffu, v, o);
     const int ob = __shfl_xor_sync(0xffffffffu, b, o);
     const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
     if (ov > v || (ov == v && ob < b)) { v = ov; b = ob; idx = oi; }
@@ -433,6 +462,7 @@ template <typename T>
 __global__ void __launch_bounds__(CT)
     panel_cluster_kernel(T *Ag, int lda, int M, int jb, int koff, int *ipiv, int *info, int *perm) {
   using V = typename Vec16<T>::type;
+  using K = typename PivKey<T>::K;
   constexpr int VE = 16 / (int)sizeof(T);        // elements per 16-byte vector
   constexpr int NV = NB / VE;                    // vectors per row
   constexpr int RS = cl_rs<T>();
@@ -444,7 +474,8 @@ __global__ void __launch_bounds__(CT)
   __shared__ __align__(16) T Pb[2][NB];
   __shared__ __align__(16) T Jb[2][NB];
   __shared__ T s_rcp[2];
-  __shared__ T wv[NW];
+  __shared__ int s_use_rcp[2];
+  __shared__ K wv[NW];
   __shared__ int wi[NW];
   __shared__ int piv_local[NB];
   cg::cluster_group cluster = cg::this_cluster();
@@ -467,24 +498,24 @@ __global__ void __launch_bounds__(CT)
 
   // Reduce the per-thread candidates (rows ci already complete) to the CTA's
   // first-max; keep its row and row jn locally, push |a| and row to all.
-  auto publish = [&](T best, int bi, int jn) -> int {
+  auto publish = [&](K best, int bi, int jn) -> int {
     for (int o = 16; o > 0; o >>= 1) {
-      const T ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const K ov = __shfl_xor_sync(0xffffffffu, best, o);
       const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ov > best || (ov == best && oi < bi && ov >= T(0))) { best = ov; bi = oi; }
+      if (ov > best || (ov == best && oi < bi && ov >= K(0))) { best = ov; bi = oi; }
     }
     if (lane == 0) { wv[w] = best; wi[w] = bi; }
     __syncthreads();
-    best = lane < NW ? wv[lane] : T(-1);
+    best = lane < NW ? wv[lane] : K(-1);
     bi = lane < NW ? wi[lane] : 0x7fffffff;
     for (int o = 16; o > 0; o >>= 1) {
-      const T ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const K ov = __shfl_xor_sync(0xffffffffu, best, o);
       const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ov > best || (ov == best && oi < bi && ov >= T(0))) { best = ov; bi = oi; }
+      if (ov > best || (ov == best && oi < bi && ov >= K(0))) { best = ov; bi = oi; }
     }
-    return best >= T(0) ? bi : -1;
+    return best >= K(0) ? bi : -1;
   };
-  auto push = [&](T best, int ci, int jn) {
+  auto push = [&](K best, int ci, int jn) {
     const int par = jn & 1;
     if (ci >= 0 && tid < nvj)
       reinterpret_cast<V *>(slot.crow[par])[tid] = reinterpret_cast<const V *>(&AT(ci, 0))[tid];
@@ -498,17 +529,14 @@ __global__ void __launch_bounds__(CT)
   };
 
   {
-    T best = T(-1);
+    K best = K(-1);
     int bi = 0x7fffffff;
     for (int i = r0 + tid; i < r1; i += CT) {
-      T a = AT(i, 0);
-      a = a < T(0) ? -a : a;
+      const K a = PivKey<T>::key(AT(i, 0));
       if (a > best) { best = a; bi = i; }
     }
     const int ci = publish(best, bi, 0);
-    T cv = T(-1);
-    if (ci >= 0) { cv = AT(ci, 0); cv = cv < T(0) ? -cv : cv; }
-    push(cv, ci, 0);
+    push(ci >= 0 ? PivKey<T>::key(AT(ci, 0)) : K(-1), ci, 0);
   }
 
   for (int j = 0; j < jb; ++j) {
@@ -516,11 +544,11 @@ __global__ void __launch_bounds__(CT)
     if (j == 0) cluster.sync();
     else cluster.barrier_wait();
     // ---- global winner, computed by every warp from its own CTA's slots ----
-    T v = T(-1);
+    K v = K(-1);
     int b = 0x7fffffff, idx = -1;
     if (lane < CN) { v = slot.cval[par][lane]; idx = slot.cidx[par][lane]; b = lane; }
     warp_winner(v, b, idx);
-    const bool zero = !(b < CN && v > T(0));
+    const bool zero = !(b < CN && v > K(0));
     const int p = zero ? j : idx;
     if (me == 0 && tid == 0) {
       ipiv[j] = koff + p;
@@ -528,7 +556,7 @@ __global__ void __launch_bounds__(CT)
       if (zero && *info == 0) *info = koff + j + 1;
     }
     const bool last = (j + 1 >= jb);
-    T best = T(-1);
+    K best = K(-1);
     int bi = 0x7fffffff;
     if (!zero) {
       // the winner's row and row j, pulled once per CTA
@@ -545,6 +573,7 @@ __global__ void __launch_bounds__(CT)
             for (int e = 1; e < VE; ++e)
               if (tid * VE + e == j) pj = pe[e];
             s_rcp[par] = T(1) / pj;
+            s_use_rcp[par] = (pj < T(0) ? -pj : pj) > Lim<T>::safmin();
           }
         } else
           reinterpret_cast<V *>(Js)[tid - NV] =
@@ -552,8 +581,7 @@ __global__ void __launch_bounds__(CT)
       }
       __syncthreads();   // also: every thread is done with the previous column's phase 2
       const T pv = Ps[j];
-      const T apv = pv < T(0) ? -pv : pv;
-      const bool use_rcp = apv > Lim<T>::safmin();
+      const bool use_rcp = s_use_rcp[par] != 0;
       const T rcp = s_rcp[par];
       const int lo = r0 > j ? r0 : j;
       // phase 1: multipliers and column j+1 of every own row (rows j and p
@@ -576,8 +604,7 @@ __global__ void __launch_bounds__(CT)
           if (!last) row[j + 1] -= l * Ps[j + 1];
         }
         if (!last) {
-          T a = row[j + 1];
-          a = a < T(0) ? -a : a;
+          const K a = PivKey<T>::key(row[j + 1]);
           if (a > best) { best = a; bi = i; }
         }
       }
@@ -604,9 +631,7 @@ __global__ void __launch_bounds__(CT)
           }
         }
         __syncthreads();
-        T cv = T(-1);
-        if (ci >= 0) { cv = AT(ci, j + 1); cv = cv < T(0) ? -cv : cv; }
-        push(cv, ci, j + 1);
+        push(ci >= 0 ? PivKey<T>::key(AT(ci, j + 1)) : K(-1), ci, j + 1);
         cluster.barrier_arrive();
         // phase 2 (overlaps the barrier): columns j+2.. of the other rows
         if (j + 2 < jb) {
@@ -620,15 +645,12 @@ __global__ void __launch_bounds__(CT)
     } else if (!last) {
       const int lo = r0 > j + 1 ? r0 : j + 1;
       for (int i = lo + tid; i < r1; i += CT) {
-        T a = AT(i, j + 1);
-        a = a < T(0) ? -a : a;
+        const K a = PivKey<T>::key(AT(i, j + 1));
         if (a > best) { best = a; bi = i; }
       }
       const int ci = publish(best, bi, j + 1);
       __syncthreads();
-      T cv = T(-1);
-      if (ci >= 0) { cv = AT(ci, j + 1); cv = cv < T(0) ? -cv : cv; }
-      push(cv, ci, j + 1);
+      push(ci >= 0 ? PivKey<T>::key(AT(ci, j + 1)) : K(-1), ci, j + 1);
       cluster.barrier_arrive();
     }
     if (last) break;
@@ -847,6 +869,12 @@ static int cluster_panel_size() {
 void set_panel_cluster(bool on) { g_panel_cluster = on; }
 static int g_panel_grid = 0;   // CTAs of the grid panel; 0: the default below
 void set_panel_grid(int ctas) { g_panel_grid = ctas > 0 ? ctas : 0; }
+// Panel width of the FP64 LU (8..NB, a multiple of 8).  A panel's own
+// rank-1 updates run on the FP64 pipe of the few SMs the panel occupies
+// (M x w^2 / 2 FMAs per panel); a narrower panel moves that work into the
+// trailing DGEMMs, which use every SM.
+static int g_panel_nb_f64 = NB;
+void set_panel_width_f64(int w) { g_panel_nb_f64 = (w >= 8 && w <= NB) ? w / 8 * 8 : NB; }
 
 template <typename T>
 static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaStream_t st, bool tc = false) {
@@ -854,18 +882,17 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
   if (M <= 0 || N <= 0) return;
   Context &c = ctx();
   const int MN = M < N ? M : N;
+  const int PW = (sizeof(T) == 8) ? g_panel_nb_f64 : NB;   // panel width
   // Look-ahead: the trailing update of step k is split into the next panel's
   // columns (on the caller's stream, so panel k+1 can start at once) and the
   // rest (on a low-priority side stream, overlapping panel k+1).  The panel
   // grid then takes a quarter of the SMs, as few as its shared-memory slices
   // allow, leaving the rest to the concurrent update.
-  const bool lookahead = MN > 2 * NB && N > 2 * NB;
+  const bool lookahead = MN > 2 * PW && N > 2 * PW;
   int G = c.num_sms;
   if (lookahead) {
     G = c.num_sms / 4;
-    const size_t need = (size_t)M * NB * sizeof(T);
-    while (G < c.num_sms && ((size_t)((M + G - 1) / G) * NB * sizeof(T)) > kPanelSmemMax) G += 1;
-    (void)need;
+    while (G < c.num_sms && ((size_t)((M + G - 1) / G) * PW * sizeof(T)) > kPanelSmemMax) G += 1;
   }
   if (g_panel_grid > 0) G = g_panel_grid < c.num_sms ? g_panel_grid : c.num_sms;
   // at least a few rows per CTA for the tallest panel
@@ -888,8 +915,8 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
   const int cn = g_panel_cluster ? cluster_panel_size<T>() : 0;
   bool used_cluster = false;
 
-  for (int k = 0; k < MN; k += NB) {
-    const int jb = (MN - k < NB) ? MN - k : NB;
+  for (int k = 0; k < MN; k += PW) {
+    const int jb = (MN - k < PW) ? MN - k : PW;
     T *Ap = A + k + (size_t)k * lda;
     int Mp = M - k;
     int *ipk = ipiv + k;
@@ -955,7 +982,7 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
           dev_sgemm_tf32x3_pack_a(m, jb, (const float *)L21, lda, Ap, st);
           dev_sgemm_tf32x3_pack_b(jb, ntot, (const float *)U12, lda, Bp, st);
         }
-        const int nxt = (c_from < MN) ? ((MN - c_from < NB) ? MN - c_from : NB) : 0;
+        const int nxt = (c_from < MN) ? ((MN - c_from < PW) ? MN - c_from : PW) : 0;
         if (lookahead && nxt > 0 && c_from + nxt < N) {
           trailing_update<T>(use_tc, m, nxt, jb, L21, U12, C, lda, 0, ntot, Ap, Bp, st);
           ATLG_CHECK(cudaEventRecord(ev_ready, st));

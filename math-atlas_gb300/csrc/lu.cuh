@@ -10,6 +10,7 @@ void set_panel_cluster(bool on);
 // CTAs of the cooperative-grid panel (0: a quarter of the SMs with look-ahead,
 // more when the row slices would not fit shared memory).
 void set_panel_grid(int ctas);
+void set_panel_width_f64(int w);
 
 // Column-major LU with partial pivoting of the M x N matrix A (device).
 // ipiv (device, min(M,N) ints, 0-based, global row indices) and info

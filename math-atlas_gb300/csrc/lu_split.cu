@@ -44,23 +44,22 @@ __global__ void unit_lower_kernel(int kb, const double *A, int lda, double *W, i
     if (i < kb) W[i + (size_t)j * ldw] = (i > j) ? A[i + (size_t)j * lda] : (i == j ? 1.0 : 0.0);
 }
 
-// Widest block column handed to the FP64 LU; wider ones are factored
-// recursively with blocks of this width.  Measured at n=16384 (outer 1024):
-// leaves of 256 (K = 256 split products on narrow outputs) are slower than
-// DFMA updates inside a 1024-wide leaf (530 vs 482 ms).
-constexpr int kInnerNb = 1024;
+// Widest block column handed to the FP64 LU (a multiple of 256); wider ones
+// are factored recursively with blocks of this width.
+static int g_leaf_nb = 1024;
+void set_split_lu_leaf(int nb) { g_leaf_nb = (nb >= kSplitTileN) ? nb / kSplitTileN * kSplitTileN : 1024; }
 
 // M x N (M >= N) partial-pivoting LU of A in place; pivots relative to row 0
 // of A; returns 0 or the first zero pivot (1-based).  Outer blocks of nb
-// columns; a block column wider than kInnerNb is itself factored by this
-// routine with kInnerNb blocks (no look-ahead there), a narrower one by the
+// columns; a block column wider than g_leaf_nb is itself factored by this
+// routine with g_leaf_nb blocks (no look-ahead there), a narrower one by the
 // FP64 LU.  With lookahead, each trailing update is sliced once into the
 // second slot set, its first block of columns is computed on st and the rest
 // on the library's outer stream, overlapping the next block column.
 static int split_lu(int M, int N, double *A, int lda, int *ipiv, int nslices, int nb, bool lookahead,
                     cudaStream_t st) {
   Context &c = ctx();
-  const int NB2 = (nb >= kSplitTileN) ? (nb / kSplitTileN) * kSplitTileN : kInnerNb;
+  const int NB2 = (nb >= kSplitTileN) ? (nb / kSplitTileN) * kSplitTileN : g_leaf_nb;
   int *dinfo = static_cast<int *>(c.buffer(kBufX2, 64));
   cudaStream_t outer = c.outer_stream();
   cudaEvent_t ev_ready = c.sync_event(2), ev_done = c.sync_event(3);
@@ -71,9 +70,9 @@ static int split_lu(int M, int N, double *A, int lda, int *ipiv, int nslices, in
     const int m = M - k, r = N - k - kb;
     double *Akk = A + k + (size_t)k * lda;
     int binfo = 0;
-    bool leaf = kb <= kInnerNb;
+    bool leaf = kb <= g_leaf_nb;
     if (!leaf) {
-      binfo = split_lu(m, kb, Akk, lda, ipiv + k, nslices, kInnerNb, false, st);   // relative to row k
+      binfo = split_lu(m, kb, Akk, lda, ipiv + k, nslices, g_leaf_nb, false, st);   // relative to row k
     } else {
       dev_dgetrf(m, kb, Akk, lda, ipiv + k, dinfo, st);                       // relative to row k
       ATLG_CHECK(cudaMemcpyAsync(&binfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -11,5 +11,8 @@ namespace atlg {
 // products).
 // Synchronizes once per outer block (the block column's info).
 int dev_dgetrf_split(int n, double *A, int lda, int *ipiv, int nslices, int nb, cudaStream_t st);
+// Widest block column factored by the FP64 LU inside the split LU (rounded
+// down to a multiple of 256; below 256: the default 1024).
+void set_split_lu_leaf(int nb);
 
 }  // namespace atlg

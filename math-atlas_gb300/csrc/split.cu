@@ -269,25 +269,41 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1)
           mbar_arrive(&acc_empty[buf]);
         }
       if (!ok) break;
-      // diagonal d complete: C (+)= alpha 2^(ea - 7(d+2)) acc 2^(eb); C is
-      // read in batches of 8 independent loads before any store
+      // diagonal d complete: C (+)= alpha 2^(ea - 7(d+2)) acc 2^(eb).  Every
+      // diagonal after the first (and the first too when beta = 1) is added
+      // with fire-and-forget FP64 reductions in L2: the epilogue does not wait
+      // for C, so the MMAs of the next diagonal keep running.  Each element
+      // belongs to one thread, whose same-address operations stay in program
+      // order, so C sees the same sequence of rounded additions as a
+      // load/add/store would produce.
       const double fr = ldexp(rowpow, rexp - kSliceBits * (d + 2));
-      const bool need_old = !first || p.beta != 0.0;
-      const double cscale = first ? p.beta : 1.0;
+      // mode 0: reduction; 1: plain store (first diagonal, beta = 0);
+      // 2: C = beta C + v with C read in batches of 8 loads before any store
+      const int mode = (!first || p.beta == 1.0) ? 0 : (p.beta == 0.0 ? 1 : 2);
+      const int ncol = row_ok ? p.N - (n0 + h * EPI_COLS) : 0;   // valid columns of this thread
+      const size_t ldc = (size_t)p.ldc;
+      double *cp = p.C + gm + (size_t)(n0 + h * EPI_COLS) * ldc;
+      const double *cs = colscale + h * EPI_COLS;
+      if (mode == 0) {
 #pragma unroll
-      for (int c0 = 0; c0 < EPI_COLS; c0 += 8) {
-        double old[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int gn = n0 + h * EPI_COLS + c0 + j;
-          old[j] = (need_old && row_ok && gn < p.N) ? p.C[gm + (size_t)gn * p.ldc] : 0.0;
+        for (int c = 0; c < EPI_COLS; ++c) {
+          if (c < ncol) red_add_f64(cp, (double)acc[c] * fr * cs[c]);
+          cp += ldc;
+          acc[c] = 0;
         }
+      } else {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int gn = n0 + h * EPI_COLS + c0 + j;
-          const double v = (double)acc[c0 + j] * fr * colscale[h * EPI_COLS + c0 + j];
-          if (row_ok && gn < p.N) p.C[gm + (size_t)gn * p.ldc] = need_old ? fma(cscale, old[j], v) : v;
-          acc[c0 + j] = 0;
+        for (int c0 = 0; c0 < EPI_COLS; c0 += 8) {
+          double old[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) old[j] = (mode == 2 && c0 + j < ncol) ? cp[j * ldc] : 0.0;
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const double v = (double)acc[c0 + j] * fr * cs[c0 + j];
+            if (c0 + j < ncol) cp[j * ldc] = (mode == 2) ? fma(p.beta, old[j], v) : v;
+            acc[c0 + j] = 0;
+          }
+          cp += 8 * ldc;
         }
       }
       first = false;

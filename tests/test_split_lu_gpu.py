@@ -64,3 +64,25 @@ def test_split_lu_zero_pivot_info(gb, ora):
     info = gb.dgesv_split(n, 1, A, n, piv, B, n)
     assert info == 701
     assert (B == 1.0).all()
+
+
+@pytest.mark.parametrize("leaf", [256, 512])
+def test_split_lu_narrow_leaves(gb, ora, leaf):
+    # 1024-wide outer blocks factored recursively with narrower FP64 leaves
+    # (split products inside the block column); same residual bound, and the
+    # zero-pivot info from inside a recursive block
+    lib = gb.lib()
+    lib.atlg_split_lu_leaf(leaf)
+    try:
+        n = 2300
+        A = ora.gegen(n, n, 77)
+        piv = np.zeros(n, dtype=np.int32)
+        B = np.zeros((n, 1), order="F")
+        assert gb.dgesv_split(n, 0, A, n, piv, B, n) == 0
+        assert (piv >= np.arange(n)).all() and (piv < n).all()
+        assert ora.lu_resid(n, n, A, piv, 77) <= 100.0
+        A = ora.gegen(n, n, 78)
+        A[:, 1500] = 0.0
+        assert gb.dgesv_split(n, 0, A, n, piv, B, n) == 1501
+    finally:
+        lib.atlg_split_lu_leaf(0)
