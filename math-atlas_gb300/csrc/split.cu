@@ -58,58 +58,101 @@ constexpr int EPI_WARPS = 16;
 constexpr int SPLIT_THREADS = 64 + EPI_WARPS * 32;             // 2 + 16 warps
 constexpr int EPI_COLS = 64;                                   // columns per epilogue thread
 constexpr int SPLIT_SMEM = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int kRasterN = 8;                                    // column tiles per raster group
 
 // --------------------------------------------------------------- scaling
+// |x| as an integer key: the bit pattern of |x| orders exactly as |x| for x
+// not NaN; NaN maps to 0, so a maximum over keys ignores NaN as fmax does.
+// Integer max/compare keeps the scan off GB300's narrow FP64 pipe.
+__device__ __forceinline__ long long abs_bits(double x) {
+  const long long b = __double_as_longlong(x) & 0x7fffffffffffffffLL;
+  return b > 0x7ff0000000000000LL ? 0LL : b;
+}
+
 // ex[r] = exponent e with max_k |In(r,k)| < 2^e (0 for an all-zero vector);
 // In(r,k) = In[r*rs + k*ks].  Contiguous-in-k vectors: a warp per vector;
 // otherwise 32 consecutive vectors per CTA, 8 warps striding over k.
 __global__ void __launch_bounds__(256) vec_exp_kernel(int R, int Kd, const double *__restrict__ In, long rs, long ks,
                                                       int *__restrict__ ex) {
-  __shared__ double part[8][32];
+  __shared__ long long part[8][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  double m = 0.0;
+  long long m = 0;
   int r;
   if (ks == 1) {
     r = blockIdx.x * 8 + w;
     if (r < R)
-      for (int k = lane; k < Kd; k += 32) m = fmax(m, fabs(In[(size_t)r * rs + k]));
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+      for (int k = lane; k < Kd; k += 32) m = max(m, abs_bits(In[(size_t)r * rs + k]));
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
     if (lane == 0 && r < R) {
       int e = 0;
-      if (m > 0.0) frexp(m, &e);
+      if (m > 0) frexp(__longlong_as_double(m), &e);
       ex[r] = e;
     }
   } else {
     r = blockIdx.x * 32 + lane;
     if (r < R)
-      for (int k = w; k < Kd; k += 8) m = fmax(m, fabs(In[(size_t)r * rs + (size_t)k * ks]));
+      for (int k = w; k < Kd; k += 8) m = max(m, abs_bits(In[(size_t)r * rs + (size_t)k * ks]));
     part[w][lane] = m;
     __syncthreads();
     if (w == 0 && r < R) {
-      double mm = 0.0;
-      for (int q = 0; q < 8; ++q) mm = fmax(mm, part[q][lane]);
+      long long mm = 0;
+      for (int q = 0; q < 8; ++q) mm = max(mm, part[q][lane]);
       int e = 0;
-      if (mm > 0.0) frexp(mm, &e);
+      if (mm > 0) frexp(__longlong_as_double(mm), &e);
       ex[r] = e;
     }
   }
 }
 
 // Digit split of In (R x Kd, strides rs/ks) into s FP16 slices
-// Out[(t*Rp + r)*Kp + k], zero outside R x Kd.  x = In * 2^-e in (-1, 1);
-// digit t = trunc(128 * remainder), exact in binary64.
+// Out[(t*Rp + r)*Kp + k], zero outside R x Kd.  With x = In * 2^-e in
+// (-1, 1), digit t = trunc(128 * remainder_t): the binary fraction of |x| cut
+// into 7-bit groups, with the sign of x.  A finite x is exact in 56 fraction
+// bits of fixed point taken straight from its significand and exponent
+// (integer shifts, no FP64 arithmetic; the FP64 recurrence
+// x *= 128, d = trunc(x), x -= d is exact, so the digits are the same).
+// Values the fixed point cannot hold (NaN, infinity, |x| >= 1 in a vector
+// whose maximum was not finite) take that FP64 recurrence.
+__device__ __forceinline__ void digits_of(double v, int e, int s, __half *h) {
+  const long long b = __double_as_longlong(v);
+  const int ef = (int)((b >> 52) & 0x7ff);
+  const int E = (ef ? ef : 1) - 1075;            // |v| = mant * 2^E
+  const int sh = 56 - (e - E);                   // frac56 = mant * 2^sh
+  if (ef == 0x7ff || (ef != 0 && sh > 3) || sh > 55) {
+    double x = ldexp(v, -e);
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      x *= 128.0;
+      const double d = trunc(x);
+      x -= d;
+      if (t < s) h[t] = __double2half((float)d);
+    }
+    return;
+  }
+  const unsigned long long mant = (unsigned long long)(b & 0xfffffffffffffLL) | (ef ? (1ull << 52) : 0ull);
+  unsigned long long f = 0;
+  if (sh >= 0) f = mant << sh;
+  else if (sh > -64) f = mant >> (-sh);
+  const int sg = (b < 0) ? -1 : 1;
+#pragma unroll
+  for (int t = 0; t < 8; ++t)
+    if (t < s) h[t] = __int2half_rn(sg * (int)((f >> (49 - 7 * t)) & 127ull));
+}
+
 __global__ void __launch_bounds__(256) slice_kernel(int R, int Kd, int Rp, int Kp, int s, const double *__restrict__ In,
                                                     long rs, long ks, const int *__restrict__ ex,
                                                     __half *__restrict__ Out) {
   __shared__ double tile[32][33];
+  __shared__ int tex[32];
   const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
+  if (threadIdx.x < 32) tex[threadIdx.x] = (r0 + threadIdx.x < R) ? ex[r0 + threadIdx.x] : 0;
   // load: coalesce along whichever dimension is contiguous
   for (int q = ty; q < 32; q += 8) {
     int r, k;
     if (ks == 1) { r = r0 + q; k = k0 + tx; } else { r = r0 + tx; k = k0 + q; }
     double v = 0.0;
-    if (r < R && k < Kd) v = ldexp(In[(size_t)r * rs + (size_t)k * ks], -ex[r]);
+    if (r < R && k < Kd) v = In[(size_t)r * rs + (size_t)k * ks];
     if (ks == 1) tile[q][tx] = v; else tile[tx][q] = v;
   }
   __syncthreads();
@@ -117,13 +160,11 @@ __global__ void __launch_bounds__(256) slice_kernel(int R, int Kd, int Rp, int K
   for (int q = ty; q < 32; q += 8) {
     const int r = r0 + q, k = k0 + tx;
     if (r >= Rp || k >= Kp) continue;
-    double x = tile[q][tx];
-    for (int t = 0; t < s; ++t) {
-      x *= 128.0;
-      const double dg = trunc(x);
-      x -= dg;
-      Out[((size_t)t * Rp + r) * Kp + k] = __double2half((float)dg);
-    }
+    __half h[8];
+    digits_of(tile[q][tx], tex[q], s, h);
+#pragma unroll
+    for (int t = 0; t < 8; ++t)
+      if (t < s) Out[((size_t)t * Rp + r) * Kp + k] = h[t];
   }
 }
 
@@ -155,7 +196,17 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1)
   __shared__ double colscale[TN];
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * TM, n0 = (blockIdx.y + p.nt0) * TN;
+  // Tile order: CTAs launch in linear order; consecutive CTAs walk groups of
+  // kRasterN column tiles row tile by row tile, so the CTAs resident at one
+  // time share few A and B slices (L2 reuse across the wave).
+  int m0, n0;
+  {
+    const int L = blockIdx.x + blockIdx.y * gridDim.x, Mt = gridDim.x, Nt = gridDim.y;
+    const int g = L / (kRasterN * Mt), loc = L - g * kRasterN * Mt;
+    const int gw = (Nt - g * kRasterN < kRasterN) ? Nt - g * kRasterN : kRasterN;
+    m0 = (loc / gw) * TM;
+    n0 = (g * kRasterN + loc % gw + p.nt0) * TN;
+  }
   const int nkb = p.Kp / KB;
   const int nchunk = (nkb + KCHUNK_BLOCKS - 1) / KCHUNK_BLOCKS;
 

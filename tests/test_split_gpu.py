@@ -82,3 +82,63 @@ def test_split_dgemm_transposes_alpha_beta(gb, ta, tb):
     opB = B if tb == 111 else B.T
     ref = -1.5 * (opA @ opB) + 0.5 * C0
     assert np.abs(Cs - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def split_emulation(A, B, alpha, beta, C0, ns):
+    """The split DGEMM's arithmetic restated in numpy: per-row / per-column
+    exponents (frexp of the max), 7-bit digits by the exact FP64 recurrence
+    x *= 128, d = trunc(x), x -= d, exact integer diagonal sums, and the FP64
+    recombination smallest diagonal first (C = beta C + v for the first
+    diagonal, C += v after it, v = (acc * alpha 2^(ea - 7(d+2))) * 2^eb)."""
+    def expo(v):
+        m = np.abs(v).max(axis=1)
+        return np.where(m > 0, np.frexp(m)[1], 0)
+
+    def digits(V, e):
+        x = np.ldexp(V, -e[:, None])
+        out = []
+        for _ in range(ns):
+            x = x * 128.0
+            d = np.trunc(x)
+            x = x - d
+            out.append(d)
+        return out
+
+    ea, eb = expo(A), expo(B.T)
+    At, Bt = digits(A, ea), digits(B.T, eb)
+    C = C0.copy()
+    first = True
+    for d in range(ns - 1, -1, -1):
+        # digit products < 2^14, sums < 2^53: exact in FP64 in any order
+        acc = sum(At[t] @ Bt[d - t].T for t in range(d + 1))
+        fr = np.ldexp(alpha, ea - 7 * (d + 2))
+        v = (acc * fr[:, None]) * np.ldexp(1.0, eb)[None, :]
+        if first and beta == 0.0:
+            C = v
+        else:
+            C = C + v
+        first = False
+    return C
+
+
+@pytest.mark.parametrize("alpha,beta,ns", [(1.0, 0.0, 8), (-0.75, 1.0, 8), (1.0 / 3.0, 0.0, 5), (-1.0, 1.0, 3)])
+def test_split_dgemm_bit_exact_vs_emulation(gb, alpha, beta, ns):
+    # every step of the split scheme, bit for bit: mixed magnitudes and signs,
+    # an all-zero row and column, subnormal entries, exact powers of two
+    M, N, K = 190, 300, 1100
+    rng = np.random.default_rng(ns)
+    A = rng.uniform(-1, 1, (M, K)) * np.exp2(rng.integers(-30, 31, (M, K)))
+    B = rng.uniform(-1, 1, (K, N)) * np.exp2(rng.integers(-30, 31, (K, N)))
+    A[5, :] = 0.0
+    B[:, 7] = 0.0
+    A[9, :10] = 5e-310
+    A[9, 10] = 1.0
+    B[3, 11] = -4.9e-324
+    A[11, 12] = -2.0 ** 40
+    A = np.asfortranarray(A)
+    B = np.asfortranarray(B)
+    C0 = np.asfortranarray(rng.standard_normal((M, N)))
+    Cg = C0.copy(order="F")
+    gb.dgemm_split(111, 111, alpha, A, B, beta, Cg, nslices=ns)
+    ref = split_emulation(A, B, alpha, beta, C0, ns)
+    assert np.array_equal(Cg, ref)
