@@ -618,6 +618,8 @@ def run_case(args):
     elif args.case == "dgetrf":
         if args.pw:
             L.atlg_panel_width(args.pw)
+        if args.grid:
+            L.atlg_panel_grid(args.grid)
         A0 = torch.rand(n, n, device="cuda", dtype=torch.float64, generator=g) - 0.5
         A = torch.empty_like(A0)
         piv = torch.zeros(n, dtype=torch.int32, device="cuda")
@@ -637,6 +639,8 @@ def run_case(args):
             L.atlg_split_lu_leaf(args.leaf)
         if args.pw:
             L.atlg_panel_width(args.pw)
+        if args.grid:
+            L.atlg_panel_grid(args.grid)
         A0 = torch.rand(n, n, device="cuda", dtype=torch.float64, generator=g) - 0.5
         A = torch.empty_like(A0)
         piv = torch.zeros(n, dtype=torch.int32, device="cuda")
@@ -714,6 +718,7 @@ def main():
     ap.add_argument("--k", type=int, default=0, help="inner dimension of --case split (0: n)")
     ap.add_argument("--leaf", type=int, default=0, help="FP64 leaf width of --case splitlu (0: default)")
     ap.add_argument("--pw", type=int, default=0, help="FP64 LU panel width for --case splitlu/dgetrf (0: default)")
+    ap.add_argument("--grid", type=int, default=0, help="grid-panel CTAs for --case splitlu/dgetrf (0: default)")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
     ap.add_argument("--case", choices=["split", "sgetrf", "dgetrf", "mixed", "potrf", "trmm", "getri", "splitlu"], default=None,
                     help="run one kernel workload for a profiling capture instead of the benchmark")

@@ -256,7 +256,7 @@ int atlg_sgetrf_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void 
 int atlg_dgetrf_split_dev(int N, double *A, int lda, int *ipiv, int nslices, int nb,
                           void *stream);
 /* widest block column the split LU hands to the FP64 LU (rounded down to a
- * multiple of 256; 0: the default 1024); narrower leaves move more of the
+ * multiple of 256; 0: the default 512); narrower leaves move more of the
  * block column's own updates onto split products */
 void atlg_split_lu_leaf(int nb);
 int atlg_dgetrs_dev(int Order, int Trans, int N, int NRHS, const double *A, int lda,

@@ -877,12 +877,13 @@ static int g_panel_nb_f64 = NB;
 void set_panel_width_f64(int w) { g_panel_nb_f64 = (w >= 8 && w <= NB) ? w / 8 * 8 : NB; }
 
 template <typename T>
-static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaStream_t st, bool tc = false) {
+static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaStream_t st, bool tc = false,
+                       int pw_f64 = 0) {
   ATLG_CHECK(cudaMemsetAsync(info, 0, sizeof(int), st));
   if (M <= 0 || N <= 0) return;
   Context &c = ctx();
   const int MN = M < N ? M : N;
-  const int PW = (sizeof(T) == 8) ? g_panel_nb_f64 : NB;   // panel width
+  const int PW = (sizeof(T) == 8) ? (pw_f64 > 0 ? pw_f64 : g_panel_nb_f64) : NB;   // panel width
   // Look-ahead: the trailing update of step k is split into the next panel's
   // columns (on the caller's stream, so panel k+1 can start at once) and the
   // rest (on a low-priority side stream, overlapping panel k+1).  The panel
@@ -1001,6 +1002,9 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
 
 void dev_dgetrf(int M, int N, double *A, int lda, int *ipiv, int *info, cudaStream_t st) {
   getrf_impl<double>(M, N, A, lda, ipiv, info, st);
+}
+void dev_dgetrf_pw(int M, int N, double *A, int lda, int *ipiv, int *info, int pw, cudaStream_t st) {
+  getrf_impl<double>(M, N, A, lda, ipiv, info, st, false, (pw >= 8 && pw <= NB) ? pw / 8 * 8 : NB);
 }
 void dev_sgetrf(int M, int N, float *A, int lda, int *ipiv, int *info, cudaStream_t st) {
   getrf_impl<float>(M, N, A, lda, ipiv, info, st);

@@ -16,6 +16,8 @@ void set_panel_width_f64(int w);
 // ipiv (device, min(M,N) ints, 0-based, global row indices) and info
 // (device int: 0, or the 1-based index of the first exactly-zero pivot).
 void dev_dgetrf(int M, int N, double *A, int lda, int *ipiv, int *info, cudaStream_t st);
+// dev_dgetrf with an explicit panel width (8..64, a multiple of 8)
+void dev_dgetrf_pw(int M, int N, double *A, int lda, int *ipiv, int *info, int pw, cudaStream_t st);
 void dev_sgetrf(int M, int N, float *A, int lda, int *ipiv, int *info, cudaStream_t st);
 // FP32 LU whose trailing updates run on tcgen05 tensor cores in 3xTF32 (the
 // mixed-precision solver's factor; pivots may differ from the FFMA sgetrf

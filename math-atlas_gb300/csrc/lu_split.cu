@@ -7,9 +7,9 @@
 //
 // Outer blocks of nb columns (a multiple of 256; 1024 by default), right-
 // looking, with look-ahead:
-//  1. the (n-k) x nb block column is factored by the FP64 LU (lu.cu: 64-wide
-//     panels, look-ahead, DFMA updates inside the block column; wider than
-//     1024 columns, by this same method with 1024-column blocks);
+//  1. the (n-k) x nb block column is factored by this same method with
+//     512-column blocks (split updates between them), each of those by the
+//     FP64 LU (lu.cu: 32-wide panels, look-ahead, DFMA updates);
 //  2. its interchanges are applied to the columns left and right of it;
 //  3. U12 = L11^-1 A12 as inv(L11) (unit lower, trtri in FP64) times A12 on
 //     the split DGEMM;
@@ -45,9 +45,15 @@ __global__ void unit_lower_kernel(int kb, const double *A, int lda, double *W, i
 }
 
 // Widest block column handed to the FP64 LU (a multiple of 256); wider ones
-// are factored recursively with blocks of this width.
-static int g_leaf_nb = 1024;
-void set_split_lu_leaf(int nb) { g_leaf_nb = (nb >= kSplitTileN) ? nb / kSplitTileN * kSplitTileN : 1024; }
+// are factored recursively with blocks of this width.  The leaves' FP64 LU
+// uses 32-wide panels: a panel's own rank-1 updates run on the FP64 pipe of
+// the few SMs the panel occupies, a narrower panel leaves more of that work
+// to the leaf's DGEMMs on every SM.  Measured at n = 16384 with 1024-wide
+// outer blocks: leaves 1024/512/256 with 64-wide panels 362/360/382 ms,
+// 512-wide leaves with 32-wide panels 342 ms.
+constexpr int kLeafDefault = 512, kLeafPanel = 32;
+static int g_leaf_nb = kLeafDefault;
+void set_split_lu_leaf(int nb) { g_leaf_nb = (nb >= kSplitTileN) ? nb / kSplitTileN * kSplitTileN : kLeafDefault; }
 
 // M x N (M >= N) partial-pivoting LU of A in place; pivots relative to row 0
 // of A; returns 0 or the first zero pivot (1-based).  Outer blocks of nb
@@ -74,7 +80,7 @@ static int split_lu(int M, int N, double *A, int lda, int *ipiv, int nslices, in
     if (!leaf) {
       binfo = split_lu(m, kb, Akk, lda, ipiv + k, nslices, g_leaf_nb, false, st);   // relative to row k
     } else {
-      dev_dgetrf(m, kb, Akk, lda, ipiv + k, dinfo, st);                       // relative to row k
+      dev_dgetrf_pw(m, kb, Akk, lda, ipiv + k, dinfo, kLeafPanel, st);        // relative to row k
       ATLG_CHECK(cudaMemcpyAsync(&binfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
     }
     if (outer_pending) {   // the interchanges touch every column
