@@ -54,8 +54,14 @@ template <typename T, int BM, int BN, int BK, int TM, int TN, int NT, int STAGES
 __global__ void __launch_bounds__(NT)
     gemm_kernel(int M, int N, int K, T alpha, const T *__restrict__ A, int lda,
                 const T *__restrict__ B, int ldb, T beta, T *__restrict__ C, int ldc, int uplo, int tri,
-                const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB) {
+                const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, long sA, long sB,
+                long sC) {
   using KC = GemmKernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, USE_TMA>;
+  if (!USE_TMA && blockIdx.z) {   // batched products (pointer arithmetic only on the cp.async path)
+    A += blockIdx.z * sA;
+    B += blockIdx.z * sB;
+    C += blockIdx.z * sC;
+  }
   extern __shared__ __align__(128) unsigned char smem_raw[];
   T *smem = reinterpret_cast<T *>(smem_raw);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + STAGES * KC::STAGE_ELEMS * sizeof(T));
@@ -231,10 +237,12 @@ template <> struct DT<float>  { static constexpr CUtensorMapDataType v = CU_TENS
 
 template <typename T, int BM, int BN, int BK, int TM, int TN, int NT, int STAGES, int TA, int TB>
 static void launch_cfg(int M, int N, int K, T alpha, const T *A, int lda, const T *B, int ldb,
-                       T beta, T *C, int ldc, cudaStream_t st, bool allow_tma, int uplo, int tri) {
-  dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN);
+                       T beta, T *C, int ldc, cudaStream_t st, bool allow_tma, int uplo, int tri,
+                       const GemmOpts &o) {
+  const int nb = o.batch > 1 ? o.batch : 1;
+  dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN, nb);
   CUtensorMap tmA, tmB;
-  bool tma = allow_tma;
+  bool tma = allow_tma && nb == 1;
   if (tma) {
     // op(A) is M x K; stored TA==N as M x K (inner M), TA==T as K x M (inner K)
     if (TA == kNoTrans) tma = encode_tmap_2d(&tmA, A, DT<T>::v, sizeof(T), M, K, lda, BM, BK);
@@ -248,7 +256,8 @@ static void launch_cfg(int M, int N, int K, T alpha, const T *A, int lda, const 
     using KC = GemmKernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, true>;
     auto k = gemm_kernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, true>;
     ATLG_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, KC::SMEM_BYTES));
-    k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, uplo, tri, tmA, tmB);
+    k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, uplo, tri, tmA, tmB, 0L, 0L,
+                                        0L);
     note_launch();
   } else {
     memset(&tmA, 0, sizeof(tmA));
@@ -256,7 +265,8 @@ static void launch_cfg(int M, int N, int K, T alpha, const T *A, int lda, const 
     using KC = GemmKernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, false>;
     auto k = gemm_kernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, false>;
     ATLG_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, KC::SMEM_BYTES));
-    k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, uplo, tri, tmA, tmB);
+    k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, uplo, tri, tmA, tmB,
+                                        o.stride_a, o.stride_b, o.stride_c);
     note_launch();
   }
   ATLG_CHECK(cudaGetLastError());
@@ -279,18 +289,21 @@ static int pick_dtile(int M, int N, int nsm) {
 
 template <int TA, int TB>
 static void dgemm_t(int M, int N, int K, double alpha, const double *A, int lda, const double *B, int ldb,
-                    double beta, double *C, int ldc, cudaStream_t st, bool tma, int nsm, int uplo, int tri) {
-  switch (pick_dtile(M, N, nsm)) {
-    case 0: launch_cfg<double, 64, 64, 16, 8, 4, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo, tri); break;
-    case 1: launch_cfg<double, 64, 32, 16, 4, 4, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo, tri); break;
-    default: launch_cfg<double, 32, 32, 16, 4, 2, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo, tri); break;
+                    double beta, double *C, int ldc, cudaStream_t st, bool tma, int nsm, int uplo, int tri,
+                    const GemmOpts &o) {
+  // a batch spreads its products over the SMs: tile choice per product
+  const int per = (o.batch > 1) ? (nsm + o.batch - 1) / o.batch : nsm;
+  switch (pick_dtile(M, N, per)) {
+    case 0: launch_cfg<double, 64, 64, 16, 8, 4, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo, tri, o); break;
+    case 1: launch_cfg<double, 64, 32, 16, 4, 4, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo, tri, o); break;
+    default: launch_cfg<double, 32, 32, 16, 4, 2, 128, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo, tri, o); break;
   }
 }
 
 template <int TA, int TB>
 static void sgemm_t(int M, int N, int K, float alpha, const float *A, int lda, const float *B, int ldb,
-                    float beta, float *C, int ldc, cudaStream_t st, bool tma, int uplo, int tri) {
-  launch_cfg<float, 128, 128, 16, 8, 8, 256, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo, tri);
+                    float beta, float *C, int ldc, cudaStream_t st, bool tma, int uplo, int tri, const GemmOpts &o) {
+  launch_cfg<float, 128, 128, 16, 8, 8, 256, 4, TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, tma, uplo, tri, o);
 }
 
 __global__ void scale_kernel_d(int M, int N, double beta, double *C, int ldc) {
@@ -433,35 +446,41 @@ struct ProfScope {
 // ATL_gemm semantics: alpha==0 or K==0 -> C = beta*C (gescal / gezero).
 void dev_dgemm(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda, const double *B,
                int ldb, double beta, double *C, int ldc, cudaStream_t st, const GemmOpts &o) {
-  if (M <= 0 || N <= 0) return;
-  if (alpha == 0.0 || K <= 0) { dev_gescal(M, N, beta, C, ldc, st); return; }
+  if (M <= 0 || N <= 0 || o.batch < 1) return;
+  if (alpha == 0.0 || K <= 0) {
+    for (int z = 0; z < o.batch; ++z) dev_gescal(M, N, beta, C + z * o.stride_c, ldc, st);
+    return;
+  }
   const bool ta = TA != kNoTrans, tb = TB != kNoTrans;
   const int nsm = o.num_sms > 0 ? o.num_sms : ctx().num_sms;
-  if (N == 1 && o.allow_gemv && o.uplo == 0 && o.tri == 0) {   // matrix-vector product: x = op(B)(:,0)
+  if (N == 1 && o.allow_gemv && o.uplo == 0 && o.tri == 0 && o.batch == 1) {   // matrix-vector: x = op(B)(:,0)
     gemv_launch<double>(TA, M, K, alpha, A, lda, B, tb ? ldb : 1, beta, C, st);
     return;
   }
-  ProfScope ps(st, 2.0 * M * N * K);
-  if (!ta && !tb) dgemm_t<kNoTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo, o.tri);
-  else if (!ta && tb) dgemm_t<kNoTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo, o.tri);
-  else if (ta && !tb) dgemm_t<kTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo, o.tri);
-  else dgemm_t<kTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo, o.tri);
+  ProfScope ps(st, 2.0 * M * N * K * o.batch);
+  if (!ta && !tb) dgemm_t<kNoTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo, o.tri, o);
+  else if (!ta && tb) dgemm_t<kNoTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo, o.tri, o);
+  else if (ta && !tb) dgemm_t<kTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo, o.tri, o);
+  else dgemm_t<kTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, nsm, o.uplo, o.tri, o);
 }
 
 void dev_sgemm(int TA, int TB, int M, int N, int K, float alpha, const float *A, int lda, const float *B,
                int ldb, float beta, float *C, int ldc, cudaStream_t st, const GemmOpts &o) {
-  if (M <= 0 || N <= 0) return;
-  if (alpha == 0.0f || K <= 0) { dev_gescal(M, N, beta, C, ldc, st); return; }
+  if (M <= 0 || N <= 0 || o.batch < 1) return;
+  if (alpha == 0.0f || K <= 0) {
+    for (int z = 0; z < o.batch; ++z) dev_gescal(M, N, beta, C + z * o.stride_c, ldc, st);
+    return;
+  }
   const bool ta = TA != kNoTrans, tb = TB != kNoTrans;
-  if (N == 1 && o.allow_gemv && o.uplo == 0 && o.tri == 0) {
+  if (N == 1 && o.allow_gemv && o.uplo == 0 && o.tri == 0 && o.batch == 1) {
     gemv_launch<float>(TA, M, K, alpha, A, lda, B, tb ? ldb : 1, beta, C, st);
     return;
   }
-  ProfScope ps(st, 2.0 * M * N * K);
-  if (!ta && !tb) sgemm_t<kNoTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo, o.tri);
-  else if (!ta && tb) sgemm_t<kNoTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo, o.tri);
-  else if (ta && !tb) sgemm_t<kTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo, o.tri);
-  else sgemm_t<kTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo, o.tri);
+  ProfScope ps(st, 2.0 * M * N * K * o.batch);
+  if (!ta && !tb) sgemm_t<kNoTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo, o.tri, o);
+  else if (!ta && tb) sgemm_t<kNoTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo, o.tri, o);
+  else if (ta && !tb) sgemm_t<kTrans, kNoTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo, o.tri, o);
+  else sgemm_t<kTrans, kTrans>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, o.allow_tma, o.uplo, o.tri, o);
 }
 
 unsigned gemm_status_read_and_clear() {

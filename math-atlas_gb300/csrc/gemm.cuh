@@ -11,6 +11,10 @@ struct GemmOpts {
   bool allow_gemv = true;  // N == 1 goes to the matrix-vector kernels
   int uplo = 0;            // kLower / kUpper: update only that triangle of C (M == N), as SYRK
   int tri = 0;             // triangular operand (TRMM): kTriA|kTriB, kTriUpper, kTriUnit; 0 = dense
+  // batch of products of one shape: product z uses A + z*stride_a,
+  // B + z*stride_b, C + z*stride_c (elements); batch > 1 uses the cp.async loader
+  int batch = 1;
+  long stride_a = 0, stride_b = 0, stride_c = 0;
 };
 
 // GemmOpts::tri bits.  The triangle is stated for op(A) (M x K, M == K) or

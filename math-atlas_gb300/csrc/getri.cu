@@ -6,12 +6,13 @@
 // clapack_getri (atlas-lp.base:16-220, AtlasBase/Clint/atlas-clp.base:115-139).
 //
 // GB300 design.
-//  * trtri keeps the reference's recursion -- the off-diagonal block of each
-//    split becomes -inv(A11) A12 inv(A22) through two TRSMs -- but splits at
-//    multiples of 64 and defers the diagonal blocks: every TRSM reads only
-//    original diagonal blocks, so all of them are issued first (pre-order),
-//    and one launch then inverts every 64 x 64 diagonal block, one CTA each,
-//    in shared memory.
+//  * trtri keeps the reference's recursive split (the off-diagonal block of
+//    each split becomes -inv(A11) A12 inv(A22)) at multiples of 64, but runs
+//    it bottom-up: one launch inverts every 64 x 64 diagonal block (one CTA
+//    each, in shared memory), then each split, children first, forms its
+//    off-diagonal block from the two inverses already in place with GEMMs
+//    whose triangular operand skips the zero k-tiles -- no triangular solves,
+//    whose short dependency chains left the FP64 pipe idle.
 //  * getri: inv(U) by trtri, the strictly lower factor moved to a workspace
 //    (zeros left in A) by one kernel, X L = inv(U) as a single Right/Lower/
 //    Unit TRSM over the whole matrix, and the column interchanges composed on
@@ -27,6 +28,7 @@
 
 #include "common.cuh"
 #include "context.cuh"
+#include "gemm.cuh"
 #include "getri.cuh"
 #include "trsm.cuh"
 
@@ -86,24 +88,93 @@ static void trsm_t(int side, int uplo, int diag, int M, int N, T alpha, const T 
     dev_strsm(side, uplo, kNoTrans, diag, M, N, (float)alpha, (const float *)A, lda, (float *)B, ldb, st);
 }
 
-// The off-diagonal blocks of the recursion, pre-order (diagonal blocks later).
 template <typename T>
-static void trtri_offdiag(int upper, int diag, int n, T *A, int lda, cudaStream_t st) {
-  if (n <= TB) return;
-  const int nl = ((n / 2 + TB - 1) / TB) * TB;
-  const int nr = n - nl;
-  T *A22 = A + nl + (size_t)nl * lda;
-  if (upper) {
-    T *A12 = A + (size_t)nl * lda;
-    trsm_t<T>(kRight, kUpper, diag, nl, nr, T(1), A22, lda, A12, lda, st);   // A12 inv(U22)
-    trsm_t<T>(kLeft, kUpper, diag, nl, nr, T(-1), A, lda, A12, lda, st);     // -inv(U11) A12 inv(U22)
+static void gemm_t(int M, int N, int K, T alpha, const T *A, int lda, const T *B, int ldb, T beta, T *C, int ldc,
+                   int tri, cudaStream_t st, int batch = 1, long sa = 0, long sb = 0, long sc = 0) {
+  if (M <= 0 || N <= 0 || K <= 0 || batch <= 0) return;
+  GemmOpts o;
+  o.tri = tri;
+  o.batch = batch;
+  o.stride_a = sa;
+  o.stride_b = sb;
+  o.stride_c = sc;
+  if (sizeof(T) == 8)
+    dev_dgemm(kNoTrans, kNoTrans, M, N, K, (double)alpha, (const double *)A, lda, (const double *)B, ldb,
+              (double)beta, (double *)C, ldc, st, o);
+  else
+    dev_sgemm(kNoTrans, kNoTrans, M, N, K, (float)alpha, (const float *)A, lda, (const float *)B, ldb, (float)beta,
+              (float *)C, ldc, st, o);
+}
+
+// Columns of the off-diagonal block computed per pass (bounds the workspace).
+constexpr int kTriChunk = 1024;
+
+// One split of the recursion whose diagonal blocks already hold their
+// inverses X11 (nl x nl at P) and X22 (nr x nr):
+//   lower:  X21 = -X22 (L21 X11),   upper:  X12 = -X11 (U12 X22),
+// as GEMMs whose triangular operand skips the k-tiles outside its triangle.
+// The inner product goes through a workspace W of at most kTriChunk columns:
+// columns [c0, c1) of L21 X11 are L21(:, c0:c1) X11(c0:c1, c0:c1) (lower
+// triangular operand) + L21(:, c1:) X11(c1:, c0:c1) (dense), so the chunks
+// run left to right and overwrite L21 in place; those of U12 X22 are
+// U12(:, c0:c1) X22(c0:c1, c0:c1) (upper) + U12(:, :c0) X22(:c0, c0:c1),
+// right to left.
+template <typename T>
+static void combine_node(int upper, int unit, int nl, int nr, T *P, int lda, T *W, cudaStream_t st) {
+  T *A22 = P + nl + (size_t)nl * lda;
+  if (!upper) {
+    T *A21 = P + nl;                                           // nr x nl
+    for (int c0 = 0; c0 < nl; c0 += kTriChunk) {
+      const int c1 = (c0 + kTriChunk < nl) ? c0 + kTriChunk : nl, w = c1 - c0;
+      const T *X11c = P + c0 + (size_t)c0 * lda;               // X11(c0:, c0:c1)
+      gemm_t<T>(nr, w, w, T(1), A21 + (size_t)c0 * lda, lda, X11c, lda, T(0), W, nr, kTriB | unit, st);
+      gemm_t<T>(nr, w, nl - c1, T(1), A21 + (size_t)c1 * lda, lda, X11c + w, lda, T(1), W, nr, 0, st);
+      gemm_t<T>(nr, w, nr, T(-1), A22, lda, W, nr, T(0), A21 + (size_t)c0 * lda, lda, kTriA | unit, st);
+    }
   } else {
-    T *A21 = A + nl;
-    trsm_t<T>(kRight, kLower, diag, nr, nl, T(1), A, lda, A21, lda, st);     // A21 inv(L11)
-    trsm_t<T>(kLeft, kLower, diag, nr, nl, T(-1), A22, lda, A21, lda, st);   // -inv(L22) A21 inv(L11)
+    T *A12 = P + (size_t)nl * lda;                             // nl x nr
+    for (int c1 = nr; c1 > 0; c1 -= kTriChunk) {
+      const int c0 = (c1 - kTriChunk > 0) ? c1 - kTriChunk : 0, w = c1 - c0;
+      const T *X22c = A22 + (size_t)c0 * lda;                  // X22(:, c0:c1)
+      gemm_t<T>(nl, w, w, T(1), A12 + (size_t)c0 * lda, lda, X22c + c0, lda, T(0), W, nl,
+                kTriB | kTriUpper | unit, st);
+      gemm_t<T>(nl, w, c0, T(1), A12, lda, X22c, lda, T(1), W, nl, 0, st);
+      gemm_t<T>(nl, w, nl, T(-1), P, lda, W, nl, T(0), A12 + (size_t)c0 * lda, lda, kTriA | kTriUpper | unit, st);
+    }
   }
-  trtri_offdiag<T>(upper, diag, nl, A, lda, st);
-  trtri_offdiag<T>(upper, diag, nr, A22, lda, st);
+}
+
+// Bottom-up recursion over aligned power-of-two blocks: after the 64 x 64
+// diagonal blocks are inverted, level b (64, 128, ...) combines every
+// aligned 2b block [2bz, 2bz + 2b) from its two inverted halves; the full
+// blocks of a level go in one batched GEMM per step (when one chunk covers
+// them), a ragged last block (second half shorter than b) on its own.
+template <typename T>
+static void trtri_combine(int upper, int diag, int n, T *A, int lda, T *W, cudaStream_t st) {
+  const int unit = (diag == kUnit) ? kTriUnit : 0;
+  for (int b = TB; b < n; b *= 2) {
+    const int count = n / (2 * b);
+    const long sd = 2L * b * (lda + 1);                        // diagonal step between blocks
+    if (count > 0 && b <= kTriChunk) {
+      const long sw = (long)b * b;
+      if (!upper) {
+        // W_z = L21_z X11_z;  L21_z = -X22_z W_z
+        gemm_t<T>(b, b, b, T(1), A + b, lda, A, lda, T(0), W, b, kTriB | unit, st, count, sd, sd, sw);
+        gemm_t<T>(b, b, b, T(-1), A + b + (size_t)b * lda, lda, W, b, T(0), A + b, lda, kTriA | unit, st, count, sd,
+                  sw, sd);
+      } else {
+        // W_z = U12_z X22_z;  U12_z = -X11_z W_z
+        gemm_t<T>(b, b, b, T(1), A + (size_t)b * lda, lda, A + b + (size_t)b * lda, lda, T(0), W, b,
+                  kTriB | kTriUpper | unit, st, count, sd, sd, sw);
+        gemm_t<T>(b, b, b, T(-1), A, lda, W, b, T(0), A + (size_t)b * lda, lda, kTriA | kTriUpper | unit, st, count,
+                  sd, sw, sd);
+      }
+    } else {
+      for (int z = 0; z < count; ++z) combine_node<T>(upper, unit, b, b, A + z * sd, lda, W, st);
+    }
+    const int r0 = count * 2 * b;
+    if (r0 + b < n) combine_node<T>(upper, unit, b, n - r0 - b, A + (size_t)r0 * (lda + 1), lda, W, st);
+  }
 }
 
 // Column-major inverse of the `upper` triangle in place; 0 or the 1-based
@@ -124,10 +195,21 @@ static int trtri_impl(int upper, int diag, int n, T *A, int lda, cudaStream_t st
     ATLG_CHECK(cudaStreamSynchronize(st));
     if (first < n) return first + 1;
   }
-  trtri_offdiag<T>(upper, diag, n, A, lda, st);
   trtri_leaf_kernel<T><<<(n + TB - 1) / TB, TB, 0, st>>>(n, upper, diag == kUnit ? 1 : 0, A, lda);
   note_launch();
   ATLG_CHECK(cudaGetLastError());
+  if (n > TB) {
+    // workspace: a level's batched products (count * b * b <= n * b / 2 for
+    // b <= kTriChunk) or one node's chunk (at most n/2 x kTriChunk)
+    size_t welems = 0;
+    for (int b = TB; b < n; b *= 2) {
+      const size_t need = (b <= kTriChunk) ? (size_t)(n / (2 * b)) * b * b + (size_t)b * b
+                                           : (size_t)b * kTriChunk;
+      if (need > welems) welems = need;
+    }
+    T *W = static_cast<T *>(ctx().buffer(kBufTri, sizeof(T) * welems));
+    trtri_combine<T>(upper, diag, n, A, lda, W, st);
+  }
   return 0;
 }
 
