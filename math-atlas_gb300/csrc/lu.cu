@@ -395,10 +395,15 @@ __device__ __forceinline__ void warp_winner(K &v, int &b, int &idx) {
 
 constexpr int CT = 512;         // threads per cluster-panel CTA (16 warps)
 
-// Row stride of the cluster panel's shared-memory tile: NB plus one 16-byte
-// vector, an odd number of vectors, so 16-byte accesses to consecutive rows
-// hit distinct banks.
-template <typename T> __host__ __device__ constexpr int cl_rs() { return NB + 16 / (int)sizeof(T); }
+// Row stride of the cluster panel's shared-memory tile for a panel of jb
+// columns: jb rounded up to an even number of 16-byte vectors plus one
+// vector -- an odd number of vectors, so 16-byte accesses to consecutive rows
+// hit distinct banks (NB + 16/sizeof(T) for a full panel).  A narrower
+// panel's rows take proportionally less shared memory, so taller panels fit
+// one cluster.
+template <typename T> __host__ __device__ constexpr int cl_rs(int jb) {
+  return (jb + 32 / (int)sizeof(T) - 1) / (32 / (int)sizeof(T)) * (32 / (int)sizeof(T)) + 16 / (int)sizeof(T);
+}
 
 // Vector update of one row's columns [cb, jb) (cb >= 1): a -= l * P.
 template <typename T>
@@ -465,7 +470,7 @@ __global__ void __launch_bounds__(CT)
   using K = typename PivKey<T>::K;
   constexpr int VE = 16 / (int)sizeof(T);        // elements per 16-byte vector
   constexpr int NV = NB / VE;                    // vectors per row
-  constexpr int RS = cl_rs<T>();
+  const int RS = cl_rs<T>(jb);
   constexpr int NW = CT / 32;
   extern __shared__ __align__(16) unsigned char panel_dyn[];
   __shared__ ClusterSlots<T> slot;
@@ -925,7 +930,7 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     void *args[] = {&Ap, (void *)&lda, &Mp, (void *)&jb, &koff, &ipk, &info, &rec, &jrow, &bar, &perm};
     // one cluster when the panel fits its shared memory (panels only shrink,
     // so the grid path below is never needed after it)
-    const size_t ctile = cn ? sizeof(T) * (size_t)((Mp + cn - 1) / cn) * cl_rs<T>() : 0;
+    const size_t ctile = cn ? sizeof(T) * (size_t)((Mp + cn - 1) / cn) * cl_rs<T>(jb) : 0;
     if (cn && ctile <= kClusterSmemMax) {
       cudaLaunchConfig_t cfg = {};
       cudaLaunchAttribute at[1];
