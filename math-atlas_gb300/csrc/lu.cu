@@ -83,26 +83,37 @@ struct BlockArgmax {
   int i[PT / 32];
 };
 
+// Warp-wide first-max on (key, idx): the larger key wins, the lower idx
+// among equal keys; every lane ends with the result.  Hardware warp
+// reductions (redux.sync) instead of a five-level shuffle tree; a 64-bit key
+// is compared as (signed high word, unsigned low word).
+__device__ __forceinline__ void warp_argmax(int &key, int &idx) {
+  const int mk = __reduce_max_sync(0xffffffffu, key);
+  idx = __reduce_min_sync(0xffffffffu, key == mk ? idx : 0x7fffffff);
+  key = mk;
+}
+__device__ __forceinline__ void warp_argmax(long long &key, int &idx) {
+  const int hi = (int)(key >> 32);
+  const unsigned lo = (unsigned)(key & 0xffffffffLL);
+  const int mh = __reduce_max_sync(0xffffffffu, hi);
+  const unsigned ml = __reduce_max_sync(0xffffffffu, hi == mh ? lo : 0u);
+  idx = __reduce_min_sync(0xffffffffu, (hi == mh && lo == ml) ? idx : 0x7fffffff);
+  key = (long long)(((unsigned long long)(unsigned)mh << 32) | ml);
+}
+
 // first-max reduction over the block: (key, idx) with the larger key
-// winning, lower idx winning ties; key < 0 marks "no candidate".
+// winning, lower idx winning ties; key < 0 marks "no candidate".  Warp 0
+// ends with the result.
 template <typename K>
 __device__ void block_argmax(K &val, int &idx, BlockArgmax<K> &sh) {
-  for (int o = 16; o > 0; o >>= 1) {
-    const K ov = __shfl_down_sync(0xffffffffu, val, o);
-    const int oi = __shfl_down_sync(0xffffffffu, idx, o);
-    if (ov > val || (ov == val && oi < idx && ov >= K(0))) { val = ov; idx = oi; }
-  }
+  warp_argmax(val, idx);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (lane == 0) { sh.v[w] = val; sh.i[w] = idx; }
   __syncthreads();
   if (w == 0) {
     val = lane < PT / 32 ? sh.v[lane] : K(-1);
     idx = lane < PT / 32 ? sh.i[lane] : 0x7fffffff;
-    for (int o = 16; o > 0; o >>= 1) {
-      const K ov = __shfl_down_sync(0xffffffffu, val, o);
-      const int oi = __shfl_down_sync(0xffffffffu, idx, o);
-      if (ov > val || (ov == val && oi < idx && ov >= K(0))) { val = ov; idx = oi; }
-    }
+    warp_argmax(val, idx);
   }
   __syncthreads();
 }
@@ -266,11 +277,7 @@ __global__ void __launch_bounds__(PT)
         const K v = PivKey<T>::from_t(gather_all ? gath[b * RS + NB] : __ldcg(rp + (size_t)b * RS + NB));
         if (v > best) { best = v; bb = b; }
       }
-      for (int o = 16; o > 0; o >>= 1) {
-        const K ov = __shfl_down_sync(0xffffffffu, best, o);
-        const int ob = __shfl_down_sync(0xffffffffu, bb, o);
-        if (ov > best || (ov == best && ob < bb)) { best = ov; bb = ob; }
-      }
+      warp_argmax(best, bb);
       if (threadIdx.x == 0) {
         int p = -1;
         if (bb < G && best > K(0)) p = (int)(gather_all ? gath[bb * RS + NB + 1] : __ldcg(rp + (size_t)bb * RS + NB + 1));
@@ -382,15 +389,12 @@ template <typename T> struct Vec16;
 template <> struct Vec16<float> { using type = float4; };
 template <> struct Vec16<double> { using type = double2; };
 
-// (larger key, then lower source) wins; every lane ends with the winner
+// (larger key, then lower source) wins; every lane ends with the winner.
+// Lane s holds source s (b = s), so the winner's row comes from lane b.
 template <typename K>
 __device__ __forceinline__ void warp_winner(K &v, int &b, int &idx) {
-  for (int o = 16; o > 0; o >>= 1) {
-    const K ov = __shfl_xor_sync(0xffffffffu, v, o);
-    const int ob = __shfl_xor_sync(0xffffffffu, b, o);
-    const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
-    if (ov > v || (ov == v && ob < b)) { v = ov; b = ob; idx = oi; }
-  }
+  warp_argmax(v, b);
+  idx = __shfl_sync(0xffffffffu, idx, b & 31);
 }
 
 constexpr int CT = 512;         // threads per cluster-panel CTA (16 warps)
@@ -504,20 +508,12 @@ __global__ void __launch_bounds__(CT)
   // Reduce the per-thread candidates (rows ci already complete) to the CTA's
   // first-max; keep its row and row jn locally, push |a| and row to all.
   auto publish = [&](K best, int bi, int jn) -> int {
-    for (int o = 16; o > 0; o >>= 1) {
-      const K ov = __shfl_xor_sync(0xffffffffu, best, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ov > best || (ov == best && oi < bi && ov >= K(0))) { best = ov; bi = oi; }
-    }
+    warp_argmax(best, bi);
     if (lane == 0) { wv[w] = best; wi[w] = bi; }
     __syncthreads();
     best = lane < NW ? wv[lane] : K(-1);
     bi = lane < NW ? wi[lane] : 0x7fffffff;
-    for (int o = 16; o > 0; o >>= 1) {
-      const K ov = __shfl_xor_sync(0xffffffffu, best, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ov > best || (ov == best && oi < bi && ov >= K(0))) { best = ov; bi = oi; }
-    }
+    warp_argmax(best, bi);
     return best >= K(0) ? bi : -1;
   };
   auto push = [&](K best, int ci, int jn) {

@@ -47,8 +47,8 @@ __global__ void __launch_bounds__(WARPS * 32)
   __shared__ T rinv[TB];
   load_tri(A, lda, ta, r0, n, tri, rinv, unit != 0);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int col = blockIdx.x * WARPS + w;
-  if (col >= ncols) return;
+  // a warp per right-hand side; the CTA's triangle serves every column it visits
+  for (int col = blockIdx.x * WARPS + w; col < ncols; col += gridDim.x * WARPS) {
   T *b = B + r0 + (size_t)col * ldb;
   T x0 = lane < n ? b[lane] : T(0);
   T x1 = lane + 32 < n ? b[lane + 32] : T(0);
@@ -71,6 +71,7 @@ __global__ void __launch_bounds__(WARPS * 32)
   }
   if (lane < n) b[lane] = x0;
   if (lane + 32 < n) b[lane + 32] = x1;
+  }
 }
 
 // Right diagonal block: solve x * T = b for each row of B[:, c0:c0+n].
@@ -83,8 +84,8 @@ __global__ void __launch_bounds__(WARPS * 32)
   __shared__ T rinv[TB];
   load_tri(A, lda, ta, c0, n, tri, rinv, unit != 0);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int row = blockIdx.x * WARPS + w;
-  if (row >= nrows) return;
+  // a warp per row of B; the CTA's triangle serves every row it visits
+  for (int row = blockIdx.x * WARPS + w; row < nrows; row += gridDim.x * WARPS) {
   T *b = B + row + (size_t)c0 * ldb;
   T x0 = lane < n ? b[(size_t)lane * ldb] : T(0);
   T x1 = lane + 32 < n ? b[(size_t)(lane + 32) * ldb] : T(0);
@@ -107,6 +108,7 @@ __global__ void __launch_bounds__(WARPS * 32)
   }
   if (lane < n) b[(size_t)lane * ldb] = x0;
   if (lane + 32 < n) b[(size_t)(lane + 32) * ldb] = x1;
+  }
 }
 
 template <typename T>
@@ -129,6 +131,13 @@ static const T *opblk(const T *A, int lda, int ta, int r, int c) {
   return ta == kNoTrans ? A + r + (size_t)c * lda : A + c + (size_t)r * lda;
 }
 
+// CTAs of a diagonal-block solve over `count` columns (or rows): enough for
+// four CTAs per SM, each reusing its triangle over the rest.
+static int diag_grid(int count) {
+  const int need = (count + WARPS - 1) / WARPS, cap = 4 * ctx().num_sms;
+  return need < cap ? need : cap;
+}
+
 template <typename T>
 static void trsm_impl(int side, int uplo, int tA, int diag, int M, int N, T alpha, const T *A, int lda, T *B,
                       int ldb, cudaStream_t st) {
@@ -141,7 +150,7 @@ static void trsm_impl(int side, int uplo, int tA, int diag, int M, int N, T alph
   if (side == kLeft) {
     const bool lower = (uplo == kLower) != (ta != kNoTrans);
     const int nb = (M + TB - 1) / TB;
-    const dim3 grid((N + WARPS - 1) / WARPS);
+    const dim3 grid(diag_grid(N));
     for (int s = 0; s < nb; ++s) {
       const int b = lower ? s : nb - 1 - s;
       const int r0 = b * TB, n = (M - r0 < TB) ? M - r0 : TB;
@@ -157,7 +166,7 @@ static void trsm_impl(int side, int uplo, int tA, int diag, int M, int N, T alph
   } else {
     const bool upper = (uplo == kUpper) != (ta != kNoTrans);
     const int nb = (N + TB - 1) / TB;
-    const dim3 grid((M + WARPS - 1) / WARPS);
+    const dim3 grid(diag_grid(M));
     for (int s = 0; s < nb; ++s) {
       const int b = upper ? s : nb - 1 - s;
       const int c0 = b * TB, n = (N - c0 < TB) ? N - c0 : TB;
@@ -188,7 +197,7 @@ void dev_strsm(int side, int uplo, int ta, int diag, int M, int N, float alpha, 
 // generic driver's scaling).
 void dev_trsm_llnu_block(const double *A, int lda, int k, int n, double *B, int ldb, int ncols, cudaStream_t st) {
   if (n <= 0 || ncols <= 0) return;
-  const dim3 grid((ncols + WARPS - 1) / WARPS);
+  const dim3 grid(diag_grid(ncols));
   trsm_diag_left<double><<<grid, WARPS * 32, 0, st>>>(A + k + (size_t)k * lda, lda, kNoTrans, 1, 1, 0, n, ncols,
                                                        B, ldb);
       note_launch();
@@ -196,7 +205,7 @@ void dev_trsm_llnu_block(const double *A, int lda, int k, int n, double *B, int 
 }
 void dev_trsm_llnu_block(const float *A, int lda, int k, int n, float *B, int ldb, int ncols, cudaStream_t st) {
   if (n <= 0 || ncols <= 0) return;
-  const dim3 grid((ncols + WARPS - 1) / WARPS);
+  const dim3 grid(diag_grid(ncols));
   trsm_diag_left<float><<<grid, WARPS * 32, 0, st>>>(A + k + (size_t)k * lda, lda, kNoTrans, 1, 1, 0, n, ncols, B,
                                                       ldb);
       note_launch();
