@@ -648,7 +648,8 @@ def run_case(args):
             A.copy_(A0)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            L.atlg_dgetrf_split_dev(n, C.c_void_p(A.data_ptr()), n, C.c_void_p(piv.data_ptr()), 8, 1024, st)
+            L.atlg_dgetrf_split_dev(n, C.c_void_p(A.data_ptr()), n, C.c_void_p(piv.data_ptr()), 8,
+                                    args.k or 1024, st)
             torch.cuda.synchronize()
             ms = (time.perf_counter() - t0) * 1e3
     elif args.case == "trmm":
@@ -715,7 +716,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=8192)
-    ap.add_argument("--k", type=int, default=0, help="inner dimension of --case split (0: n)")
+    ap.add_argument("--k", type=int, default=0,
+                    help="inner dimension of --case split (0: n); outer block of --case splitlu (0: 1024)")
     ap.add_argument("--leaf", type=int, default=0, help="FP64 leaf width of --case splitlu (0: default)")
     ap.add_argument("--pw", type=int, default=0, help="FP64 LU panel width for --case splitlu/dgetrf (0: default)")
     ap.add_argument("--grid", type=int, default=0, help="grid-panel CTAs for --case splitlu/dgetrf (0: default)")
