@@ -170,6 +170,19 @@ __global__ void __launch_bounds__(256) slice_kernel(int R, int Kd, int Rp, int K
 
 // ------------------------------------------------------------ tensor cores
 
+// acc * 2^E as a double, built with integer operations only (GB300 runs
+// int->double conversion and FP64 multiplies on its narrow FP64 pipe, which
+// made them the cost of the recombination).  Valid when acc != 0 and the
+// result is a normal number; the caller checks the exponent range.
+__device__ __forceinline__ double int_times_pow2(int acc, int E) {
+  const unsigned a = acc < 0 ? 0u - (unsigned)acc : (unsigned)acc;
+  const int e2 = 31 - __clz(a);                                   // a = 1.f * 2^e2
+  const unsigned long long mant = ((unsigned long long)a << (52 - e2)) & 0xfffffffffffffull;
+  const unsigned long long bits = ((unsigned long long)(acc < 0) << 63) |
+                                  ((unsigned long long)(unsigned)(e2 + E + 1023) << 52) | mant;
+  return __longlong_as_double((long long)bits);
+}
+
 __device__ __forceinline__ bool wait_or_abort(uint64_t *bar, unsigned parity, volatile int *abort_flag) {
   for (unsigned i = 0; i < kMbarPollLimit; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
@@ -194,6 +207,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1)
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
   __shared__ double colscale[TN];
+  __shared__ int colexp[TN];
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // Tile order: CTAs launch in linear order; consecutive CTAs walk groups of
@@ -220,6 +234,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1)
   for (int c = threadIdx.x; c < TN; c += SPLIT_THREADS) {
     const int col = n0 + c;
     colscale[c] = (col < p.N) ? ldexp(1.0, p.exB[col]) : 0.0;
+    colexp[c] = (col < p.N) ? p.exB[col] : 0;
   }
   if (warp == 1) tmem_alloc(tmem_slot, 2 * TN);
   tc_fence_before();
@@ -335,10 +350,28 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1)
       const size_t ldc = (size_t)p.ldc;
       double *cp = p.C + gm + (size_t)(n0 + h * EPI_COLS) * ldc;
       const double *cs = colscale + h * EPI_COLS;
+      const int *ce = colexp + h * EPI_COLS;
+      // alpha = +-2^k: v = (acc * fr) * cs is acc * 2^(rE + eb) exactly while
+      // acc * fr and the result are normal numbers; then v is assembled from
+      // integers (same value), otherwise computed in FP64 as written
+      const int rE = rexp - kSliceBits * (d + 2) + p.alpha_exp;
+      const bool pow2 = p.alpha_pow2 != 0;
+      const bool aneg = p.alpha < 0.0;
+      auto term = [&](int c) -> double {
+        const int a = aneg ? -acc[c] : acc[c];
+        if (pow2) {
+          if (a == 0) return aneg ? -0.0 : 0.0;
+          const unsigned ua = a < 0 ? 0u - (unsigned)a : (unsigned)a;
+          const int e2 = 31 - __clz(ua);
+          const int e_mid = e2 + rE, e_out = e_mid + ce[c];
+          if (e_mid >= -1022 && e_mid <= 1023 && e_out >= -1022 && e_out <= 1023) return int_times_pow2(a, rE + ce[c]);
+        }
+        return (double)acc[c] * fr * cs[c];
+      };
       if (mode == 0) {
 #pragma unroll
         for (int c = 0; c < EPI_COLS; ++c) {
-          if (c < ncol) red_add_f64(cp, (double)acc[c] * fr * cs[c]);
+          if (c < ncol) red_add_f64(cp, term(c));
           cp += ldc;
           acc[c] = 0;
         }
@@ -350,7 +383,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1)
           for (int j = 0; j < 8; ++j) old[j] = (mode == 2 && c0 + j < ncol) ? cp[j * ldc] : 0.0;
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
-            const double v = (double)acc[c0 + j] * fr * cs[c0 + j];
+            const double v = term(c0 + j);
             if (c0 + j < ncol) cp[j * ldc] = (mode == 2) ? fma(p.beta, old[j], v) : v;
             acc[c0 + j] = 0;
           }
@@ -413,6 +446,12 @@ void dev_dgemm_split_run(const SplitPlan &plan, int t0, int t1, double alpha, do
   if (t0 >= t1) return;
   SplitArgs a = plan.a;
   a.alpha = alpha; a.beta = beta; a.C = C; a.ldc = ldc; a.nt0 = t0;
+  {
+    int e = 0;
+    const double m = frexp(alpha, &e);                // alpha = m 2^e, |m| in [0.5, 1)
+    a.alpha_pow2 = (m == 0.5 || m == -0.5) ? 1 : 0;
+    a.alpha_exp = e - 1;
+  }
   ATLG_CHECK(cudaFuncSetAttribute(ozaki_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPLIT_SMEM));
   ozaki_tc_kernel<<<dim3(a.Mp / TM, t1 - t0), SPLIT_THREADS, SPLIT_SMEM, st>>>(plan.tA, plan.tB, a);
   note_launch();

@@ -18,6 +18,7 @@ struct SplitArgs {
   int M, N, Mp, Np, Kp, s;
   int nt0;                 // first output column tile of a launch
   double alpha, beta;
+  int alpha_pow2, alpha_exp;   // alpha = +-2^alpha_exp exactly (integer-only scaling)
   double *C;
   int ldc;
   const int *exA, *exB;
