@@ -788,8 +788,8 @@ void dev_sgetrs_perm(int n, const float *LU, int lda, const int *perm, float *x,
   permute_vec_kernel<float><<<(n + 255) / 256, 256, 0, st>>>(n, perm, x, tmp);
   ATLG_CHECK(cudaMemcpyAsync(x, tmp, sizeof(float) * (size_t)n, cudaMemcpyDeviceToDevice, st));
   note_launch();
-  dev_strsv(kLower, kNoTrans, kUnit, n, LU, lda, x, st);
-  dev_strsv(kUpper, kNoTrans, kNonUnit, n, LU, lda, x, st);
+  dev_strsv_inv(kLower, kNoTrans, kUnit, n, LU, lda, x, st);
+  dev_strsv_inv(kUpper, kNoTrans, kNonUnit, n, LU, lda, x, st);
 }
 
 void dev_dlaswp(int N, double *A, int lda, int K1, int K2, const int *ipiv, int inci, int nrows, cudaStream_t st) {

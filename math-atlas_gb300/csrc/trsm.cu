@@ -228,11 +228,16 @@ __device__ unsigned g_trsv_status;
 constexpr int TV_B = 64;
 constexpr unsigned kFlagPollLimit = 1u << 24;
 
-template <typename T>
+// INV: the CTA inverts its diagonal block while it waits for the earlier
+// blocks (off the solve's critical path), and its block of x is then one
+// 64 x 64 product by the inverse instead of a 64-step substitution.
+template <typename T, bool INV>
 __global__ void __launch_bounds__(256)
     trsv_lookback_kernel(int n, const T *__restrict__ A, int lda, int ta, int lower, int unit, T *x, int *flags,
                          int *ticket) {
   __shared__ T tri[TV_B][TV_B + 1];
+  __shared__ T tinv[INV ? TV_B : 1][TV_B + 1];
+  __shared__ T ys[TV_B];
   __shared__ T rinv[TV_B];
   __shared__ T part[8][TV_B];
   __shared__ int s_b, s_fail;
@@ -254,6 +259,30 @@ __global__ void __launch_bounds__(256)
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nr; i += 256) rinv[i] = unit ? T(1) : T(1) / tri[i][i];
+  if (INV) {
+    __syncthreads();
+    // column j of the inverse of the (op) diagonal block, one thread per column
+    const int j = threadIdx.x;
+    if (j < TV_B) {
+      for (int i = 0; i < TV_B; ++i) tinv[i][j] = T(0);
+      if (j < nr) {
+        tinv[j][j] = rinv[j];
+        if (lower) {
+          for (int i = j + 1; i < nr; ++i) {
+            T s = T(0);
+            for (int k = j; k < i; ++k) s = fma(tri[i][k], tinv[k][j], s);
+            tinv[i][j] = -s * rinv[i];
+          }
+        } else {
+          for (int i = j - 1; i >= 0; --i) {
+            T s = T(0);
+            for (int k = i + 1; k <= j; ++k) s = fma(tri[i][k], tinv[k][j], s);
+            tinv[i][j] = -s * rinv[i];
+          }
+        }
+      }
+    }
+  }
   // contributions of earlier blocks: warp w takes columns k = c0 + w, w+8, ...
   T acc0 = T(0), acc1 = T(0);              // rows lane, lane+32 (op(A) = A)
   T accT[8];                               // rows w*8..w*8+7, lanes over k (op(A) = A^T)
@@ -320,6 +349,32 @@ __global__ void __launch_bounds__(256)
     }
   }
   __syncthreads();
+  if (INV) {
+    if (w == 0) {
+      T y0 = T(0), y1 = T(0);
+      if (ta == kNoTrans) {
+        for (int q = 0; q < 8; ++q) { y0 += part[q][lane]; y1 += part[q][lane + 32]; }
+      } else {
+        y0 = part[0][lane];
+        y1 = part[0][lane + 32];
+      }
+      ys[lane] = lane < nr ? x[r0 + lane] - y0 : T(0);
+      ys[lane + 32] = lane + 32 < nr ? x[r0 + lane + 32] - y1 : T(0);
+    }
+    __syncthreads();
+    // x_i = sum_k inv[i][k] ys[k]: four threads per row, 16 terms each
+    const int i = threadIdx.x >> 2, q = threadIdx.x & 3;
+    T s = T(0);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) s = fma(tinv[i][q * 16 + k], ys[q * 16 + k], s);
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    if (q == 0 && i < nr) x[r0 + i] = s;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) atomicExch(&flags[b], 1);
+    return;
+  }
   if (w == 0) {
     T y0 = T(0), y1 = T(0);
     if (ta == kNoTrans) {
@@ -357,14 +412,19 @@ __global__ void __launch_bounds__(256)
 
 // op(A) x = x for one right-hand side (incx = 1), cblas Uplo/Trans/Diag.
 template <typename T>
-static void trsv_impl(int uplo, int tA, int diag, int n, const T *A, int lda, T *x, cudaStream_t st) {
+static void trsv_impl(int uplo, int tA, int diag, int n, const T *A, int lda, T *x, cudaStream_t st,
+                      bool inv = false) {
   if (n <= 0) return;
   const int ta = (tA == kNoTrans) ? kNoTrans : kTrans;
   const int lower = ((uplo == kLower) != (ta != kNoTrans)) ? 1 : 0;
   const int nb = (n + TV_B - 1) / TV_B;
   int *w = static_cast<int *>(ctx().buffer(kBufV0, sizeof(int) * (size_t)(nb + 32)));
   ATLG_CHECK(cudaMemsetAsync(w, 0, sizeof(int) * (size_t)(nb + 32), st));
-  trsv_lookback_kernel<T><<<nb, 256, 0, st>>>(n, A, lda, ta, lower, diag == kUnit ? 1 : 0, x, w + 32, w);
+  if (inv && sizeof(T) == 4)   // FP32 only: the FP64 tiles would exceed static shared memory
+    trsv_lookback_kernel<T, sizeof(T) == 4><<<nb, 256, 0, st>>>(n, A, lda, ta, lower, diag == kUnit ? 1 : 0, x,
+                                                                w + 32, w);
+  else
+    trsv_lookback_kernel<T, false><<<nb, 256, 0, st>>>(n, A, lda, ta, lower, diag == kUnit ? 1 : 0, x, w + 32, w);
   note_launch();
   ATLG_CHECK(cudaGetLastError());
 }
@@ -374,6 +434,9 @@ void dev_dtrsv(int uplo, int ta, int diag, int n, const double *A, int lda, doub
 }
 void dev_strsv(int uplo, int ta, int diag, int n, const float *A, int lda, float *x, cudaStream_t st) {
   trsv_impl<float>(uplo, ta, diag, n, A, lda, x, st);
+}
+void dev_strsv_inv(int uplo, int ta, int diag, int n, const float *A, int lda, float *x, cudaStream_t st) {
+  trsv_impl<float>(uplo, ta, diag, n, A, lda, x, st, true);
 }
 
 unsigned trsv_status_read_and_clear() {

@@ -16,6 +16,10 @@ void dev_trsm_llnu_block(const float *A, int lda, int k, int n, float *B, int ld
 // op(A) x = x for one right-hand side, one launch (look-back over 64-row blocks).
 void dev_dtrsv(int uplo, int ta, int diag, int n, const double *A, int lda, double *x, cudaStream_t st);
 void dev_strsv(int uplo, int ta, int diag, int n, const float *A, int lda, float *x, cudaStream_t st);
+// dev_strsv whose 64 x 64 diagonal blocks are applied as inverses formed
+// while each block waits (for the mixed solver's FP32 refinement solves;
+// rounding differs from substitution)
+void dev_strsv_inv(int uplo, int ta, int diag, int n, const float *A, int lda, float *x, cudaStream_t st);
 unsigned trsv_status_read_and_clear();
 
 }  // namespace atlg
