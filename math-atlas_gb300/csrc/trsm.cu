@@ -410,6 +410,121 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The mixed solver's FP32 refinement solves (op(A) = A): as the INV form of
+// trsv_lookback_kernel, but a block publishes its piece of x as 64-bit words
+// (float value, call epoch) and a waiting CTA polls those words themselves,
+// so each value arrives with its signal -- one L2 round trip per block on the
+// solve's critical path instead of a flag and then the data.  Words from
+// earlier calls carry older epochs and are never taken.
+__global__ void __launch_bounds__(256)
+    trsv_tagged_kernel(int n, const float *__restrict__ A, int lda, int lower, int unit, float *x,
+                       unsigned long long *pub, unsigned epoch, int *ticket) {
+  __shared__ float tri[TV_B][TV_B + 1];
+  __shared__ float tinv[TV_B][TV_B + 1];
+  __shared__ float ys[TV_B], rinv[TV_B];
+  __shared__ float part[8][TV_B];
+  __shared__ float xs[2][TV_B];
+  __shared__ int s_b, s_fail;
+  const int nb = (n + TV_B - 1) / TV_B;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    const int t = atomicAdd(ticket, 1);
+    s_b = lower ? t : nb - 1 - t;
+    s_fail = 0;
+  }
+  __syncthreads();
+  const int b = s_b;
+  const int r0 = b * TV_B;
+  const int nr = (n - r0 < TV_B) ? n - r0 : TV_B;
+  for (int e = threadIdx.x; e < nr * nr; e += 256) {
+    const int i = e % nr, k = e / nr;
+    tri[i][k] = A[(r0 + i) + (size_t)(r0 + k) * lda];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nr; i += 256) rinv[i] = unit ? 1.0f : 1.0f / tri[i][i];
+  __syncthreads();
+  {   // inverse of the diagonal block, one thread per column, while earlier blocks solve
+    const int j = threadIdx.x;
+    if (j < TV_B) {
+      for (int i = 0; i < TV_B; ++i) tinv[i][j] = 0.0f;
+      if (j < nr) {
+        tinv[j][j] = rinv[j];
+        if (lower) {
+          for (int i = j + 1; i < nr; ++i) {
+            float s = 0.0f;
+            for (int k = j; k < i; ++k) s = fmaf(tri[i][k], tinv[k][j], s);
+            tinv[i][j] = -s * rinv[i];
+          }
+        } else {
+          for (int i = j - 1; i >= 0; --i) {
+            float s = 0.0f;
+            for (int k = i + 1; k <= j; ++k) s = fmaf(tri[i][k], tinv[k][j], s);
+            tinv[i][j] = -s * rinv[i];
+          }
+        }
+      }
+    }
+  }
+  const float rhs0 = (w == 0 && lane < nr) ? x[r0 + lane] : 0.0f;          // own block: not written by others
+  const float rhs1 = (w == 0 && lane + 32 < nr) ? x[r0 + lane + 32] : 0.0f;
+  float acc0 = 0.0f, acc1 = 0.0f;
+  for (int s = 0; s < nb - 1; ++s) {
+    const int c = lower ? s : nb - 1 - s;
+    if (lower ? c >= b : c <= b) break;
+    const int c0 = c * TV_B;
+    const int nc = (n - c0 < TV_B) ? n - c0 : TV_B;
+    const int par = s & 1;
+    float pa[16];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const int k = w + 8 * m;
+      const float *col = A + r0 + (size_t)(c0 + k) * lda;
+      pa[2 * m] = (k < nc && lane < nr) ? col[lane] : 0.0f;
+      pa[2 * m + 1] = (k < nc && lane + 32 < nr) ? col[lane + 32] : 0.0f;
+    }
+    if (threadIdx.x < nc) {
+      const volatile unsigned long long *src = pub + c0 + threadIdx.x;
+      unsigned i = 0;
+      unsigned long long v = *src;
+      while ((unsigned)(v >> 32) != epoch) {
+        if (++i > kFlagPollLimit) { atomicOr(&g_trsv_status, kErrGridTimeout); s_fail = 1; break; }
+        if (i > 32) __nanosleep(32);
+        v = *src;
+      }
+      xs[par][threadIdx.x] = __uint_as_float((unsigned)(v & 0xffffffffull));
+    }
+    __syncthreads();
+    if (s_fail) return;
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const int k = w + 8 * m;
+      const float xk = (k < nc) ? xs[par][k] : 0.0f;
+      acc0 = fmaf(pa[2 * m], xk, acc0);
+      acc1 = fmaf(pa[2 * m + 1], xk, acc1);
+    }
+  }
+  part[w][lane] = acc0;
+  part[w][lane + 32] = acc1;
+  __syncthreads();
+  if (w == 0) {
+    float y0 = 0.0f, y1 = 0.0f;
+    for (int q = 0; q < 8; ++q) { y0 += part[q][lane]; y1 += part[q][lane + 32]; }
+    ys[lane] = lane < nr ? rhs0 - y0 : 0.0f;
+    ys[lane + 32] = lane + 32 < nr ? rhs1 - y1 : 0.0f;
+  }
+  __syncthreads();
+  const int i = threadIdx.x >> 2, q = threadIdx.x & 3;
+  float s = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) s = fmaf(tinv[i][q * 16 + k], ys[q * 16 + k], s);
+  s += __shfl_xor_sync(0xffffffffu, s, 1);
+  s += __shfl_xor_sync(0xffffffffu, s, 2);
+  if (q == 0 && i < nr) {
+    x[r0 + i] = s;
+    pub[r0 + i] = ((unsigned long long)epoch << 32) | (unsigned long long)__float_as_uint(s);
+  }
+}
+
 // op(A) x = x for one right-hand side (incx = 1), cblas Uplo/Trans/Diag.
 template <typename T>
 static void trsv_impl(int uplo, int tA, int diag, int n, const T *A, int lda, T *x, cudaStream_t st,
@@ -436,7 +551,31 @@ void dev_strsv(int uplo, int ta, int diag, int n, const float *A, int lda, float
   trsv_impl<float>(uplo, ta, diag, n, A, lda, x, st);
 }
 void dev_strsv_inv(int uplo, int ta, int diag, int n, const float *A, int lda, float *x, cudaStream_t st) {
-  trsv_impl<float>(uplo, ta, diag, n, A, lda, x, st, true);
+  if (n <= 0) return;
+  if (ta != kNoTrans) {
+    trsv_impl<float>(uplo, ta, diag, n, A, lda, x, st, true);
+    return;
+  }
+  // published words: zeroed whenever the buffer is new, epochs from 1
+  static unsigned long long *s_pub = nullptr;
+  static size_t s_len = 0;
+  static unsigned s_epoch = 0;
+  const int nb = (n + TV_B - 1) / TV_B;
+  int *tk = static_cast<int *>(ctx().buffer(kBufV0, sizeof(int) * (size_t)(nb + 32)));
+  unsigned long long *pub =
+      static_cast<unsigned long long *>(ctx().buffer(kBufV2, sizeof(unsigned long long) * (size_t)n));
+  if (pub != s_pub || (size_t)n > s_len || s_epoch == 0xffffffffu) {
+    ATLG_CHECK(cudaMemsetAsync(pub, 0, sizeof(unsigned long long) * (size_t)n, st));
+    s_pub = pub;
+    s_len = (size_t)n > s_len ? (size_t)n : s_len;
+    s_epoch = 0;
+  }
+  ++s_epoch;
+  ATLG_CHECK(cudaMemsetAsync(tk, 0, sizeof(int), st));
+  trsv_tagged_kernel<<<nb, 256, 0, st>>>(n, A, lda, uplo == kLower ? 1 : 0, diag == kUnit ? 1 : 0, x, pub, s_epoch,
+                                         tk);
+  note_launch();
+  ATLG_CHECK(cudaGetLastError());
 }
 
 unsigned trsv_status_read_and_clear() {
