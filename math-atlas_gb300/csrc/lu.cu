@@ -701,21 +701,27 @@ __global__ void __launch_bounds__(256)
 // laswp as one permutation: laswp_perm_kernel runs the interchange sequence
 // K1..K2-1 (reversed when inci < 0) on a row-content table held in shared
 // memory (global memory above kPermSmemRows rows), then the rows are moved
-// with one gather into scratch and one copy back.
+// by laswp_cols_kernel (or, for tables too large for shared memory, by one
+// gather into scratch and one copy back).  use_smem = 2 also stages the
+// K2-K1 pivots in shared memory first, so the one-thread interchange chain
+// runs on shared-memory operands only (no L2 round trip per interchange).
 constexpr int kPermSmemRows = 48 * 1024;
 
 __global__ void laswp_perm_kernel(const int *ipiv, int K1, int K2, int inci, int *content_g, int nrows,
                                   int use_smem) {
   extern __shared__ int content_s[];
   int *content = use_smem ? content_s : content_g;
+  int *piv_s = content_s + nrows;
+  const int n = K2 - K1;
+  const int step = inci > 0 ? inci : -inci;
   for (int i = threadIdx.x; i < nrows; i += blockDim.x) content[i] = i;
+  if (use_smem == 2)
+    for (int s = threadIdx.x; s < n; s += blockDim.x) piv_s[s] = ipiv[(size_t)(K1 + s) * step];
   __syncthreads();
   if (threadIdx.x == 0) {
-    const int n = K2 - K1;
-    const int step = inci > 0 ? inci : -inci;
     for (int s = 0; s < n; ++s) {
       const int i = inci > 0 ? K1 + s : K2 - 1 - s;
-      const int ip = ipiv[(size_t)i * step];
+      const int ip = use_smem == 2 ? piv_s[i - K1] : ipiv[(size_t)i * step];
       if (ip == i || ip < 0 || ip >= nrows) continue;
       const int t = content[i];
       content[i] = content[ip];
@@ -748,6 +754,121 @@ static int grid_for(long work) {
   return (int)b;
 }
 
+// laswp_cols_kernel applies the row permutation `content` (row r <- row
+// content[r], rows [0, nrows)) to N columns of A with the rows of a column
+// held in shared memory: one read of what moves and one write, no scratch
+// copy of A.  Every CTA loads the table, counts the rows that move (mv) and
+// the span [lo, hi) they cover, then per column
+//   dense  (4*mv >= span): rows [lo, hi) read with coalesced loads into
+//          shared memory, only the moved rows written back;
+//   sparse (a few rows moving in a tall column, as for the interchanges of
+//          one block column): a compact (destination, source) list, only the
+//          source rows read, for G columns at a time.
+// Algorithmic bytes per column: 2 * sizeof(T) * mv (each moved element read
+// and written once); the dense form also reads the unmoved rows of the span.
+constexpr int kLcThreads = 1024;
+constexpr size_t kLaswpColsSmemMax = 200 * 1024;
+
+__host__ __device__ inline size_t laswp_cols_table_bytes(int nrows) {
+  return ((size_t)nrows * sizeof(int) + 15) & ~size_t(15);
+}
+template <typename T>
+inline size_t laswp_cols_smem(int nrows) {
+  return laswp_cols_table_bytes(nrows) + (size_t)nrows * sizeof(T);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kLcThreads)
+    laswp_cols_kernel(T *A, int lda, const int *__restrict__ content_g, int nrows, int N) {
+  extern __shared__ __align__(16) unsigned char lc_smem[];
+  int *content = reinterpret_cast<int *>(lc_smem);
+  unsigned char *buf = lc_smem + laswp_cols_table_bytes(nrows);
+  const size_t buf_bytes = (size_t)nrows * sizeof(T);
+  __shared__ int s_lo, s_hi, s_mv, s_cnt;
+  const int tid = threadIdx.x, lane = tid & 31;
+  if (tid == 0) { s_lo = nrows; s_hi = 0; s_mv = 0; s_cnt = 0; }
+  __syncthreads();
+  int lo = nrows, hi = 0, mv = 0;
+  for (int r = tid; r < nrows; r += kLcThreads) {
+    const int s = content_g[r];
+    content[r] = s;
+    if (s != r) { lo = min(lo, r); hi = max(hi, r + 1); ++mv; }
+  }
+  lo = __reduce_min_sync(0xffffffffu, lo);
+  hi = __reduce_max_sync(0xffffffffu, hi);
+  mv = __reduce_add_sync(0xffffffffu, mv);
+  if (lane == 0) { atomicMin(&s_lo, lo); atomicMax(&s_hi, hi); atomicAdd(&s_mv, mv); }
+  __syncthreads();
+  lo = s_lo; hi = s_hi; mv = s_mv;
+  if (mv == 0) return;
+  if (4 * (long)mv >= (long)(hi - lo)) {
+    T *col = reinterpret_cast<T *>(buf);
+    constexpr int U = 8;
+    for (int c = blockIdx.x; c < N; c += gridDim.x) {
+      T *colp = A + (size_t)c * lda;
+      for (int b = lo + tid; b < hi; b += U * kLcThreads) {
+        T v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int r = b + u * kLcThreads;
+          v[u] = r < hi ? colp[r] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int r = b + u * kLcThreads;
+          if (r < hi) col[r] = v[u];
+        }
+      }
+      __syncthreads();
+      for (int r = lo + tid; r < hi; r += kLcThreads) {
+        const int s = content[r];
+        if (s != r) colp[r] = col[s];
+      }
+      __syncthreads();
+    }
+    return;
+  }
+  // sparse: compact (destination, source) pairs, warp-aggregated
+  int2 *pr = reinterpret_cast<int2 *>(buf);
+  for (int r0 = lo + (tid & ~31); r0 < hi; r0 += kLcThreads) {
+    const int r = r0 + lane;
+    const int s = r < hi ? content[r] : r;
+    const bool moves = r < hi && s != r;
+    const unsigned m = __ballot_sync(0xffffffffu, moves);
+    int base = 0;
+    if (lane == 0 && m) base = atomicAdd(&s_cnt, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (moves) pr[base + __popc(m & ((1u << lane) - 1u))] = make_int2(r, s);
+  }
+  __syncthreads();
+  const size_t pair_bytes = ((size_t)mv * sizeof(int2) + 15) & ~size_t(15);
+  T *vals = reinterpret_cast<T *>(buf + pair_bytes);
+  int G = (int)((buf_bytes - pair_bytes) / ((size_t)mv * sizeof(T)));
+  G = G < 1 ? 1 : (G > 8 ? 8 : G);
+  for (int c0 = blockIdx.x * G; c0 < N; c0 += gridDim.x * G) {
+    const int gc = (N - c0 < G) ? N - c0 : G;
+    for (int e = tid; e < gc * mv; e += kLcThreads) {
+      const int g = e / mv, k = e - g * mv;
+      vals[e] = A[pr[k].y + (size_t)(c0 + g) * lda];
+    }
+    __syncthreads();
+    for (int e = tid; e < gc * mv; e += kLcThreads) {
+      const int g = e / mv, k = e - g * mv;
+      A[pr[k].x + (size_t)(c0 + g) * lda] = vals[e];
+    }
+    __syncthreads();
+  }
+}
+
+// Shared-memory form of the interchange chain for n interchanges on nrows rows.
+static int perm_smem_mode(int nrows, int n) {
+  if ((long)nrows + n <= kPermSmemRows) return 2;
+  return nrows <= kPermSmemRows ? 1 : 0;
+}
+static size_t perm_smem_bytes(int mode, int nrows, int n) {
+  return mode == 2 ? sizeof(int) * ((size_t)nrows + n) : mode == 1 ? sizeof(int) * (size_t)nrows : 0;
+}
+
 // The rows that can move are [0, nrows); nrows must exceed every pivot.
 template <typename T>
 static void laswp_impl(int N, T *A, int lda, int K1, int K2, const int *ipiv, int inci, int nrows,
@@ -755,14 +876,27 @@ static void laswp_impl(int N, T *A, int lda, int K1, int K2, const int *ipiv, in
   if (K2 <= K1 || N <= 0 || nrows <= 0) return;
   Context &c = ctx();
   int *content = static_cast<int *>(c.buffer(kBufW3, sizeof(int) * (size_t)nrows));
-  T *W = static_cast<T *>(c.buffer(kBufW4, sizeof(T) * (size_t)nrows * N));
-  const int use_smem = nrows <= kPermSmemRows;
-  const size_t smem = use_smem ? sizeof(int) * (size_t)nrows : 0;
+  const int mode = perm_smem_mode(nrows, K2 - K1);
   ATLG_CHECK(cudaFuncSetAttribute(laswp_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  laswp_perm_kernel<<<1, 1024, smem, st>>>(ipiv, K1, K2, inci, content, nrows, use_smem);
-  gather_rows_kernel<T><<<grid_for((long)nrows * N), 256, 0, st>>>(A, lda, W, nrows, content, nrows, N);
-  copy_rows_kernel<T><<<grid_for((long)nrows * N), 256, 0, st>>>(A, lda, W, nrows, nrows, N);
-  note_launch(3);
+  laswp_perm_kernel<<<1, 1024, perm_smem_bytes(mode, nrows, K2 - K1), st>>>(ipiv, K1, K2, inci, content, nrows,
+                                                                             mode);
+  const size_t csmem = laswp_cols_smem<T>(nrows);
+  if (csmem <= kLaswpColsSmemMax) {
+    ATLG_CHECK(cudaFuncSetAttribute(laswp_cols_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kLaswpColsSmemMax));
+    int per_sm = 0;
+    ATLG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, laswp_cols_kernel<T>, kLcThreads, csmem));
+    if (per_sm < 1) per_sm = 1;
+    const long cap = (long)per_sm * c.num_sms;
+    const int grid = (int)(N < cap ? N : cap);
+    laswp_cols_kernel<T><<<grid, kLcThreads, csmem, st>>>(A, lda, content, nrows, N);
+    note_launch(2);
+  } else {
+    T *W = static_cast<T *>(c.buffer(kBufW4, sizeof(T) * (size_t)nrows * N));
+    gather_rows_kernel<T><<<grid_for((long)nrows * N), 256, 0, st>>>(A, lda, W, nrows, content, nrows, N);
+    copy_rows_kernel<T><<<grid_for((long)nrows * N), 256, 0, st>>>(A, lda, W, nrows, nrows, N);
+    note_launch(3);
+  }
   ATLG_CHECK(cudaGetLastError());
 }
 
@@ -770,9 +904,9 @@ static void laswp_impl(int N, T *A, int lda, int K1, int K2, const int *ipiv, in
 // the interchanges ipiv[0..n) are applied in order (ATL_laswp forward), so
 // that the forward interchange of one vector is y[i] = b[perm[i]].
 void dev_perm_from_ipiv(const int *ipiv, int n, int *perm, cudaStream_t st) {
-  const int use_smem = n <= kPermSmemRows;
+  const int mode = perm_smem_mode(n, n);
   ATLG_CHECK(cudaFuncSetAttribute(laswp_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  laswp_perm_kernel<<<1, 1024, use_smem ? sizeof(int) * (size_t)n : 0, st>>>(ipiv, 0, n, 1, perm, n, use_smem);
+  laswp_perm_kernel<<<1, 1024, perm_smem_bytes(mode, n, n), st>>>(ipiv, 0, n, 1, perm, n, mode);
   note_launch();
   ATLG_CHECK(cudaGetLastError());
 }
