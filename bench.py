@@ -411,6 +411,95 @@ def measure_next(G, O, torch, n=16384):
     return out
 
 
+def laswp_moved_rows(piv, K1, K2, nrows):
+    """Rows whose content changes under the interchanges piv[K1:K2] (forward)."""
+    content = np.arange(nrows)
+    for i in range(K1, K2):
+        ip = int(piv[i])
+        if ip != i:
+            content[i], content[ip] = content[ip], content[i]
+    return int((content != np.arange(nrows)).sum())
+
+
+def measure_memory(G, O, torch, reps=5):
+    """The HBM-bound rows: ATL_laswp row interchanges and the iamax pivot
+    search, achieved GB/s of algorithmic bytes against the measured copy
+    bandwidth.  laswp: 2*8*N bytes per moved row (each moved element read
+    and written once); iamax: 8 bytes per element.  CUDA events on the
+    library stream around each call, best of `reps` after one warm-up; the
+    inputs are larger than L2."""
+    import ctypes as C
+    L = G.lib()
+    st = L.atlg_stream()
+    s = torch.cuda.ExternalStream(st)
+    peak = load_peaks().get("hbm_gbs") or 6800.0
+    out = {}
+
+    def timed(fn):
+        ts = []
+        for rep in range(reps + 1):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            fn()
+            e1.record(s)
+            torch.cuda.synchronize()
+            if rep:
+                ts.append(e0.elapsed_time(e1))
+        return min(ts)
+
+    rng = np.random.default_rng(31)
+    # dense: the interchanges of a full LU of n = 8192 on all 8192 columns
+    # (a random pivot vector ipiv[i] >= i, as partial pivoting produces)
+    for (m, N, K1, K2, name) in ((8192, 8192, 0, 8192, "dlaswp_lu_n8192"),
+                                 (16384, 15360, 0, 1024, "dlaswp_block_column_n16384")):
+        piv = np.arange(m, dtype=np.int32)
+        piv[K1:K2] = [rng.integers(i, m) for i in range(K1, K2)]
+        mv = laswp_moved_rows(piv, K1, K2, m)
+        A = torch.rand(N, m, device="cuda", dtype=torch.float64)        # column-major m x N
+        dpiv = torch.from_numpy(piv).cuda()
+        ms = timed(lambda: L.atlg_dlaswp_dev(N, A.data_ptr(), m, K1, K2, dpiv.data_ptr(), 1, m, st))
+        alg = 16.0 * mv * N
+        gbs = alg / (ms * 1e-3) / 1e9
+        row = {"rows": m, "columns": N, "interchanges": K2 - K1, "moved_rows": mv, "ms": ms,
+               "algorithmic_bytes": alg, "gbs": gbs, "peak_gbs": peak, "frac": gbs / peak,
+               "timing": "CUDA events on the library stream around atlg_dlaswp_dev (interchange-chain "
+                         "kernel + column kernel), best of %d after one warm-up" % reps}
+        mc, Nc = 2048, 2048
+        Ah = np.asfortranarray(rng.random((mc, Nc)))
+        pc = np.array([rng.integers(i, mc) for i in range(mc)], dtype=np.int32)
+        t0 = time.perf_counter()
+        O.laswp(Nc, Ah, 0, mc, pc, 1)
+        tc = time.perf_counter() - t0
+        row["cpu_baseline"] = {"value": 16.0 * laswp_moved_rows(pc, 0, mc, mc) * Nc / tc / 1e9, "unit": "GB/s",
+                               "cores": 1, "kind": "port",
+                               "sample": f"oracle laswp {mc} x {Nc}, full pivot vector (32-column blocks)"}
+        out[name] = row
+        del A
+    torch.cuda.empty_cache()
+    # iamax over 2^27 doubles (1 GiB) and one pivot-column-sized call
+    res = torch.zeros(1, dtype=torch.int32, device="cuda")
+    for (n, name) in (((1 << 27), "idamax_n134217728"), (8192, "idamax_n8192")):
+        x = torch.randn(n, device="cuda", dtype=torch.float64)
+        ms = timed(lambda: L.atlg_idamax_dev(n, x.data_ptr(), 1, res.data_ptr(), st))
+        gbs = 8.0 * n / (ms * 1e-3) / 1e9
+        ok = int(res.item()) == int(torch.argmax(x.abs()).item())
+        out[name] = {"n": n, "ms": ms, "gbs": gbs, "peak_gbs": peak, "frac": gbs / peak,
+                     "matches_first_argmax": ok,
+                     "timing": "CUDA events on the library stream around atlg_idamax_dev, best of %d" % reps}
+        del x
+    nc = 1 << 24
+    xh = rng.standard_normal(nc)
+    t0 = time.perf_counter()
+    O.cblas_iamax(nc, xh, 1)
+    tc = time.perf_counter() - t0
+    out["idamax_n134217728"]["cpu_baseline"] = {
+        "value": 8.0 * nc / tc / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+        "sample": f"oracle cblas_iamax (ATL_iamax comparison sequence) on {nc} doubles"}
+    torch.cuda.empty_cache()
+    return out
+
+
 # ------------------------------------------------------------------ GPU side
 def run_gpu(args):
     import torch
@@ -538,6 +627,7 @@ def run_gpu(args):
         if world == 1 and not args.skip_extras:
             forms = measure_forms(G, O, torch)
             nxt = measure_next(G, O, torch)
+            nxt.update(measure_memory(G, O, torch))
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
@@ -576,6 +666,8 @@ def run_case(args):
     trmm   -- FP64 TRMM Left/Upper/NoTrans at M = N = n
     getri  -- FP64 inverse from the dgetrf factors at n
     splitlu -- FP64 LU with split-DGEMM (tensor-core) trailing updates at n
+    laswp  -- ATL_laswp of a full random pivot vector on an n x n matrix (--k: first k interchanges)
+    idamax -- cblas_idamax over n doubles
     Prints one JSON line with the device time of the last run."""
     import ctypes as C
     import torch
@@ -604,6 +696,38 @@ def run_case(args):
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1)
         print(json.dumps({"case": "split", "n": n, "k": k, "ms": ms, "tflops_fp64_equiv": 2.0 * n * n * k / ms / 1e9}))
+    elif args.case == "laswp":
+        # full pivot vector on an n x n matrix (--k > 0: only the first k interchanges)
+        K2 = args.k or n
+        rng = np.random.default_rng(31)
+        piv = np.arange(n, dtype=np.int32)
+        piv[:K2] = [rng.integers(i, n) for i in range(K2)]
+        A = torch.rand(n, n, device="cuda", dtype=torch.float64, generator=g)
+        dpiv = torch.from_numpy(piv).cuda()
+        torch.cuda.synchronize()
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            L.atlg_dlaswp_dev(n, A.data_ptr(), n, 0, K2, dpiv.data_ptr(), 1, n, st)
+            e1.record(s)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+        mv = laswp_moved_rows(piv, 0, K2, n)
+        print(json.dumps({"case": "laswp", "n": n, "interchanges": K2, "moved_rows": mv, "ms": ms,
+                          "gbs": 16.0 * mv * n / (ms * 1e-3) / 1e9}))
+    elif args.case == "idamax":
+        x = torch.randn(n, device="cuda", dtype=torch.float64, generator=g)
+        res = torch.zeros(1, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            L.atlg_idamax_dev(n, x.data_ptr(), 1, res.data_ptr(), st)
+            e1.record(s)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+        print(json.dumps({"case": "idamax", "n": n, "ms": ms, "gbs": 8.0 * n / (ms * 1e-3) / 1e9,
+                          "index": int(res.item())}))
     elif args.case == "sgetrf":
         S = torch.randn(n, n, device="cuda", dtype=torch.float32, generator=g)
         piv = torch.zeros(n, dtype=torch.int32, device="cuda")
@@ -722,7 +846,8 @@ def main():
     ap.add_argument("--pw", type=int, default=0, help="FP64 LU panel width for --case splitlu/dgetrf (0: default)")
     ap.add_argument("--grid", type=int, default=0, help="grid-panel CTAs for --case splitlu/dgetrf (0: default)")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
-    ap.add_argument("--case", choices=["split", "sgetrf", "dgetrf", "mixed", "potrf", "trmm", "getri", "splitlu"], default=None,
+    ap.add_argument("--case", choices=["split", "sgetrf", "dgetrf", "mixed", "potrf", "trmm", "getri", "splitlu",
+                                       "laswp", "idamax"], default=None,
                     help="run one kernel workload for a profiling capture instead of the benchmark")
     ap.add_argument("--skip-extras", action="store_true",
                     help="omit the n=16384 mixed-dgesv and split-DGEMM measurements")

@@ -82,6 +82,12 @@ void cblas_strmm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side,
                  const enum CBLAS_DIAG Diag, const int M, const int N, const float alpha,
                  const float *A, const int lda, float *B, const int ldb);
 
+/* ---- Level 1: AtlasBase/Clint/cblas-lvl1.base:408-420 (I?AMAX, CBLAS_INDEX = int):
+ * 0-based index of the first element of largest magnitude, ATL_i?amax's
+ * comparison sequence (AtlasBase/Clint/atlas-lvl1.base:1148-1340) including
+ * its NaN behaviour; 0 when N < 2 or incX <= 0. */
+int cblas_idamax(const int N, const double *X, const int incX);
+int cblas_isamax(const int N, const float *X, const int incX);
 /* ---- Level 2: AtlasBase/Clint/cblas-lvl2.base:21-93 (GEMV, d and s) */
 void cblas_dgemv(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TA, const int M,
                  const int N, const double alpha, const double *A, const int lda,
@@ -221,6 +227,12 @@ int atlg_sgemm_dev(int TA, int TB, int M, int N, int K, float alpha, const float
                    const float *B, int ldb, float beta, float *C, int ldc, void *stream);
 int atlg_dtrsm_dev(int Side, int Uplo, int TA, int Diag, int M, int N, double alpha,
                    const double *A, int lda, double *B, int ldb, void *stream);
+/* cblas_i?amax on device data (AtlasBase/Clint/cblas-lvl1.base:408): the
+ * 0-based index is written to the device int *result.  Returns 0, -1 for
+ * N < 0.  Calls whose work overlaps on the GPU (different streams) race on
+ * the search's completion counter: serialise them. */
+int atlg_idamax_dev(int N, const double *X, int incX, int *result, void *stream);
+int atlg_isamax_dev(int N, const float *X, int incX, int *result, void *stream);
 /* ATL_laswp semantics (AtlasBase/Clint/atlas-lp.base:1053); rows [0,nrows) may move */
 int atlg_dlaswp_dev(int N, double *A, int lda, int K1, int K2, const int *ipiv, int inci,
                     int nrows, void *stream);

@@ -35,6 +35,7 @@ EXPORTS = [
     "atlg_dtrmm_dev", "atlg_dgemv_dev", "atlg_dtrsv_dev",
     "clapack_dtrtri", "clapack_strtri", "clapack_dgetri", "clapack_sgetri", "atlg_dtrtri_dev", "atlg_dgetri_dev",
     "atlg_panel_cluster", "dgesv_split", "atlg_dgetrf_split_dev", "atlg_panel_grid", "atlg_split_lu_leaf", "atlg_panel_width",
+    "cblas_idamax", "cblas_isamax", "atlg_idamax_dev", "atlg_isamax_dev",
 ]
 
 _lib = None
@@ -114,6 +115,10 @@ def _declare(L):
         "atlg_sgemm_dev": (_i, [_i, _i, _i, _i, _i, _f, _v, _i, _v, _i, _f, _v, _i, _v]),
         "atlg_dtrsm_dev": (_i, [_i, _i, _i, _i, _i, _i, _d, _v, _i, _v, _i, _v]),
         "atlg_dlaswp_dev": (_i, [_i, _v, _i, _i, _i, _v, _i, _i, _v]),
+        "cblas_idamax": (_i, [_i, _v1d, _i]),
+        "cblas_isamax": (_i, [_i, _v1s, _i]),
+        "atlg_idamax_dev": (_i, [_i, _v, _i, _v, _v]),
+        "atlg_isamax_dev": (_i, [_i, _v, _i, _v, _v]),
         "atlg_dlaswp_noalloc": (_i, [_i, _v, _i, _i, _i, _v, _i, _i, _v]),
         "atlg_dgetrf_dev": (_i, [_i, _i, _v, _i, _v, _v, _v]),
         "atlg_sgetrf_dev": (_i, [_i, _i, _v, _i, _v, _v, _v]),
@@ -187,6 +192,14 @@ def cblas_dtrmm(order, side, uplo, ta, diag, M, N, alpha, A, lda, B, ldb):
 
 def cblas_strmm(order, side, uplo, ta, diag, M, N, alpha, A, lda, B, ldb):
     lib().cblas_strmm(order, side, uplo, ta, diag, M, N, alpha, A, lda, B, ldb)
+
+
+def cblas_idamax(N, X, incx):
+    return int(lib().cblas_idamax(N, np.ascontiguousarray(X, dtype=np.float64), incx))
+
+
+def cblas_isamax(N, X, incx):
+    return int(lib().cblas_isamax(N, np.ascontiguousarray(X, dtype=np.float32), incx))
 
 
 def cblas_dgemv(order, ta, M, N, alpha, A, lda, X, incx, beta, Y, incy):

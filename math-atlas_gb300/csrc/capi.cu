@@ -27,6 +27,7 @@
 #include "chol.cuh"
 #include "gemm.cuh"
 #include "getri.cuh"
+#include "iamax.cuh"
 #include "lu.cuh"
 #include "lu_split.cuh"
 #include "mixed.cuh"
@@ -583,6 +584,44 @@ void vec_unpack(const std::vector<T> &v, T *X, int n, int inc) {
   for (int i = 0; i < n; ++i) X[inc > 0 ? (size_t)i * inc : (size_t)(n - 1 - i) * (size_t)(-inc)] = v[i];
 }
 
+// cblas_i?amax (AtlasBase/Clint/cblas-lvl1.base:408-420): ATL_i?amax when
+// N > 0 and incX > 0, else 0; ATL_i?amax itself returns 0 for N < 2.  A
+// strided vector is packed on the host and searched with the strided form's
+// final rule (no zero-magnitude check, atlas-lvl1.base:1318-1340).
+template <typename T>
+int host_iamax(int N, const T *X, int incX) {
+  if (N < 2 || incX <= 0) return 0;
+  cudaStream_t st = ctx().stream;
+  std::vector<T> hx;
+  const T *src = X;
+  if (incX != 1) {
+    vec_pack(hx, X, N, incX);
+    src = hx.data();
+  }
+  T *dx = static_cast<T *>(ctx().buffer(kBufB, sizeof(T) * (size_t)N));
+  int *dres = static_cast<int *>(ctx().buffer(kBufInfo, sizeof(int)));
+  ATLG_CHECK(cudaMemcpyAsync(dx, src, sizeof(T) * (size_t)N, cudaMemcpyHostToDevice, st));
+  if (sizeof(T) == 8) dev_idamax(N, (const double *)dx, 1, incX == 1, dres, st);
+  else dev_isamax(N, (const float *)dx, 1, incX == 1, dres, st);
+  int res = 0;
+  ATLG_CHECK(cudaMemcpyAsync(&res, dres, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  return res;
+}
+
+template <typename T>
+int iamax_dev(int N, const T *X, int incX, int *result, void *stream) {
+  if (N < 0) return -1;
+  cudaStream_t st = stream_of(stream);
+  if (N < 2 || incX <= 0) {
+    ATLG_CHECK(cudaMemsetAsync(result, 0, sizeof(int), st));
+    return 0;
+  }
+  if (sizeof(T) == 8) dev_idamax(N, (const double *)X, incX, incX == 1, result, st);
+  else dev_isamax(N, (const float *)X, incX, incX == 1, result, st);
+  return 0;
+}
+
 template <typename T>
 void host_gemv(const char *rout, int Order, int TA, int M, int N, T alpha, const T *A, int lda, const T *X, int incX,
                T beta, T *Y, int incY) {
@@ -839,6 +878,8 @@ void cblas_strmm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side, const
                  const float alpha, const float *A, const int lda, float *B, const int ldb) {
   host_trmm<float>("cblas_strmm", Order, Side, Uplo, TA, Diag, M, N, alpha, A, lda, B, ldb);
 }
+int cblas_idamax(const int N, const double *X, const int incX) { return host_iamax<double>(N, X, incX); }
+int cblas_isamax(const int N, const float *X, const int incX) { return host_iamax<float>(N, X, incX); }
 void cblas_dgemv(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TA, const int M, const int N,
                  const double alpha, const double *A, const int lda, const double *X, const int incX,
                  const double beta, double *Y, const int incY) {
@@ -1099,6 +1140,12 @@ int atlg_dtrsm_dev(int Side, int Uplo, int TA, int Diag, int M, int N, double al
 int atlg_dlaswp_dev(int N, double *A, int lda, int K1, int K2, const int *ipiv, int inci, int nrows, void *stream) {
   dev_dlaswp(N, A, lda, K1, K2, ipiv, inci, nrows, stream_of(stream));
   return 0;
+}
+int atlg_idamax_dev(int N, const double *X, int incX, int *result, void *stream) {
+  return iamax_dev<double>(N, X, incX, result, stream);
+}
+int atlg_isamax_dev(int N, const float *X, int incX, int *result, void *stream) {
+  return iamax_dev<float>(N, X, incX, result, stream);
 }
 void atlg_panel_cluster(int on) { set_panel_cluster(on != 0); }
 void atlg_panel_grid(int ctas) { set_panel_grid(ctas); }

@@ -71,6 +71,9 @@ int  ora_idamax(int N, const double *X, int incX);
 int  ora_isamax(int N, const float *X, int incX);
 
 /* --- LAPACK LU path (AtlasBase/Clint/atlas-lp.base:1053-1717, 5204) --- */
+/* cblas_i?amax: ATL_i?amax's comparison sequence, NaNs included */
+int ora_dcblas_iamax(int N, const double *X, int incX);
+int ora_scblas_iamax(int N, const float *X, int incX);
 void ora_dlaswp(int N, double *A, int lda, int K1, int K2, const int *ipiv,
                 int inci);
 void ora_slaswp(int N, float *A, int lda, int K1, int K2, const int *ipiv,

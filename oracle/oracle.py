@@ -67,6 +67,8 @@ def _declare(L):
         "ora_strsm": (None, [_i, _i, _i, _i, _i, _i, _f, _sp, _i, _sp, _i]),
         "ora_dcblas_trsm": (None, [_i, _i, _i, _i, _i, _i, _i, _d, _dp, _i, _dp, _i]),
         "ora_idamax": (_i, [_i, _dp, _i]),
+        "ora_dcblas_iamax": (_i, [_i, _dp, _i]),
+        "ora_scblas_iamax": (_i, [_i, _sp, _i]),
         "ora_dlaswp": (None, [_i, _dp, _i, _i, _i, _ip, _i]),
         "ora_slaswp": (None, [_i, _sp, _i, _i, _i, _ip, _i]),
         "ora_set_lu_params": (None, [_l, _i]),
@@ -200,6 +202,13 @@ def potrs(A, B, uplo=Lower, N=None, order=ColMajor):
     nrhs = B.shape[1]
     f(order, uplo, N, nrhs, A, A.shape[0], B, B.shape[0])
     return B
+
+
+def cblas_iamax(N, X, incX):
+    """cblas_i?amax on a 1-D array (ATL_i?amax semantics, NaNs included)."""
+    X = np.asfortranarray(X)
+    f = lib().ora_dcblas_iamax if X.dtype == np.float64 else lib().ora_scblas_iamax
+    return int(f(N, X, incX))
 
 
 def laswp(N, A, K1, K2, ipiv, inci):

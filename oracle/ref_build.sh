@@ -6,7 +6,8 @@
 #  2. extracts, one routine per file, ATL_getrfC/getrfR/getf2/laswp/getrs and
 #     ATL_potrfU/potrfL/potrf/potrs, ATL_trtri* and ATL_getri*
 #     (AtlasBase/Clint/atlas-lp.base),
-#     ATL_rand/gegen/epsilon (AtlasBase/Clint/atlas-tst.base) and the C
+#     ATL_rand/gegen/epsilon (AtlasBase/Clint/atlas-tst.base), ATL_iamax
+#     (AtlasBase/Clint/atlas-lvl1.base) and the C
 #     reference BLAS they run on (gemm, trsm, trmm, syrk, gemv, trsv, ger, scal,
 #     swap, iamax from
 #     AtlasBase/Antoine/atlrefblas.base);
@@ -47,13 +48,14 @@ done
 for r in ATL_rand ATL_gegen ATL_epsilon; do
    $X -b $R/Clint/atlas-tst.base -o $r.c rout=$r
 done
+$X -b $R/Clint/atlas-lvl1.base -o ATL_iamax.c rout=ATL_iamax
 CF="-O2 -fPIC -w -ffp-contract=off -fno-strict-aliasing -fwrapv -I$SRC -I$HERE/ref_shim"
 OBJ=""
 for f in ATL_dref*.c ATL_idrefamax.c; do $CC $CF -DDREAL -c $f -o ${f%.c}.o; OBJ="$OBJ ${f%.c}.o"; done
 for f in ATL_sref*.c ATL_isrefamax.c; do $CC $CF -DSREAL -c $f -o ${f%.c}.o; OBJ="$OBJ ${f%.c}.o"; done
 for f in ATL_getrfC ATL_getrfR ATL_getf2 ATL_laswp ATL_getrs ATL_potrfU ATL_potrfL ATL_potrf ATL_potrs \
          ATL_trtri ATL_trtriCU ATL_trtriCL ATL_trtriRU ATL_trtriRL ATL_getri ATL_getriC ATL_getriR \
-         ATL_gegen ATL_epsilon; do
+         ATL_gegen ATL_epsilon ATL_iamax; do
    $CC $CF -DDREAL -c $f.c -o d_$f.o
    $CC $CF -DSREAL -c $f.c -o s_$f.o
    OBJ="$OBJ d_$f.o s_$f.o"

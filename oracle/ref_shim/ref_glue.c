@@ -98,6 +98,9 @@ void atlref_##P##trsm(int order, int s, int u, int t, int d, int M, int N, T al,
 { refshim_##P##trsm((enum CBLAS_ORDER)order, (enum CBLAS_SIDE)s, (enum CBLAS_UPLO)u, \
                     (enum CBLAS_TRANSPOSE)t, (enum CBLAS_DIAG)d, M, N, al, A, lda, B, ldb); } \
 int atlref_i##P##amax(int N, const T *X, int incx) { return ATL_i##P##refamax(N, X, incx); } \
+long ATL_i##P##amax(long, const T*, long); \
+int atlref_cblas_i##P##amax(int N, const T *X, int incx) \
+{ return (N > 0 && incx > 0) ? (int)ATL_i##P##amax(N, X, incx) : 0; } \
 /* cblas_syrk's RowMajor flip of Uplo and Trans (AtlasBase/Clint/cblas.base:440-448) */ \
 void refshim_##P##syrk(enum CBLAS_ORDER o, enum CBLAS_UPLO u, enum CBLAS_TRANSPOSE t, int N, int K, \
    T al, const T *A, int lda, T be, T *C, int ldc) \

@@ -57,6 +57,39 @@ def load():
     return R
 
 
+def iamax_cases(rng):
+    """(buffer, N, incX) cases for cblas_i?amax: random, ties, zeros, signed
+    zeros, infinities, and NaNs followed by ordered and inverted runs."""
+    nan, inf = np.nan, np.inf
+    vecs = [rng.standard_normal(n) for n in (0, 1, 2, 3, 4, 5, 7, 8, 9, 31, 100, 1000)]
+    vecs += [np.array(v, dtype=np.float64) for v in (
+        [1.0, -3.0, 3.0, 2.0, -3.0], [0.0, 0.0, 0.0, 0.0, 0.0], [0.0, -0.0, 0.0, -0.0, 0.0, 0.0],
+        [-0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 5e-324], [2.0, inf, 1.0, -inf, 7.0], [1.0, -inf, inf, 3.0],
+        [nan, 1.0, 2.0, 3.0], [1.0, 2.0, nan], [5.0, nan, 0.0, 0.0, 0.0, 0.0], [5.0, nan, -0.0, 1.0],
+        [5.0, nan, 3.0, -2.0, -1.0, -0.5, 0.25, 4.0, 1.0], [5.0, nan, 3.0, -2.0, -1.0, -4.0, 2.0, 6.0, 6.0],
+        [9.0, nan, 2.0, -1.0, -0.5, -0.25], [nan, nan, 8.0, nan, 4.0, -3.0, 10.0, -10.0],
+        [nan, -2.0, 1.0, 1.5, -3.0, 0.5], [1.0, nan, 0.0, -0.0, 0.0, 2.0], [3.0, 1.0, nan, 7.0],
+        [0.0, 0.0, nan, 0.0, 0.0, 0.0, 0.0])]
+    big = rng.standard_normal(3000)
+    big[1234] = 40.0
+    big[2500] = -40.0
+    vecs.append(big)
+    big2 = rng.standard_normal(3000)
+    big2[700] = nan
+    big2[701] = 0.5
+    big2[702:705] = [-0.4, -0.3, 0.2]
+    vecs.append(big2)
+    cases = []
+    for v in vecs:
+        cases.append((v.copy(), v.size, 1))
+        if v.size >= 2:             # the same values at stride 3, other slots filled with larger noise
+            buf = np.full(3 * (v.size - 1) + 1, 1e6)
+            buf[::3] = v
+            cases.append((buf, v.size, 3))
+    cases.append((np.array([1.0, -7.0, 2.0]), 3, -1))     # negative increment: 0
+    return cases
+
+
 def gegen(R, M, N, lda, seed, dtype=np.float64):
     A = np.zeros((lda, N), dtype=dtype, order="F")
     (R.atlref_dgegen if dtype == np.float64 else R.atlref_sgegen)(M, N, A, lda, seed)
@@ -273,6 +306,16 @@ def main():
             out[f"getri_{n}_{order}_piv"] = piv.copy()
             out[f"getri_{n}_{order}_info"] = np.array(R.atlref_dgetri(order, n, A, n, piv))
             out[f"getri_{n}_{order}_inv"] = A
+    # cblas_i?amax (ATL_i?amax): ties, zeros, infinities and NaN runs, unit and strided
+    R.atlref_cblas_idamax.argtypes = [I, dp, I]
+    R.atlref_cblas_idamax.restype = I
+    R.atlref_cblas_isamax.argtypes = [I, sp, I]
+    R.atlref_cblas_isamax.restype = I
+    for k, (x, n, inc) in enumerate(iamax_cases(np.random.default_rng(4242))):
+        for pre, dt, f in (("d", np.float64, R.atlref_cblas_idamax), ("s", np.float32, R.atlref_cblas_isamax)):
+            xx = np.asfortranarray(x.astype(dt))
+            out[f"iamax_{pre}_{k}_x"] = xx
+            out[f"iamax_{pre}_{k}_meta"] = np.array([n, inc, f(n, xx, inc)], dtype=np.int64)
     np.savez_compressed(OUT, **out)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")
 

@@ -258,3 +258,18 @@ def test_getri_matches_reference(ora, golden):
             if order == 102 and n <= 5:
                 assert np.array_equal(A, ref), key
             assert np.abs(A - ref).max() <= 1e-13 * n * max(1.0, np.abs(ref).max()), key
+
+
+def test_cblas_iamax_matches_reference(ora, golden):
+    """cblas_i?amax restated (ATL_i?amax, AtlasBase/Clint/atlas-lvl1.base:1148-1340)
+    against the reference's own routine: ties, zeros, infinities, NaN runs,
+    unit and strided, double and float."""
+    n = 0
+    for k in golden.files:
+        if k.startswith("iamax_") and k.endswith("_meta"):
+            pre, idx = k.split("_")[1:3]
+            x = golden[f"iamax_{pre}_{idx}_x"]
+            N, inc, res = (int(v) for v in golden[k])
+            assert ora.cblas_iamax(N, x, inc) == res, k
+            n += 1
+    assert n >= 100
