@@ -718,10 +718,32 @@ __global__ void laswp_perm_kernel(const int *ipiv, int K1, int K2, int inci, int
   if (use_smem == 2)
     for (int s = threadIdx.x; s < n; s += blockDim.x) piv_s[s] = ipiv[(size_t)(K1 + s) * step];
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0 && use_smem == 2) {
+    // pivots read a batch ahead into registers: each interchange is then two
+    // shared loads with known addresses and two stores, no load-to-address wait
+    constexpr int B = 16;
+    for (int s0 = 0; s0 < n; s0 += B) {
+      int ipb[B];
+#pragma unroll
+      for (int u = 0; u < B; ++u) {
+        const int s = s0 + u;
+        ipb[u] = s < n ? piv_s[(inci > 0 ? K1 + s : K2 - 1 - s) - K1] : -1;
+      }
+#pragma unroll
+      for (int u = 0; u < B; ++u) {
+        const int s = s0 + u;
+        const int i = inci > 0 ? K1 + s : K2 - 1 - s;
+        const int ip = ipb[u];
+        if (s >= n || ip == i || ip < 0 || ip >= nrows) continue;
+        const int a = content[i], b = content[ip];
+        content[i] = b;
+        content[ip] = a;
+      }
+    }
+  } else if (threadIdx.x == 0) {
     for (int s = 0; s < n; ++s) {
       const int i = inci > 0 ? K1 + s : K2 - 1 - s;
-      const int ip = use_smem == 2 ? piv_s[i - K1] : ipiv[(size_t)i * step];
+      const int ip = ipiv[(size_t)i * step];
       if (ip == i || ip < 0 || ip >= nrows) continue;
       const int t = content[i];
       content[i] = content[ip];
@@ -732,6 +754,155 @@ __global__ void laswp_perm_kernel(const int *ipiv, int K1, int K2, int inci, int
   if (use_smem)
     for (int i = threadIdx.x; i < nrows; i += blockDim.x) content_g[i] = content_s[i];
 }
+// The interchange chain without the chain, for pivots that only look down
+// (ipiv[i] >= i, as getrf produces).  Position i is final after step i, and
+// what it receives is what the last earlier step with the same target left
+// there, so with
+//   last(x)  = the largest source j whose target ipiv[j] is x,
+//   prev(j)  = the largest source j' < j with the same target as j,
+//   V(i)     = the row at position i just before step i
+//            = V(last(i)) when some j < i targets i, else i,
+// the forward result is content[i] = V(prev(i)), or ipiv[i] when i is the
+// first source of its target, or V(i) for a self-interchange (i in [K1,K2));
+// content[x] = V(last(x)), or x when nothing targets x (elsewhere).  The
+// backward order (inci < 0) gives the inverse permutation.  One CTA: warp 0
+// finds prev/last 32 sources at a time (__match_any_sync groups equal
+// targets), pointer jumping resolves V in log2(n) rounds.  Pivot vectors that
+// do not look down run the one-thread chain on the same shared arrays.
+// Shared memory: ints r[n] (pivots, then the encoded prev), ptr[n], val[n],
+// ls[nrows] (last(x)).
+constexpr int kChainThreads = 1024;
+constexpr int kChainPer = 16;                       // sources per thread in the jumping rounds
+constexpr size_t kChainSmemMax = 200 * 1024;
+
+static size_t chain_smem_bytes(int nrows, int n) { return sizeof(int) * (3 * (size_t)n + (size_t)nrows); }
+static bool chain_fits(int nrows, int n) {
+  return n <= kChainThreads * kChainPer && chain_smem_bytes(nrows, n) <= kChainSmemMax;
+}
+
+__global__ void __launch_bounds__(kChainThreads)
+    laswp_chain_kernel(const int *ipiv, int K1, int K2, int inci, int *content_g, int nrows) {
+  extern __shared__ int ch_smem[];
+  const int n = K2 - K1;
+  const int step = inci > 0 ? inci : -inci;
+  int *r = ch_smem, *ptr = ch_smem + n, *val = ch_smem + 2 * n, *ls = ch_smem + 3 * n;
+  const int tid = threadIdx.x;
+  int viol = 0;
+  for (int x = tid; x < nrows; x += kChainThreads) ls[x] = -1;
+  for (int s = tid; s < n; s += kChainThreads) {
+    const int j = K1 + s, ip = ipiv[(size_t)j * step];
+    r[s] = ip;
+    if (ip != j && ip >= 0 && ip < nrows && ip < j) viol = 1;
+  }
+  if (__syncthreads_or(viol)) {        // general pivots: the chain, one thread
+    for (int x = tid; x < nrows; x += kChainThreads) ls[x] = x;
+    __syncthreads();
+    if (tid == 0)
+      for (int t = 0; t < n; ++t) {
+        const int s = inci > 0 ? t : n - 1 - t;
+        const int i = K1 + s, ip = r[s];
+        if (ip == i || ip < 0 || ip >= nrows) continue;
+        const int a = ls[i], b = ls[ip];
+        ls[i] = b;
+        ls[ip] = a;
+      }
+    __syncthreads();
+    for (int x = tid; x < nrows; x += kChainThreads) content_g[x] = ls[x];
+    return;
+  }
+  if (tid < 32) {                      // prev(j) into r, last(x) into ls, 32 sources at a time
+    const int lane = tid;
+    for (int s0 = 0; s0 < n; s0 += 32) {
+      const int s = s0 + lane, j = K1 + s;
+      int x = -1;
+      if (s < n) {
+        const int ip = r[s];
+        if (ip != j && ip >= 0 && ip < nrows) x = ip;
+      }
+      const unsigned grp = __match_any_sync(0xffffffffu, x >= 0 ? x : -1 - lane);
+      const unsigned lower = grp & ((1u << lane) - 1u);
+      int q = j;                                       // self: V(j)
+      if (x >= 0) {
+        if (lower) q = K1 + s0 + (31 - __clz(lower));  // an earlier source in this group of 32
+        else {
+          const int l = ls[x];
+          q = l >= 0 ? l : -2 - x;                     // -2 - x: the original row x
+        }
+      }
+      const bool top = x >= 0 && (grp >> lane) == 1u;  // the group's last source
+      __syncwarp();
+      if (s < n) r[s] = q;
+      if (top) ls[x] = j;
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  for (int s = tid; s < n; s += kChainThreads) {
+    const int l = ls[K1 + s];
+    ptr[s] = l >= 0 ? l - K1 : -1;
+    val[s] = K1 + s;
+  }
+  __syncthreads();
+  for (;;) {                           // pointer jumping: V(i) = V(last(i))
+    int np[kChainPer], nv[kChainPer];
+    int any = 0;
+#pragma unroll
+    for (int k = 0; k < kChainPer; ++k) {
+      const int s = tid + k * kChainThreads;
+      np[k] = -1;
+      nv[k] = 0;
+      if (s < n) {
+        const int p = ptr[s];
+        if (p >= 0) {
+          nv[k] = val[p];
+          np[k] = ptr[p];
+          any = 1;
+        } else {
+          nv[k] = val[s];
+        }
+      }
+    }
+    if (!__syncthreads_or(any)) break;
+#pragma unroll
+    for (int k = 0; k < kChainPer; ++k) {
+      const int s = tid + k * kChainThreads;
+      if (s < n) {
+        ptr[s] = np[k];
+        val[s] = nv[k];
+      }
+    }
+    __syncthreads();
+  }
+  for (int x = tid; x < nrows; x += kChainThreads) {
+    int c;
+    if (x >= K1 && x < K2) {
+      const int q = r[x - K1];
+      c = q >= 0 ? val[q - K1] : -2 - q;
+    } else {
+      const int l = ls[x];
+      c = l >= 0 ? val[l - K1] : x;
+    }
+    if (inci > 0) content_g[x] = c;
+    else content_g[c] = x;
+  }
+}
+
+// The row-content table of the interchanges K1..K2-1 into content (nrows ints).
+static void launch_interchange_table(const int *ipiv, int K1, int K2, int inci, int *content, int nrows,
+                                     cudaStream_t st) {
+  const int n = K2 - K1;
+  if (chain_fits(nrows, n)) {
+    ATLG_CHECK(cudaFuncSetAttribute(laswp_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kChainSmemMax));
+    laswp_chain_kernel<<<1, kChainThreads, chain_smem_bytes(nrows, n), st>>>(ipiv, K1, K2, inci, content, nrows);
+  } else {
+    const int mode = ((long)nrows + n <= kPermSmemRows) ? 2 : (nrows <= kPermSmemRows ? 1 : 0);
+    const size_t smem = mode == 2 ? sizeof(int) * ((size_t)nrows + n) : mode == 1 ? sizeof(int) * (size_t)nrows : 0;
+    ATLG_CHECK(cudaFuncSetAttribute(laswp_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    laswp_perm_kernel<<<1, 1024, smem, st>>>(ipiv, K1, K2, inci, content, nrows, mode);
+  }
+}
+
 template <typename T>
 __global__ void gather_rows_kernel(const T *A, int lda, T *W, int ldw, const int *content, int nrows, int N) {
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < (long)nrows * N; e += (long)gridDim.x * blockDim.x) {
@@ -860,15 +1031,6 @@ __global__ void __launch_bounds__(kLcThreads)
   }
 }
 
-// Shared-memory form of the interchange chain for n interchanges on nrows rows.
-static int perm_smem_mode(int nrows, int n) {
-  if ((long)nrows + n <= kPermSmemRows) return 2;
-  return nrows <= kPermSmemRows ? 1 : 0;
-}
-static size_t perm_smem_bytes(int mode, int nrows, int n) {
-  return mode == 2 ? sizeof(int) * ((size_t)nrows + n) : mode == 1 ? sizeof(int) * (size_t)nrows : 0;
-}
-
 // The rows that can move are [0, nrows); nrows must exceed every pivot.
 template <typename T>
 static void laswp_impl(int N, T *A, int lda, int K1, int K2, const int *ipiv, int inci, int nrows,
@@ -876,10 +1038,7 @@ static void laswp_impl(int N, T *A, int lda, int K1, int K2, const int *ipiv, in
   if (K2 <= K1 || N <= 0 || nrows <= 0) return;
   Context &c = ctx();
   int *content = static_cast<int *>(c.buffer(kBufW3, sizeof(int) * (size_t)nrows));
-  const int mode = perm_smem_mode(nrows, K2 - K1);
-  ATLG_CHECK(cudaFuncSetAttribute(laswp_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  laswp_perm_kernel<<<1, 1024, perm_smem_bytes(mode, nrows, K2 - K1), st>>>(ipiv, K1, K2, inci, content, nrows,
-                                                                             mode);
+  launch_interchange_table(ipiv, K1, K2, inci, content, nrows, st);
   const size_t csmem = laswp_cols_smem<T>(nrows);
   if (csmem <= kLaswpColsSmemMax) {
     ATLG_CHECK(cudaFuncSetAttribute(laswp_cols_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -904,9 +1063,7 @@ static void laswp_impl(int N, T *A, int lda, int K1, int K2, const int *ipiv, in
 // the interchanges ipiv[0..n) are applied in order (ATL_laswp forward), so
 // that the forward interchange of one vector is y[i] = b[perm[i]].
 void dev_perm_from_ipiv(const int *ipiv, int n, int *perm, cudaStream_t st) {
-  const int mode = perm_smem_mode(n, n);
-  ATLG_CHECK(cudaFuncSetAttribute(laswp_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  laswp_perm_kernel<<<1, 1024, perm_smem_bytes(mode, n, n), st>>>(ipiv, 0, n, 1, perm, n, mode);
+  launch_interchange_table(ipiv, 0, n, 1, perm, n, st);
   note_launch();
   ATLG_CHECK(cudaGetLastError());
 }

@@ -4,7 +4,9 @@ through the C ABI, bit-exact: against the reference's own laswp output
 device applies a permutation -- the dense column form (most rows of the span
 move), the sparse pair-list form (a few hundred interchanges in a tall
 column, as for one block column of the split LU) and the gather/copy form
-for tables too large for shared memory."""
+for tables too large for shared memory -- and on the ways it builds the
+row-content table: the parallel form for pivots that look down (getrf's),
+the one-thread chain for other pivot vectors and for long chains."""
 import numpy as np
 import pytest
 
@@ -42,6 +44,7 @@ def test_laswp_matches_reference_fixtures(gb, ora, golden):
     (16384, 3, 100, 356, -1, "sparse"),
     (12000, 25, 0, 64, 1, "sparse"),
     (20000, 3, 0, 20000, 1, "gather"),         # table beyond the shared-memory form
+    (13000, 5, 0, 13000, -1, "one-thread chain"),  # too many interchanges for the parallel table
 ])
 def test_laswp_forms_match_oracle(gb, ora, m, N, K1, K2, inci, form):
     torch = pytest.importorskip("torch")
@@ -62,3 +65,18 @@ def test_laswp_no_interchange_is_identity(gb, ora):
     A = ora.gegen(m, N, 17)
     got = _run(torch, gb, A, N, 0, m, piv, 1, m)
     assert np.array_equal(got, A)
+
+
+@pytest.mark.parametrize("inci", [1, -1])
+def test_laswp_pivots_that_look_up(gb, ora, inci):
+    """Pivot vectors with ipiv[i] < i (not from getrf) take the one-thread
+    interchange chain; the result is still the reference's."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(77)
+    m, N, K1, K2 = 3000, 20, 10, 2900
+    piv = rng.integers(0, m, size=m).astype(np.int32)
+    A = ora.gegen(m, N, 99)
+    got = _run(torch, gb, A, N, K1, K2, piv, inci, m)
+    ref = A.copy(order="F")
+    ora.laswp(N, ref, K1, K2, piv, inci)
+    assert np.array_equal(got, ref)
