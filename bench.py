@@ -274,6 +274,93 @@ def measure_forms(G, O, torch, n=16384, kappas=(1e2, 1e6, 1e10), nslices=8):
     return out
 
 
+def measure_adjoint(G, O, torch, n=4096, nrhs=64, ndir=32, h=1e-6):
+    """The differentiable solve X = A^-1 B at n = 4096, nrhs = 64: A = G/sqrt(n)
+    + 4I, B and gX Gaussian (seeded).  Device time of the forward (dgetrf +
+    dgetrs) and of dgesv_adjoint (transposed getrs + DGEMM), CUDA events on
+    the library stream; gradient error against the oracle's CPU solve and
+    against central finite differences (h, ndir random directions, GPU
+    solves); the same gradient with the forward and the transposed solve
+    repeated through the mixed-precision path."""
+    import ctypes as C
+    L = G.lib()
+    st = L.atlg_stream()
+    s = torch.cuda.ExternalStream(st)
+    rng = np.random.default_rng(2024)
+    A = np.asfortranarray(rng.standard_normal((n, n)) / np.sqrt(n) + 4.0 * np.eye(n))
+    B = np.asfortranarray(rng.standard_normal((n, nrhs)))
+    gX = np.asfortranarray(rng.standard_normal((n, nrhs)))
+    dA0 = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()     # column-major A
+    dB0 = torch.from_numpy(np.ascontiguousarray(B.T)).cuda()
+    dgX = torch.from_numpy(np.ascontiguousarray(gX.T)).cuda()
+    dA, dX = torch.empty_like(dA0), torch.empty_like(dB0)
+    dgA, dgB = torch.empty_like(dA0), torch.empty_like(dB0)
+    piv = torch.zeros(n, dtype=torch.int32, device="cuda")
+    inf = torch.zeros(4, dtype=torch.int32, device="cuda")
+    fwd, adj = [], []
+    for rep in range(4):
+        dA.copy_(dA0)
+        dX.copy_(dB0)
+        torch.cuda.synchronize()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(s)
+        L.atlg_dgetrf_dev(n, n, dA.data_ptr(), n, piv.data_ptr(), inf.data_ptr(), st)
+        L.atlg_dgetrs_dev(102, 111, n, nrhs, dA.data_ptr(), n, piv.data_ptr(), dX.data_ptr(), n, st)
+        e1.record(s)
+        L.atlg_dgesv_adjoint_dev(n, nrhs, dA.data_ptr(), n, piv.data_ptr(), dX.data_ptr(), n, dgX.data_ptr(), n,
+                                 dgA.data_ptr(), n, dgB.data_ptr(), n, st)
+        e2.record(s)
+        torch.cuda.synchronize()
+        if rep:
+            fwd.append(e0.elapsed_time(e1))
+            adj.append(e1.elapsed_time(e2))
+    X = dX.cpu().numpy().T
+    gA, gB = dgA.cpu().numpy().T, dgB.cpu().numpy().T
+    O.set_threads(0)
+    Lo = A.copy(order="F")
+    info_o, opiv = O.getrf(Lo)
+    Xo = B.copy(order="F")
+    O.getrs(Lo, opiv, Xo)
+    gBo = gX.copy(order="F")
+    O.getrs(Lo, opiv, gBo, trans=O.Trans)
+    gAo = -gBo @ Xo.T
+    rel = lambda a, b: float(np.abs(a - b).max() / np.abs(b).max())
+    dev = 0.0
+    drng = np.random.default_rng(8)
+    for _ in range(ndir):
+        dA_ = drng.standard_normal((n, n))
+        dB_ = drng.standard_normal((n, nrhs))
+        xs = []
+        for sg in (1.0, -1.0):
+            Ap = np.asfortranarray(A + sg * h * dA_)
+            Xp = np.asfortranarray(B + sg * h * dB_)
+            G.clapack_dgesv(102, n, nrhs, Ap, n, np.zeros(n, dtype=np.int32), Xp, n)
+            xs.append(Xp)
+        fd = float(np.sum(gX * (xs[0] - xs[1])) / (2 * h))
+        an = float(np.sum(gA * dA_) + np.sum(gB * dB_))
+        dev = max(dev, abs(fd - an) / max(1.0, abs(an)))
+
+    def mixed(M, R):
+        Xm = np.zeros(R.shape, order="F")
+        info, berr, ferr, iters, status = G.dgesv_mixed(M.copy(order="F"), np.zeros(n, dtype=np.int32),
+                                                        R.copy(order="F"), Xm)
+        return Xm, iters, status, float(np.max(berr))
+
+    Xm, it1, st1, be1 = mixed(A, B)
+    gBm, it2, st2, be2 = mixed(np.asfortranarray(A.T), gX)
+    gAm = -gBm @ Xm.T
+    return {"n": n, "nrhs": nrhs, "forward_ms": min(fwd), "adjoint_ms": min(adj),
+            "adjoint_tflops": 4.0 * n * n * nrhs / (min(adj) * 1e-3) / 1e12,   # transposed getrs + DGEMM
+            "gA_rel_err_vs_oracle_cpu_solve": rel(gA, gAo), "gB_rel_err_vs_oracle_cpu_solve": rel(gB, gBo),
+            "fd_max_rel_dev": dev, "fd": f"central differences, h={h}, {ndir} random directions, GPU solves",
+            "mixed_path": {"gA_rel_err_vs_fp64": rel(gAm, gA), "gB_rel_err_vs_fp64": rel(gBm, gB),
+                           "iters": [it1, it2], "fallback_fp64": [st1 == 1, st2 == 1],
+                           "backward_error": max(be1, be2),
+                           "how": "X and gB = A^-T gX both through dgesv_mixed (the transposed system as A^T), "
+                                  "gA = -gB X^T"},
+            "timing": "CUDA events on the library stream, best of 3 after one warm-up"}
+
+
 def spd_device(torch, n, seed):
     """Symmetric S with entries uniform(-0.5, 0.5) plus n*I on the device,
     column-major (symmetric, so row-major is the same); positive definite by
@@ -626,6 +713,7 @@ def run_gpu(args):
         nxt = None
         if world == 1 and not args.skip_extras:
             forms = measure_forms(G, O, torch)
+            forms["adjoint_n4096"] = measure_adjoint(G, O, torch)
             nxt = measure_next(G, O, torch)
             nxt.update(measure_memory(G, O, torch))
         line = {

@@ -2,7 +2,8 @@
 harness around it: X = A^{-1} B; for an upstream gX, gB = A^{-T} gX and
 gA = -gB X^T.  Checked against central finite differences (h = 1e-6, 32
 random directions) and against the gradient built from the oracle's CPU
-solve."""
+solve, at a small size and at the workload's own size (n = 4096, nrhs = 64),
+where the solve is also repeated through the mixed-precision path."""
 import numpy as np
 import pytest
 
@@ -78,3 +79,52 @@ def test_autograd_function_against_finite_differences(gb):
         fd = np.sum(gX * (Xp - Xm)) / (2 * h)
         an = np.sum(gA * dA) + np.sum(gB * dB)
         assert abs(fd - an) <= 1e-6 * max(1.0, abs(an)), (fd, an)
+
+
+def _mixed_solve(gb, A, B):
+    n, nrhs = B.shape
+    X = np.zeros((n, nrhs), order="F")
+    ipiv = np.zeros(n, dtype=np.int32)
+    info, berr, ferr, iters, status = gb.dgesv_mixed(A.copy(order="F"), ipiv, B.copy(order="F"), X)
+    assert info == 0
+    return X, status
+
+
+def test_adjoint_at_n4096_nrhs64(gb, ora):
+    """The differentiable-solve workload at its stated size: A = G/sqrt(n) + 4I,
+    B and gX Gaussian.  gA, gB against the gradient built from the oracle's
+    CPU solve and against central finite differences (h = 1e-6, 32 random
+    directions); then the forward and the transposed solve repeated through
+    the mixed-precision path, whose gradient must agree with the FP64 one to
+    the refinement's accuracy."""
+    n, nrhs = 4096, 64
+    A, B, gX = make(n, nrhs, 2024)
+    LU, ipiv, X = solve(gb, A, B)
+    gA, gB = gb.dgesv_adjoint(LU, ipiv, X, gX)
+    ora.set_threads(0)
+    Lo = A.copy(order="F")
+    info, opiv = ora.getrf(Lo)
+    assert info == 0
+    Xo = B.copy(order="F")
+    ora.getrs(Lo, opiv, Xo)
+    gBo = gX.copy(order="F")
+    ora.getrs(Lo, opiv, gBo, trans=ora.Trans)
+    gAo = -gBo @ Xo.T
+    assert np.abs(gB - gBo).max() <= 1e-12 * np.abs(gBo).max()
+    assert np.abs(gA - gAo).max() <= 1e-12 * np.abs(gAo).max()
+    rng = np.random.default_rng(8)
+    h = 1e-6
+    for _ in range(32):
+        dA = rng.standard_normal((n, n))
+        dB = rng.standard_normal((n, nrhs))
+        Xp = solve(gb, np.asfortranarray(A + h * dA), np.asfortranarray(B + h * dB))[2]
+        Xm = solve(gb, np.asfortranarray(A - h * dA), np.asfortranarray(B - h * dB))[2]
+        fd = np.sum(gX * (Xp - Xm)) / (2 * h)
+        an = np.sum(gA * dA) + np.sum(gB * dB)
+        assert abs(fd - an) <= 1e-6 * max(1.0, abs(an)), (fd, an)
+    Xmx, st1 = _mixed_solve(gb, A, B)
+    gBm, st2 = _mixed_solve(gb, np.asfortranarray(A.T), gX)
+    gAm = -gBm @ Xmx.T
+    assert st1 == 0 and st2 == 0                     # refinement converged, no FP64 fallback
+    assert np.abs(gBm - gB).max() <= 1e-12 * np.abs(gB).max()
+    assert np.abs(gAm - gA).max() <= 1e-12 * np.abs(gA).max()
