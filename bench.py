@@ -39,6 +39,22 @@ def dgesv_flops(n, nrhs=1):
     return n * n * n - n ** 3 / 3.0 - n * n / 2.0 + 2.0 * n * n * nrhs
 
 
+def max_over_ranks(dist, ms, device):
+    """The largest of the ranks' times (each rank passes its own; no process
+    group: this rank's).  The job's time is its slowest rank's."""
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0])
+
+
+def replica_throughput(world, flops_per_step, steps, max_ms):
+    """Whole-job TFLOP/s of `world` replicas, each doing `steps` steps of
+    `flops_per_step`, finished when the slowest one is (max_ms)."""
+    return world * flops_per_step * steps / (max_ms * 1e-3) / 1e12
+
+
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -654,13 +670,9 @@ def run_gpu(args):
     clk = clocks.stop()
     if dist:
         dist.barrier()
-    dev_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
-    t_ms = torch.tensor([dev_ms], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(t_ms, op=dist.ReduceOp.MAX)
-    dev_ms = float(t_ms[0])
+    dev_ms = max_over_ranks(dist, sum(e0.elapsed_time(e1) for e0, e1 in evs), "cuda")
     flops = dgesv_flops(n, nrhs)
-    value = world * flops * args.steps / (dev_ms * 1e-3) / 1e12
+    value = replica_throughput(world, flops, args.steps, dev_ms)
 
     # ---- e2e through the host C ABI: clapack_dgesv on pinned host arrays ----
     Ah = torch.empty((n, n), dtype=torch.float64).pin_memory()
@@ -679,12 +691,8 @@ def run_gpu(args):
         assert rc == 0
         if it > 0:
             e2e_t.append(t1 - t0)
-    e2e_s = max(e2e_t) if world == 1 else max(e2e_t)
-    e2e_tensor = torch.tensor([sum(e2e_t) / len(e2e_t)], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(e2e_tensor, op=dist.ReduceOp.MAX)
-    e2e_val = world * flops / float(e2e_tensor[0]) / 1e12
-    del e2e_s
+    e2e_ms = max_over_ranks(dist, 1e3 * sum(e2e_t) / len(e2e_t), "cuda")
+    e2e_val = replica_throughput(world, flops, 1, e2e_ms)
 
     # ---- roofline of the dominant kernel (the trailing-update DGEMM) ----
     p64, _ = G.probe_peaks()
