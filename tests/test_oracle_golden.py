@@ -273,3 +273,32 @@ def test_cblas_iamax_matches_reference(ora, golden):
             assert ora.cblas_iamax(N, x, inc) == res, k
             n += 1
     assert n >= 100
+
+
+def test_cblas_iamax_random_against_reference_build(ora):
+    """Where the reference's own routines were built here (oracle/_ref), the
+    oracle's cblas_iamax agrees with the reference's ATL_iamax on random
+    vectors mixing NaN, infinities and signed zeros, unit and strided."""
+    import ctypes as C
+    import os
+    path = os.path.join(os.path.dirname(ora.LIB_PATH), "_ref", "libatlref.so")
+    if not os.path.exists(path):
+        pytest.skip("reference build absent (built only where the reference tree is)")
+    R = C.CDLL(path)
+    dp = np.ctypeslib.ndpointer(np.float64, flags="F_CONTIGUOUS")
+    sp = np.ctypeslib.ndpointer(np.float32, flags="F_CONTIGUOUS")
+    R.atlref_cblas_idamax.argtypes = [C.c_int, dp, C.c_int]
+    R.atlref_cblas_isamax.argtypes = [C.c_int, sp, C.c_int]
+    rng = np.random.default_rng(123)
+    pool = np.array([0.0, -0.0, 1.0, -1.0, 2.0, -2.0, 0.5, -0.5, np.nan, np.inf, -np.inf, 3.0, 1e-310])
+    for t in range(4000):
+        n = int(rng.integers(0, 40))
+        inc = int(rng.choice([1, 1, 2, 3, -1]))
+        v = rng.choice(pool, size=n)
+        m = max(1, (n - 1) * abs(inc) + 1)
+        buf = np.full(m, 7.0)
+        if n:
+            buf[:: abs(inc)][:n] = v
+        for dt, f in ((np.float64, R.atlref_cblas_idamax), (np.float32, R.atlref_cblas_isamax)):
+            x = np.asfortranarray(buf.astype(dt))
+            assert ora.cblas_iamax(n, x, inc) == f(n, x, inc), (v, inc, dt)
