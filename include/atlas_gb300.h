@@ -211,6 +211,10 @@ unsigned long long atlg_launch_count(void);
 void atlg_prof_enable(int on);
 int  atlg_prof_collect(double *ms, double *flops, int *count);
 void atlg_probe_peaks(double *fp64_tflops, double *fp32_tflops);
+/* benchmark support (no reference counterpart): FP64 tensor-core throughput
+ * in TFLOP/s of mma.sync with f64 operands, shapes m8n8k4, m16n8k4 and
+ * m16n8k16 (any pointer may be NULL) */
+void atlg_probe_fp64_mma(double *m8n8k4, double *m16n8k4, double *m16n8k16);
 int atlg_dgemm_dev(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda,
                    const double *B, int ldb, double beta, double *C, int ldc, void *stream);
 int atlg_dgemm_dev_opts(int TA, int TB, int M, int N, int K, double alpha, const double *A,
@@ -241,11 +245,12 @@ int atlg_dlaswp_dev(int N, double *A, int lda, int K1, int K2, const int *ipiv, 
  * GPU loading the library holds until exit.  For callers that cannot let a
  * library call cudaMalloc/cudaFree (their own pool owns device memory, or
  * they cannot take the device-wide synchronisation those calls imply).
- * Returns 0; -1 bad size; -2 when 4*nrows (rounded up to 256) + 8*nrows*N
- * bytes exceed the 16 MiB scratch; -3 CUDA error.  The first call on a
- * device looks up the scratch address (cudaGetSymbolAddress): make it before
- * any stream capture.  Calls that overlap on the GPU share the scratch and
- * race: serialise them. */
+ * Returns 0; -1 bad size (also K1 < 0 or K2 > nrows); -2 when 4*nrows
+ * (rounded up to 256) + 8*nrows*N bytes exceed the 16 MiB scratch; -3 when
+ * one of its own launches fails.  stream NULL is the library's own stream, as
+ * for the other atlg_*_dev calls.  The first call on a device looks up the
+ * scratch address (cudaGetSymbolAddress): make it before any stream capture.
+ * Calls that overlap on the GPU share the scratch and race: serialise them. */
 int atlg_dlaswp_noalloc(int N, double *A, int lda, int K1, int K2, const int *ipiv, int inci,
                         int nrows, void *stream);
 /* LU panel implementation: 1 (default) factors panels that fit one thread-

@@ -27,7 +27,7 @@ EXPORTS = [
     "clapack_sgesv", "atlg_num_sms", "atlg_stream", "atlg_status", "atlg_dgemm_dev",
     "atlg_dgemm_dev_opts", "atlg_sgemm_dev", "atlg_dtrsm_dev", "atlg_dlaswp_dev", "atlg_dgetrf_dev",
     "atlg_sgetrf_dev", "atlg_dgetrs_dev", "atlg_launch_count", "atlg_prof_enable", "atlg_prof_collect",
-    "atlg_probe_peaks", "dgesv_mixed", "dgesv_adjoint", "atlg_dgesv_mixed_dev", "atlg_dgesv_adjoint_dev",
+    "atlg_probe_peaks", "atlg_probe_fp64_mma", "dgesv_mixed", "dgesv_adjoint", "atlg_dgesv_mixed_dev", "atlg_dgesv_adjoint_dev",
     "atlg_dlaswp_noalloc", "dgemm_split", "atlg_dgemm_split_dev", "atlg_sgemm_tf32x3_dev",
     "cblas_dsyrk", "cblas_ssyrk", "clapack_dpotrf", "clapack_spotrf", "clapack_dpotrs", "clapack_spotrs",
     "clapack_dposv", "clapack_sposv", "atlg_dsyrk_dev", "atlg_dpotrf_dev", "atlg_dpotrs_dev",
@@ -136,6 +136,7 @@ def _declare(L):
         "atlg_prof_enable": (None, [_i]),
         "atlg_prof_collect": (_i, [C.POINTER(_d), C.POINTER(_d), C.POINTER(_i)]),
         "atlg_probe_peaks": (None, [C.POINTER(_d), C.POINTER(_d)]),
+        "atlg_probe_fp64_mma": (None, [C.POINTER(_d), C.POINTER(_d), C.POINTER(_d)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -342,3 +343,10 @@ def probe_peaks():
     a, b = _d(), _d()
     lib().atlg_probe_peaks(C.byref(a), C.byref(b))
     return a.value, b.value
+
+
+def probe_fp64_mma():
+    """FP64 mma.sync throughput (TFLOP/s) for shapes m8n8k4, m16n8k4, m16n8k16."""
+    a, b, c = _d(), _d(), _d()
+    lib().atlg_probe_fp64_mma(C.byref(a), C.byref(b), C.byref(c))
+    return {"m8n8k4": a.value, "m16n8k4": b.value, "m16n8k16": c.value}

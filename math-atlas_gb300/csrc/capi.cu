@@ -41,6 +41,7 @@ using namespace atlg;
 namespace atlg {
 double probe_fp64_tflops();
 double probe_fp32_tflops();
+void probe_fp64_mma_tflops(double *m8n8k4, double *m16n8k4, double *m16n8k16);
 }
 
 // ------------------------------------------------------------ error reporting
@@ -93,7 +94,6 @@ void to_host(T *h, int ldh, const T *d, int ldd, int rows, int cols, cudaStream_
                                  cudaMemcpyDeviceToHost, st));
 }
 
-cudaStream_t stream_of(void *s) { return s ? static_cast<cudaStream_t>(s) : ctx().stream; }
 
 template <typename T>
 void dev_syrk_any(int uplo, int trans, int n, int k, T alpha, const T *A, int lda, T beta, T *C, int ldc,
@@ -1106,6 +1106,9 @@ int atlg_prof_collect(double *ms, double *flops, int *count) {
   return 0;
 }
 
+void atlg_probe_fp64_mma(double *m8n8k4, double *m16n8k4, double *m16n8k16) {
+  probe_fp64_mma_tflops(m8n8k4, m16n8k4, m16n8k16);
+}
 void atlg_probe_peaks(double *fp64_tflops, double *fp32_tflops) {
   if (fp64_tflops) *fp64_tflops = probe_fp64_tflops();
   if (fp32_tflops) *fp32_tflops = probe_fp32_tflops();

@@ -49,6 +49,8 @@ Context &ctx() {
   return *c;
 }
 
+cudaStream_t stream_of(void *s) { return s ? static_cast<cudaStream_t>(s) : ctx().stream; }
+
 void *Context::buffer(int slot, size_t bytes) {
   if (slot < 0 || slot >= kNumSlots) abort();
   if (bytes == 0) bytes = 16;

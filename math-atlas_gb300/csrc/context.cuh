@@ -44,6 +44,9 @@ struct Context {
 inline void note_launch(unsigned n = 1);
 
 Context &ctx();
+// the stream an atlg_*_dev call runs on: the caller's, or for NULL the
+// library's own non-blocking stream
+cudaStream_t stream_of(void *s);
 inline void note_launch(unsigned n) { ctx().launches += n; }
 
 }  // namespace atlg

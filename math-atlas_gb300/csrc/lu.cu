@@ -1433,6 +1433,8 @@ extern "C" int atlg_dlaswp_noalloc(int N, double *A, int lda, int K1, int K2, co
   using namespace atlg;
   if (N < 0 || nrows < 0 || lda < (nrows > 1 ? nrows : 1)) return -1;
   if (K2 <= K1 || N == 0 || nrows == 0) return 0;
+  // the interchanges K1..K2-1 name rows of the table, which has nrows entries
+  if (K1 < 0 || K2 > nrows) return -1;
   const size_t table = ((size_t)nrows * sizeof(int) + 255) & ~size_t(255);
   const size_t need = table + (size_t)nrows * (size_t)N * sizeof(double);
   if (need > kNoAllocScratchBytes) {
@@ -1446,14 +1448,28 @@ extern "C" int atlg_dlaswp_noalloc(int N, double *A, int lda, int K1, int K2, co
   if (!base) return -3;
   int *content = reinterpret_cast<int *>(base);
   double *W = reinterpret_cast<double *>(base + table);
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const int use_smem = nrows <= kPermSmemRows;
+  // NULL means the library's own stream, as for every other atlg_*_dev entry
+  // point (creating it allocates no device memory)
+  cudaStream_t st = stream_of(stream);
+  int use_smem = nrows <= kPermSmemRows;
   const size_t smem = use_smem ? sizeof(int) * (size_t)nrows : 0;
   if (cudaFuncSetAttribute(laswp_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
       cudaSuccess)
     return -3;
-  laswp_perm_kernel<<<1, 1024, smem, st>>>(ipiv, K1, K2, inci, content, nrows, use_smem);
-  gather_rows_kernel<double><<<grid_for((long)nrows * N), 256, 0, st>>>(A, lda, W, nrows, content, nrows, N);
-  copy_rows_kernel<double><<<grid_for((long)nrows * N), 256, 0, st>>>(A, lda, W, nrows, nrows, N);
-  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+  // each launch reports its own status, so an error left by an unrelated
+  // earlier call is neither blamed on this one nor cleared
+  const dim3 grid(grid_for((long)nrows * N));
+  int ld_w = nrows;
+  void *perm_args[] = {(void *)&ipiv, &K1, &K2, &inci, &content, &nrows, &use_smem};
+  void *gather_args[] = {&A, &lda, &W, &ld_w, &content, &nrows, &N};
+  void *copy_args[] = {&A, &lda, &W, &ld_w, &nrows, &N};
+  if (cudaLaunchKernel((const void *)laswp_perm_kernel, dim3(1), dim3(1024), perm_args, smem, st) != cudaSuccess)
+    return -3;
+  if (cudaLaunchKernel((const void *)gather_rows_kernel<double>, grid, dim3(256), gather_args, 0, st) !=
+      cudaSuccess)
+    return -3;
+  if (cudaLaunchKernel((const void *)copy_rows_kernel<double>, grid, dim3(256), copy_args, 0, st) != cudaSuccess)
+    return -3;
+  note_launch(3);
+  return 0;
 }
