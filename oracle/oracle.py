@@ -266,3 +266,23 @@ def set_threads(n):
 
 def get_threads():
     return lib().ora_get_threads()
+
+
+# ---- the reference's own routines (oracle/_ref/libatlref.so, built by
+# oracle/ref_build.sh from the reference's basefiles) ----
+REF_LIB_PATH = os.path.join(HERE, "_ref", "libatlref.so")
+_ref = None
+
+
+def ref_lib():
+    """The reference's own LU-path routines on its C reference BLAS, or None
+    when oracle/_ref was not built (no reference tree or extraction)."""
+    global _ref
+    if _ref is None and os.path.exists(REF_LIB_PATH):
+        R = C.CDLL(REF_LIB_PATH)
+        R.atlref_dgetrf.argtypes = [_i, _i, _i, _dp, _i, _ip]
+        R.atlref_dgetrf.restype = _i
+        R.atlref_dgetrs.argtypes = [_i, _i, _i, _i, _dp, _i, _ip, _dp, _i]
+        R.atlref_dgemm.argtypes = [_i, _i, _i, _i, _i, _i, _d, _dp, _i, _dp, _i, _d, _dp, _i]
+        _ref = R
+    return _ref

@@ -22,6 +22,10 @@
 #define Mabs(x_) (((x_) >= 0) ? (x_) : -(x_))
 #define ATL_INT int
 #define ATL_CINT const int
+#define ATL_CSZT const size_t
+/* cache-line alignment used by the test library's cache flush */
+#define ATL_Cachelen 64
+#define ATL_AlignPtr(vp_) ((void *)(ATL_Cachelen + ((((size_t)(vp_)) / ATL_Cachelen) * ATL_Cachelen)))
 #define ATL_assert(x_) do { if (!(x_)) { fprintf(stderr, "assert %s\n", #x_); abort(); } } while (0)
 
 #if defined(DREAL)
@@ -32,6 +36,7 @@
    #define PATL ATL_d
    #define PATLU ATL_d
    #define ATL_MulBySize(x_) ((x_) << 3)
+   #define ATL_DivBySize(x_) ((x_) >> 3)
 #elif defined(SREAL)
    #define TREAL
    #define TYPE float
@@ -40,10 +45,13 @@
    #define PATL ATL_s
    #define PATLU ATL_s
    #define ATL_MulBySize(x_) ((x_) << 2)
+   #define ATL_DivBySize(x_) ((x_) >> 2)
 #else
    #error "define DREAL or SREAL"
 #endif
 #define SHIFT
+/* the serial build's thread multiplier of the cache size (none) */
+#define ATL_PTCACHEMUL
 #define SCALAR TYPE
 #define ATL_rzero ((TYPE)0)
 #define ATL_rone ((TYPE)1)

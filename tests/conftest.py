@@ -9,6 +9,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 sys.path.insert(0, os.path.join(ROOT, "math-atlas_gb300"))
 GOLDEN = os.path.join(ROOT, "tests", "golden", "atlas_ref_fixtures.npz")
+GOLDEN_LARGE = os.path.join(ROOT, "tests", "golden", "atlas_ref_large.npz")
 
 
 def pytest_configure(config):
@@ -27,6 +28,15 @@ def ora():
 def golden():
     import numpy as np
     return np.load(GOLDEN)
+
+
+@pytest.fixture(scope="session")
+def golden_large():
+    """Reference results at the headline sizes (pivots of the reference's own
+    ATL_getrfC at n = 2048, 4096, 8192, FP32 pivots at 4096, sampled entries
+    of the reference BLAS DGEMM at 1024^3)."""
+    import numpy as np
+    return np.load(GOLDEN_LARGE)
 
 
 @pytest.fixture(scope="session")

@@ -2,7 +2,8 @@
 routines (oracle/_ref/libatlref.so, built by oracle/ref_build.sh from the
 reference basefiles).  Run once where the reference source tree is present:
 
-    sh oracle/ref_build.sh && python tests/golden/make_golden.py
+    sh oracle/ref_build.sh <reference tree> && python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --large      # headline sizes (minutes)
 
 The fixtures pin the oracle and the GPU library to the reference:
   * ATL_rand streams and ATL_gegen matrices (bit-exact),
@@ -320,5 +321,61 @@ def main():
     print("wrote", OUT, os.path.getsize(OUT), "bytes")
 
 
+LARGE_OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "atlas_ref_large.npz")
+# headline sizes: column-major LU with the xdlutst seed n*n+lda (lda = n) and
+# the plain dgesv's right-hand side gegen(n, 1, n+1); FP32 pivots at 4096
+LARGE_LU = (2048, 4096, 8192)
+LARGE_SLU = (4096,)
+# DGEMM 1024^3 NoTrans/NoTrans, alpha 1, beta 0, gemmtst seeds
+LARGE_GEMM = 1024
+LARGE_GEMM_SAMPLES = 16384
+
+
+def main_large():
+    """Reference results at the headline sizes, too large for the main
+    fixture file: the reference's own ATL_getrfC pivots (and the diagonal of U
+    and the getrs solution) at n = 2048, 4096, 8192, FP32 pivots at 4096, and
+    sampled entries and column 1-norms of the reference BLAS product at
+    1024^3.  The n = 8192 factorization runs on the reference's triple-loop
+    BLAS on one core: minutes."""
+    if not os.path.exists(REFLIB):
+        sys.exit("build the reference routines first: sh oracle/ref_build.sh <reference tree>")
+    R = load()
+    out = {}
+    for n in LARGE_LU:
+        A = gegen(R, n, n, n, n * n + n)
+        piv = np.zeros(n, dtype=np.int32)
+        info = R.atlref_dgetrf(102, n, n, A, n, piv)
+        out[f"lu_{n}_ipiv"] = piv
+        out[f"lu_{n}_info"] = np.array(info)
+        out[f"lu_{n}_udiag"] = np.diag(A).copy()
+        b = gegen(R, n, 1, n, n + 1)
+        R.atlref_dgetrs(102, 111, n, 1, A, n, piv, b, n)
+        out[f"lu_{n}_x"] = b[:, 0].copy()
+        print("lu", n, "info", info, flush=True)
+    for n in LARGE_SLU:
+        A = gegen(R, n, n, n, n * n + n, np.float32)
+        piv = np.zeros(n, dtype=np.int32)
+        info = R.atlref_sgetrf(102, n, n, A, n, piv)
+        out[f"slu_{n}_ipiv"] = piv
+        out[f"slu_{n}_info"] = np.array(info)
+        print("slu", n, "info", info, flush=True)
+    n = LARGE_GEMM
+    A = gegen(R, n, n, n, n * n + 513 * 7 + 90)
+    B = gegen(R, n, n, n, n * n + 127 * 50 + 77)
+    Cm = gegen(R, n, n, n, n * n + 101 * 2 + 53)
+    R.atlref_dgemm(102, 111, 111, n, n, n, 1.0, A, n, B, n, 0.0, Cm, n)
+    rng = np.random.default_rng(1024)
+    idx = rng.integers(0, n * n, LARGE_GEMM_SAMPLES)
+    out["gemm_1024_idx"] = idx.astype(np.int64)                    # column-major flat index
+    out["gemm_1024_val"] = Cm.reshape(-1, order="F")[idx].copy()
+    out["gemm_1024_colnrm1"] = np.abs(Cm).sum(axis=0)
+    np.savez_compressed(LARGE_OUT, **out)
+    print("wrote", LARGE_OUT, os.path.getsize(LARGE_OUT), "bytes")
+
+
 if __name__ == "__main__":
-    main()
+    if "--large" in sys.argv[1:]:
+        main_large()
+    else:
+        main()

@@ -129,3 +129,20 @@ def test_sgemm_matches_oracle(gb, ora, ta, tb, M, N, K):
     ora.lib().ora_sgemm(ta, tb, M, N, K, 1.5, A, A.shape[0], B, B.shape[0], -0.5, Ct, M)
     eps = np.finfo(np.float32).eps
     assert np.abs(Cg - Ct).max() <= 2 * K * eps * (np.abs(A).max() * np.abs(B).max() * 1.5 + 1)
+
+
+def test_dgemm_1024_matches_reference_blas(gb, ora, golden_large):
+    """cblas_dgemm at 1024^3 (NoTrans/NoTrans, alpha 1, beta 0, gemmtst
+    seeds) against the reference BLAS product of the same operands: 16384
+    sampled entries within the elementwise bound 2 K eps K max|A| max|B| and
+    every column 1-norm to 1e-12."""
+    n = 1024
+    A, B, Cm = gen_operands(ora, 111, 111, n, n, n)
+    gb.cblas_dgemm(102, 111, 111, n, n, n, 1.0, A, n, B, n, 0.0, Cm, n)
+    idx = golden_large["gemm_1024_idx"]
+    ref = golden_large["gemm_1024_val"]
+    got = Cm.reshape(-1, order="F")[idx]
+    bound = 2 * n * np.finfo(float).eps * n * np.abs(A).max() * np.abs(B).max()
+    assert np.max(np.abs(got - ref)) <= bound
+    cn = golden_large["gemm_1024_colnrm1"]
+    assert np.max(np.abs(np.abs(Cm).sum(axis=0) - cn) / cn) <= 1e-12

@@ -28,6 +28,39 @@ def test_dgetrf_pivots_match_reference_fixtures(gb, ora, golden, order):
             assert (A[rows:, :] == -2.56e9).all()
 
 
+@pytest.mark.parametrize("n", [2048, 4096, 8192])
+def test_dgetrf_pivots_match_reference_at_headline_sizes(gb, ora, golden_large, n):
+    """clapack_dgetrf on the xdlutst-seeded n x n matrix against the
+    reference's own ATL_getrfC run on the same input (fixture): pivots bit
+    for bit, the diagonal of U to rounding, and the dgetrs solution of the
+    plain dgesv's right-hand side gegen(n, 1, n+1) against the reference's
+    ATL_getrs."""
+    A = ora.gegen(n, n, n * n + n)
+    ipiv = np.zeros(n, dtype=np.int32)
+    info = gb.clapack_dgetrf(102, n, n, A, n, ipiv)
+    assert info == int(golden_large[f"lu_{n}_info"])
+    ref = golden_large[f"lu_{n}_ipiv"]
+    mism = np.nonzero(ipiv != ref)[0]
+    assert mism.size == 0, f"pivot mismatch with the reference at columns {mism[:10]}"
+    ud = golden_large[f"lu_{n}_udiag"]
+    assert np.max(np.abs(np.diag(A) - ud)) <= 1e-9 * np.max(np.abs(ud))
+    x = ora.gegen(n, 1, n + 1)
+    gb.clapack_dgetrs(102, 111, n, 1, A, n, ipiv, x, n)
+    xr = golden_large[f"lu_{n}_x"]
+    assert np.linalg.norm(x[:, 0] - xr) <= 1e-8 * np.linalg.norm(xr)
+
+
+def test_sgetrf_pivots_match_reference_at_4096(gb, ora, golden_large):
+    """clapack_sgetrf (the reference semantics of the mixed solver's FP32
+    factor) against the reference's own FP32 ATL_getrfC at n = 4096."""
+    n = 4096
+    A = ora.gegen(n, n, n * n + n, dtype=np.float32)
+    ipiv = np.zeros(n, dtype=np.int32)
+    assert gb.clapack_sgetrf(102, n, n, A, n, ipiv) == int(golden_large[f"slu_{n}_info"])
+    mism = np.nonzero(ipiv != golden_large[f"slu_{n}_ipiv"])[0]
+    assert mism.size == 0, f"pivot mismatch with the reference at columns {mism[:10]}"
+
+
 @pytest.mark.parametrize("M,N,lda", [(500, 500, 500), (1000, 1000, 1001), (1537, 700, 1540), (300, 900, 300),
                                      (2048, 2048, 2048)])
 def test_dgetrf_matches_oracle_and_residual(gb, ora, M, N, lda):

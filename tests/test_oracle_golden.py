@@ -302,3 +302,24 @@ def test_cblas_iamax_random_against_reference_build(ora):
         for dt, f in ((np.float64, R.atlref_cblas_idamax), (np.float32, R.atlref_cblas_isamax)):
             x = np.asfortranarray(buf.astype(dt))
             assert ora.cblas_iamax(n, x, inc) == f(n, x, inc), (v, inc, dt)
+
+
+@pytest.mark.parametrize("n", [2048, 4096])
+def test_oracle_pivots_match_reference_at_large_sizes(ora, golden_large, n):
+    """The oracle's getrf against the reference's own ATL_getrfC at n = 2048
+    and 4096 (the n = 8192 pivots are checked against the GPU library)."""
+    A = ora.gegen(n, n, n * n + n)
+    info, ipiv = ora.getrf(A)
+    assert info == int(golden_large[f"lu_{n}_info"])
+    assert np.array_equal(ipiv, golden_large[f"lu_{n}_ipiv"])
+    assert np.max(np.abs(np.diag(A) - golden_large[f"lu_{n}_udiag"])) <= 1e-10
+
+
+def test_oracle_dgemm_1024_matches_reference_blas(ora, golden_large):
+    n = 1024
+    A = ora.gegen(n, n, n * n + 513 * 7 + 90)
+    B = ora.gegen(n, n, n * n + 127 * 50 + 77)
+    Cm = np.zeros((n, n), order="F")
+    ora.lib().ora_dgemm(111, 111, n, n, n, 1.0, A, n, B, n, 0.0, Cm, n)
+    got = Cm.reshape(-1, order="F")[golden_large["gemm_1024_idx"]]
+    assert np.max(np.abs(got - golden_large["gemm_1024_val"])) <= 2 * n * n * np.finfo(float).eps * 0.25
