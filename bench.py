@@ -55,6 +55,35 @@ def replica_throughput(world, flops_per_step, steps, max_ms):
     return world * flops_per_step * steps / (max_ms * 1e-3) / 1e12
 
 
+def bench_config(n, world):
+    """The workload both arms report (identical dicts, so the two lines compare
+    like for like)."""
+    return {"workload": f"dgesv FP64 plain form: clapack_dgetrf + clapack_dgetrs, ColMajor, n={n}, nrhs=1",
+            "n": n, "nrhs": 1, "parallelism": "replicas only" if world > 1 else "1 GPU",
+            "l2": "inputs larger than L2 (A is 512 MiB); A and b restored by a copy before each step, "
+                  "outside the timed region"}
+
+
+def ref_build_sample(O, n=1024):
+    """The reference's own ATL_getrfC + ATL_getrs (oracle/_ref, on its C
+    reference BLAS, one thread) on one dgesv of size n, or None when
+    oracle/_ref was not built."""
+    R = O.ref_lib()
+    if R is None:
+        return None
+    A = O.gegen(n, n, n * n + n)
+    b = O.gegen(n, 1, n + 1)
+    piv = np.zeros(n, dtype=np.int32)
+    t0 = time.perf_counter()
+    R.atlref_dgetrf(102, n, n, A, n, piv)
+    R.atlref_dgetrs(102, 111, n, 1, A, n, piv, b, n)
+    tc = time.perf_counter() - t0
+    return {"value": dgesv_flops(n) / tc / 1e12, "unit": UNIT, "cores": 1, "kind": "reference",
+            "sample": f"one dgesv n={n} nrhs=1 through the reference's own ATL_getrfC + ATL_getrs "
+                      "(extracted from its basefiles, oracle/_ref) on its C reference BLAS, one thread; "
+                      "not the tuned ATLAS kernels, which only its hours-long install search produces"}
+
+
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -159,14 +188,18 @@ def run_reference(args):
     ts = [cpu_dgesv_seconds(O, n) for _ in range(steps)]
     tot = sum(ts)
     value = dgesv_flops(n) * steps / tot / 1e12
-    sample = f"dgesv n={n} nrhs=1 per step (full workload n=8192)"
+    sample = f"dgesv n={n} nrhs=1 per step (full workload n={args.n}), oracle restatement of getrfC/getrs"
+    cpu = {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+    rb = ref_build_sample(O)
+    if rb is not None:
+        cpu["reference_build_sample"] = rb
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": steps, "warmup": warmup, "ms_per_step": tot / steps * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (ATL_gegen seeds)",
-        "config": {"workload": "dgesv FP64 plain form, clapack_dgetrf + clapack_dgetrs, n=8192 nrhs=1",
-                   "sample_n": n, "parallelism": "replicas only"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: ATL_gegen uniform(-0.5,0.5], xdlutst seed n*n+lda",
+        "config": bench_config(args.n, args.gpus),
+        "cpu_baseline": cpu,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -174,16 +207,46 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------- other forms
-def measure_forms(G, O, torch, n=16384, kappas=(1e2, 1e6, 1e10), nslices=8):
+def event_ms(torch, s, prep, run, reps):
+    """Device times (ms) of `run` over `reps` repetitions after one warm-up:
+    CUDA events on the library stream `s` around each call, `prep` (input
+    restores) outside them, a synchronize on both sides."""
+    ts = []
+    for rep in range(reps + 1):
+        prep()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        run()
+        e1.record(s)
+        torch.cuda.synchronize()
+        if rep:
+            ts.append(e0.elapsed_time(e1))
+    return ts
+
+
+def backward_error_dev(Am, x, b):
+    """Normwise backward error ||b - A x||inf / (||A||inf ||x||inf + ||b||inf)
+    in FP64 on the device, from the untouched matrix (an independent check:
+    the solver's own estimate is not used)."""
+    r = b - Am @ x
+    return float(r.abs().max() / (Am.abs().sum(dim=1).max() * x.abs().max() + b.abs().max()))
+
+
+def measure_forms(G, O, torch, n=16384, kappas=(1e2, 1e6, 1e10), nslices=8, reps=3):
     """The other FP64-accuracy forms at n=16384: mixed-precision dgesv and the
     split-DGEMM LU dgesv on A = U diag(s) V^T (U, V from Householder QR of
     seeded Gaussian matrices, s geometric 1..1/kappa) against the plain FP64
     dgesv on the same matrix, and the split-precision DGEMM on
     uniform[-1,1]*2^e operands (e in [-16,16]) against the double-double
-    oracle on sampled entries."""
+    oracle on sampled entries.  Every dgesv form is timed with CUDA events on
+    the library stream, median of `reps` after one warm-up; its backward error
+    is computed here from b - A x in FP64 on the original matrix, its forward
+    error against the plain FP64 solution of the same system."""
     import ctypes as C
     L = G.lib()
     st = L.atlg_stream()
+    s = torch.cuda.ExternalStream(st)
     out = {}
     dev = "cuda"
     g = torch.Generator(device=dev).manual_seed(4)
@@ -192,60 +255,87 @@ def measure_forms(G, O, torch, n=16384, kappas=(1e2, 1e6, 1e10), nslices=8):
     b = torch.randn(n, device=dev, dtype=torch.float64, generator=g)
     piv = torch.zeros(n, dtype=torch.int32, device=dev)
     info_d = torch.zeros(4, dtype=torch.int32, device=dev)
-    rows = []
-    srows = []
-    plain_t = None
+    rows, srows = [], []
+    plain = None
+    feps = np.finfo(float).eps
     for kappa in kappas:
         sv = torch.logspace(0, -np.log10(kappa), n, device=dev, dtype=torch.float64)
         Acm = ((U * sv) @ V.T).t().contiguous()      # column-major A
+        Am = Acm.T                                   # the matrix (a view of the column-major storage)
         A = torch.empty_like(Acm)
-        X = torch.zeros(n, device=dev, dtype=torch.float64)
-        berr, ferr, it, stt = C.c_double(), C.c_double(), C.c_int(), C.c_int()
-        ts = []
-        for rep in range(2):
+        torch.cuda.synchronize()
+
+        # plain FP64 dgesv: the denominator (timed once, on the first kappa:
+        # its time does not depend on the matrix) and the reference solution
+        xb = torch.empty_like(b)
+
+        def prep_plain():
             A.copy_(Acm)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            info = L.atlg_dgesv_mixed_dev(n, 1, A.data_ptr(), n, piv.data_ptr(), b.data_ptr(), n, X.data_ptr(), n,
-                                          C.byref(berr), C.byref(ferr), C.byref(it), C.byref(stt), st)
-            torch.cuda.synchronize()
-            ts.append(time.perf_counter() - t0)
-        row = {"kappa": kappa, "ms": min(ts) * 1e3, "tflops": dgesv_flops(n) / min(ts) / 1e12, "info": info,
-               "iters": it.value, "fallback_fp64": stt.value == 1, "backward_error": berr.value,
-               "n_eps": n * np.finfo(float).eps}
-        if plain_t is None or kappa == kappas[-1]:
-            A.copy_(Acm)
-            xb = b.clone()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
+            xb.copy_(b)
+
+        def run_plain():
             L.atlg_dgetrf_dev(n, n, A.data_ptr(), n, piv.data_ptr(), info_d.data_ptr(), st)
             L.atlg_dgetrs_dev(102, 111, n, 1, A.data_ptr(), n, piv.data_ptr(), xb.data_ptr(), n, st)
+
+        if plain is None:
+            pts = event_ms(torch, s, prep_plain, run_plain, reps)
+            plain = {"ms": statistics.median(pts), "ms_all": pts,
+                     "tflops": dgesv_flops(n) / statistics.median(pts) / 1e9}
+        else:
+            prep_plain()
             torch.cuda.synchronize()
-            plain_t = time.perf_counter() - t0
-            row["forward_vs_plain_fp64"] = float((X - xb).abs().max() / xb.abs().max())
-        row["speedup_vs_plain_fp64"] = plain_t / min(ts)
-        rows.append(row)
-        # split-DGEMM form: FP64 LU with tensor-core (integer-slice) updates
-        ts2 = []
-        for rep in range(2):
+            run_plain()
+            torch.cuda.synchronize()
+        x_plain = xb.clone()
+        plain_berr = backward_error_dev(Am, x_plain, b)
+
+        # mixed-precision dgesv
+        X = torch.zeros(n, device=dev, dtype=torch.float64)
+        berr, ferr, it, stt = C.c_double(), C.c_double(), C.c_int(), C.c_int()
+        infos = []
+
+        def prep_mixed():
             A.copy_(Acm)
-            xs = b.clone()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            sinfo = L.atlg_dgetrf_split_dev(n, A.data_ptr(), n, piv.data_ptr(), 8, 1024, st)
+
+        def run_mixed():
+            infos.append(L.atlg_dgesv_mixed_dev(n, 1, A.data_ptr(), n, piv.data_ptr(), b.data_ptr(), n,
+                                                X.data_ptr(), n, C.byref(berr), C.byref(ferr), C.byref(it),
+                                                C.byref(stt), st))
+
+        mts = event_ms(torch, s, prep_mixed, run_mixed, reps)
+        mms = statistics.median(mts)
+        rows.append({"kappa": kappa, "ms": mms, "ms_all": mts, "tflops": dgesv_flops(n) / mms / 1e9,
+                     "info": infos[-1], "iters": it.value, "fallback_fp64": stt.value == 1,
+                     "backward_error": backward_error_dev(Am, X, b), "backward_error_solver_estimate": berr.value,
+                     "forward_error_vs_plain_fp64": float((X - x_plain).abs().max() / x_plain.abs().max()),
+                     "plain_fp64_backward_error": plain_berr, "n_eps": n * feps,
+                     "speedup_vs_plain_fp64": plain["ms"] / mms})
+
+        # split-DGEMM form: FP64 LU with tensor-core (integer-slice) updates
+        xs = torch.empty_like(b)
+        sinfo = []
+
+        def prep_split():
+            A.copy_(Acm)
+            xs.copy_(b)
+
+        def run_split():
+            sinfo.append(L.atlg_dgetrf_split_dev(n, A.data_ptr(), n, piv.data_ptr(), nslices, 1024, st))
             L.atlg_dgetrs_dev(102, 111, n, 1, A.data_ptr(), n, piv.data_ptr(), xs.data_ptr(), n, st)
-            torch.cuda.synchronize()
-            ts2.append(time.perf_counter() - t0)
-        Am = Acm.T                                  # the column-major matrix
-        r = b - Am @ xs
-        sberr = float(r.abs().max() / (Am.abs().sum(dim=1).max() * xs.abs().max() + b.abs().max()))
-        srows.append({"kappa": kappa, "ms": min(ts2) * 1e3, "tflops": dgesv_flops(n) / min(ts2) / 1e12,
-                      "info": sinfo, "backward_error": sberr, "n_eps": n * np.finfo(float).eps,
-                      "speedup_vs_plain_fp64": plain_t / min(ts2)})
-        del A, Acm
+
+        sts = event_ms(torch, s, prep_split, run_split, reps)
+        sms = statistics.median(sts)
+        srows.append({"kappa": kappa, "ms": sms, "ms_all": sts, "tflops": dgesv_flops(n) / sms / 1e9,
+                      "info": sinfo[-1], "backward_error": backward_error_dev(Am, xs, b),
+                      "forward_error_vs_plain_fp64": float((xs - x_plain).abs().max() / x_plain.abs().max()),
+                      "n_eps": n * feps, "speedup_vs_plain_fp64": plain["ms"] / sms})
+        del A, Acm, Am, X, xs, xb, x_plain
+        torch.cuda.empty_cache()
+    timing = ("CUDA events on the library stream around the device call(s), median of %d after one warm-up; "
+              "matrix restored by a device copy outside the events" % reps)
+    out["plain_dgesv_n16384"] = dict(plain, timing=timing)
     out["mixed_dgesv_n16384"] = rows
     out["split_lu_dgesv_n16384"] = srows
-    out["plain_dgesv_n16384"] = {"ms": plain_t * 1e3, "tflops": dgesv_flops(n) / plain_t / 1e12}
     del U, V
     torch.cuda.empty_cache()
     # split-precision DGEMM 16384^3
@@ -254,20 +344,12 @@ def measure_forms(G, O, torch, n=16384, kappas=(1e2, 1e6, 1e10), nslices=8):
     B = (torch.rand(n, n, device=dev, dtype=torch.float64, generator=g) * 2 - 1) * \
         torch.exp2(torch.randint(-16, 17, (n, n), device=dev, generator=g).double())
     Cm = torch.zeros(n, n, device=dev, dtype=torch.float64)
-    s = torch.cuda.ExternalStream(st)
     torch.cuda.synchronize()      # the library stream does not wait for torch's stream
-    ts = []
-    for rep in range(3):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(s)
-        # column-major A, B: the torch tensors hold A^T row-major == A column-major
-        L.atlg_dgemm_split_dev(111, 111, n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0, Cm.data_ptr(), n,
-                               nslices, st)
-        e1.record(s)
-        torch.cuda.synchronize()
-        if rep:
-            ts.append(e0.elapsed_time(e1))
-    ms = min(ts)
+    # column-major A, B: the torch tensors hold A^T row-major == A column-major
+    ts = event_ms(torch, s, lambda: None,
+                  lambda: L.atlg_dgemm_split_dev(111, 111, n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0,
+                                                 Cm.data_ptr(), n, nslices, st), reps)
+    ms = statistics.median(ts)
     # accuracy on 64 sampled entries against the double-double oracle
     Ah = A.cpu().numpy().T      # column-major view of the device data
     Bh = B.cpu().numpy().T
@@ -280,13 +362,135 @@ def measure_forms(G, O, torch, n=16384, kappas=(1e2, 1e6, 1e10), nslices=8):
     got = Ch[ii, jj]
     rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
     absab = np.array([np.abs(Ah[i, :]) @ np.abs(Bh[:, j]) for i, j in zip(ii, jj)])
-    out["split_dgemm_n16384"] = {"nslices": nslices, "ms": ms, "tflops_fp64_equiv": 2.0 * n ** 3 / ms / 1e9,
+    out["split_dgemm_n16384"] = {"nslices": nslices, "ms": ms, "ms_all": ts,
+                                 "tflops_fp64_equiv": 2.0 * n ** 3 / ms / 1e9,
                                  "tensor_tflops": nslices * (nslices + 1) / 2 * 2.0 * n ** 3 / ms / 1e9,
                                  "max_rel_err_vs_double_double": float(rel.max()),
                                  "max_err_over_sum_abs_vs_double_double": float((np.abs(got - ref) / absab).max()),
-                                 "samples": 64}
+                                 "samples": 64, "timing": timing.replace("; matrix restored by a device copy "
+                                                                         "outside the events", "")}
     del A, B, Cm
     torch.cuda.empty_cache()
+    return out
+
+
+def measure_dgemm1024(G, O, torch, n=1024, reps=10):
+    """The plain DGEMM configuration: cblas_dgemm ColMajor NoTrans/NoTrans,
+    M = N = K = 1024, alpha 1, beta 0, operands from ATL_gegen with the
+    gemmtst seeds.  Device time with CUDA events on the library stream
+    (median of `reps` after warm-up; L2 flushed before each call by writing a
+    256 MiB buffer, outside the events: the operands, 24 MiB, would otherwise
+    stay in L2), against the FP64 peaks measured in this process (DFMA probe
+    and FP64 mma.sync probe); end to end through cblas_dgemm on pinned and on
+    pageable host arrays; the xdl3blastst residual against the oracle; the
+    oracle's blocked GEMM and the reference build's BLAS on the host cores."""
+    L = G.lib()
+    st = L.atlg_stream()
+    s = torch.cuda.ExternalStream(st)
+    A_h = O.gegen(n, n, n * n + 513 * 7 + 90)
+    B_h = O.gegen(n, n, n * n + 127 * 50 + 77)
+    C_h = O.gegen(n, n, n * n + 101 * 2 + 53)
+    dA = torch.from_numpy(np.ascontiguousarray(A_h.T)).cuda()
+    dB = torch.from_numpy(np.ascontiguousarray(B_h.T)).cuda()
+    dC = torch.zeros(n, n, device="cuda", dtype=torch.float64)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+
+    def prep():
+        with torch.cuda.stream(s):
+            flush.fill_(1)
+
+    run = lambda: L.atlg_dgemm_dev(111, 111, n, n, n, 1.0, dA.data_ptr(), n, dB.data_ptr(), n, 0.0,
+                                   dC.data_ptr(), n, st)
+    event_ms(torch, s, prep, run, 3)
+    ts = event_ms(torch, s, prep, run, reps)
+    ms = statistics.median(ts)
+    flops = 2.0 * n ** 3
+    tflops = flops / ms / 1e9
+    p64, _ = G.probe_peaks()
+    mma = G.probe_fp64_mma()
+    peak = max(p64, max(mma.values()))
+    # xdl3blastst residual of the device result against the oracle's product
+    Cg = dC.cpu().numpy().T.copy(order="F")
+    Ct = np.zeros((n, n), order="F")
+    O.set_threads(0)
+    t0 = time.perf_counter()
+    O.lib().ora_dgemm(111, 111, n, n, n, 1.0, A_h, n, B_h, n, 0.0, Ct, n)
+    tc = time.perf_counter() - t0
+    resid = O.gemm_resid(111, 111, n, n, n, 1.0, A_h, B_h, 0.0, C_h, Cg, Ct)
+
+    # end to end: cblas_dgemm on host arrays (copies inside the timed region)
+    def host_calls(Ah, Bh, Ch, k=5):
+        tt = []
+        for it in range(k + 1):
+            np.copyto(Ch, C_h)
+            t0 = time.perf_counter()
+            G.cblas_dgemm(102, 111, 111, n, n, n, 1.0, Ah, n, Bh, n, 0.0, Ch, n)
+            if it:
+                tt.append(time.perf_counter() - t0)
+        return statistics.median(tt) * 1e3
+
+    pin = [torch.empty((n, n), dtype=torch.float64).pin_memory() for _ in range(3)]
+    Ap, Bp, Cp = (t.numpy().T for t in pin)
+    np.copyto(Ap, A_h)
+    np.copyto(Bp, B_h)
+    e2e_pin = host_calls(Ap, Bp, Cp)
+    e2e_page = host_calls(A_h, B_h, np.asfortranarray(C_h.copy()))
+    row = {"M": n, "N": n, "K": n, "ms": ms, "ms_all": ts, "tflops": tflops,
+           "fp64_dfma_probe_tflops": p64, "fp64_mma_probe_tflops": mma, "fp64_peak_tflops": peak,
+           "frac_of_fp64_peak": tflops / peak, "frac_of_fp64_mma_probe": tflops / max(mma.values()),
+           "xdl3blastst_resid": resid, "resid_threshold": 50.0,
+           "e2e_pinned_ms": e2e_pin, "e2e_pinned_tflops": flops / e2e_pin / 1e9,
+           "e2e_pageable_ms": e2e_page, "e2e_pageable_tflops": flops / e2e_page / 1e9,
+           "e2e_bytes": {"h2d": 2 * 8 * n * n, "d2h": 8 * n * n},
+           "timing": "CUDA events on the library stream around atlg_dgemm_dev, median of %d after 3 warm-ups, "
+                     "L2 flushed (256 MiB write) before each call outside the events; e2e: wall clock around "
+                     "cblas_dgemm, median of 5" % reps,
+           "cpu_baseline": {"value": flops / tc / 1e12, "unit": "TFLOP/s", "cores": O.get_threads(), "kind": "port",
+                            "sample": f"one oracle blocked dgemm {n}^3 (OpenMP)"}}
+    R = O.ref_lib()
+    if R is not None:
+        Cr = np.zeros((n, n), order="F")
+        t0 = time.perf_counter()
+        R.atlref_dgemm(102, 111, 111, n, n, n, 1.0, A_h, n, B_h, n, 0.0, Cr, n)
+        tr = time.perf_counter() - t0
+        row["cpu_baseline"]["reference_build_sample"] = {
+            "value": flops / tr / 1e12, "unit": "TFLOP/s", "cores": 1, "kind": "reference",
+            "sample": f"one dgemm {n}^3 on the reference's C reference BLAS (oracle/_ref), one thread"}
+    del dA, dB, dC, flush, pin
+    torch.cuda.empty_cache()
+    return row
+
+
+def target_summary(forms, dgemm):
+    """The metric's comparison in one small object: the FP64-accurate dgesv
+    forms at n = 16384 against the plain FP64 form (target: at least 3x at
+    backward error <= n eps), and the plain DGEMM at 1024^3 against the FP64
+    peaks (target: at least 0.8)."""
+    out = {}
+    if forms:
+        plain = forms["plain_dgesv_n16384"]["ms"]
+        out["plain_fp64_dgesv_n16384_ms"] = plain
+        ok = True
+        for r, sr in zip(forms["mixed_dgesv_n16384"], forms["split_lu_dgesv_n16384"]):
+            k = "k%.0e" % r["kappa"]
+            acc_m = r["backward_error"] <= r["n_eps"]
+            acc_s = sr["backward_error"] <= sr["n_eps"]
+            best = max(r["speedup_vs_plain_fp64"] if acc_m else 0.0, sr["speedup_vs_plain_fp64"] if acc_s else 0.0)
+            out[k] = {"mixed_ms": round(r["ms"], 2), "mixed_speedup": round(r["speedup_vs_plain_fp64"], 2),
+                      "mixed_berr": r["backward_error"], "mixed_ferr_vs_plain": r["forward_error_vs_plain_fp64"],
+                      "mixed_iters": r["iters"], "mixed_fallback": r["fallback_fp64"],
+                      "split_lu_ms": round(sr["ms"], 2), "split_lu_speedup": round(sr["speedup_vs_plain_fp64"], 2),
+                      "split_lu_berr": sr["backward_error"], "best_fp64_accurate_speedup": round(best, 2)}
+            ok = ok and best >= 3.0
+        out["n_eps"] = forms["mixed_dgesv_n16384"][0]["n_eps"]
+        out["dgesv_3x_target_met"] = ok
+    if dgemm:
+        out["dgemm_n1024_tflops"] = dgemm["tflops"]
+        out["dgemm_n1024_frac_of_fp64_peak"] = dgemm["frac_of_fp64_peak"]
+        out["fp64_peak_tflops"] = dgemm["fp64_peak_tflops"]
+        out["dgemm_0p8_target_met"] = dgemm["frac_of_fp64_peak"] >= 0.8
+    out["timing"] = "CUDA events on the library stream, median of 3 (dgesv) / 10 (dgemm) after warm-up"
     return out
 
 
@@ -693,6 +897,21 @@ def run_gpu(args):
             e2e_t.append(t1 - t0)
     e2e_ms = max_over_ranks(dist, 1e3 * sum(e2e_t) / len(e2e_t), "cuda")
     e2e_val = replica_throughput(world, flops, 1, e2e_ms)
+    # the same call on pageable (malloc'd) host arrays, as a drop-in caller passes them
+    A_pg = np.asfortranarray(A_h.copy())
+    b_pg = np.asfortranarray(b_h.copy())
+    pg_t = []
+    for it in range(e2e_steps + 1):
+        np.copyto(A_pg, A_h)
+        np.copyto(b_pg, b_h)
+        t0 = time.perf_counter()
+        rc = G.clapack_dgesv(102, n, nrhs, A_pg, n, piv_h, b_pg, n)
+        t1 = time.perf_counter()
+        assert rc == 0
+        if it > 0:
+            pg_t.append(t1 - t0)
+    pg_ms = max_over_ranks(dist, 1e3 * sum(pg_t) / len(pg_t), "cuda")
+    del A_pg, b_pg
 
     # ---- roofline of the dominant kernel (the trailing-update DGEMM) ----
     p64, _ = G.probe_peaks()
@@ -702,7 +921,9 @@ def run_gpu(args):
         "kernel": "gemm_kernel<double> (LU trailing update)",
         "achieved": gemm_tflops, "peak": p64, "unit": "TFLOP/s",
         "frac": (gemm_tflops / p64) if gemm_tflops else None,
-        "peak_source": "FP64 FMA-throughput probe run in this process (MEASURED_PEAKS.json has no FP64 entry)",
+        "peak_source": "FP64 FMA-throughput probe run in this process (MEASURED_PEAKS.json has no FP64 entry); "
+                       "the FP64 mma.sync probe is below it (fp64_mma_probe)",
+        "fp64_mma_probe": G.probe_fp64_mma(),
         "traffic": traffic_from_profiles(),
         "launches_per_step": gemm_n / args.steps, "share_of_step": gemm_ms / dev_ms,
     }
@@ -716,10 +937,15 @@ def run_gpu(args):
             tc = cpu_dgesv_seconds(O, ncpu)
             cpu = {"value": dgesv_flops(ncpu) / tc / 1e12, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"one dgesv n={ncpu} nrhs=1 (oracle restatement of getrfC/getrs, OpenMP)"}
+            rb = ref_build_sample(O)
+            if rb is not None:
+                cpu["reference_build_sample"] = rb
         bwd = O.backward_error(np.asfortranarray(A_h), x, b_h.reshape(-1))
         forms = None
         nxt = None
+        dgemm = None
         if world == 1 and not args.skip_extras:
+            dgemm = measure_dgemm1024(G, O, torch)
             forms = measure_forms(G, O, torch)
             forms["adjoint_n4096"] = measure_adjoint(G, O, torch)
             nxt = measure_next(G, O, torch)
@@ -729,23 +955,27 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: ATL_gegen uniform(-0.5,0.5], xdlutst seed n*n+lda",
-            "config": {"workload": "dgesv FP64 plain form: clapack_dgetrf + clapack_dgetrs, ColMajor, n=8192, nrhs=1",
-                       "n": n, "nrhs": nrhs, "parallelism": "replicas only" if world > 1 else "1 GPU",
-                       "l2": "inputs larger than L2 (A is 512 MiB); A and b restored by a device copy before "
-                             "each step, outside the event-timed region"},
+            "config": bench_config(n, world),
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs,
                     "d2h_bytes_per_step": 8 * n * n + 4 * n + 8 * n * nrhs + 4,
-                    "api": "clapack_dgesv on pinned host arrays", "steps": e2e_steps},
+                    "api": "clapack_dgesv on pinned host arrays", "steps": e2e_steps,
+                    "pageable": {"value": replica_throughput(world, flops, 1, pg_ms), "unit": UNIT,
+                                 "ms": pg_ms, "api": "clapack_dgesv on pageable (malloc'd numpy) host arrays"}},
             "gpu_launches": launches,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clk,
             "accuracy": {"backward_error": bwd, "n_eps": n * np.finfo(float).eps},
         }
+        if dgemm is not None:
+            line["dgemm_n1024"] = dgemm
         if forms is not None:
             line["forms"] = forms
         if nxt is not None:
             line["next_rows"] = nxt
+        if forms is not None or dgemm is not None:
+            # last, so that it is in the tail of the output when the line is long
+            line["targets"] = target_summary(forms, dgemm)
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
@@ -757,7 +987,7 @@ def run_case(args):
     """Single-kernel workloads for profiling runs (ncu captures in profiles/):
     split  -- split-precision DGEMM n^3 (7 slices), run twice
     sgetrf -- FP32 LU (FFMA trailing update) at n
-    mixed  -- mixed-precision dgesv at n on A = G/sqrt(n) + 4I, run twice
+    mixed  -- mixed-precision dgesv at n on A = G/sqrt(n) + 4I (--kappa: U diag(s) V^T), run twice
     potrf  -- FP64 Cholesky (Lower) at n on a diagonally dominant SPD matrix
     trmm   -- FP64 TRMM Left/Upper/NoTrans at M = N = n
     getri  -- FP64 inverse from the dgetrf factors at n
@@ -910,8 +1140,15 @@ def run_case(args):
             torch.cuda.synchronize()
             ms = (time.perf_counter() - t0) * 1e3
     else:
-        A0 = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g) / n ** 0.5 + \
-            4 * torch.eye(n, device="cuda", dtype=torch.float64)
+        if args.kappa > 0:     # A = U diag(s) V^T, s geometric from 1 to 1/kappa (the mixed-precision config)
+            U, _ = torch.linalg.qr(torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g))
+            V, _ = torch.linalg.qr(torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g))
+            sv = torch.logspace(0, -np.log10(args.kappa), n, device="cuda", dtype=torch.float64)
+            A0 = ((U * sv) @ V.T).t().contiguous()
+            del U, V
+        else:
+            A0 = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g) / n ** 0.5 + \
+                4 * torch.eye(n, device="cuda", dtype=torch.float64)
         b = torch.randn(n, device="cuda", dtype=torch.float64, generator=g)
         A = A0.clone()
         X = torch.zeros(n, device="cuda", dtype=torch.float64)
@@ -941,6 +1178,8 @@ def main():
     ap.add_argument("--leaf", type=int, default=0, help="FP64 leaf width of --case splitlu (0: default)")
     ap.add_argument("--pw", type=int, default=0, help="FP64 LU panel width for --case splitlu/dgetrf (0: default)")
     ap.add_argument("--grid", type=int, default=0, help="grid-panel CTAs for --case splitlu/dgetrf (0: default)")
+    ap.add_argument("--kappa", type=float, default=0.0,
+                    help="--case mixed: A = U diag(s) V^T with condition number kappa (0: G/sqrt(n) + 4I)")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
     ap.add_argument("--case", choices=["split", "sgetrf", "dgetrf", "mixed", "potrf", "trmm", "getri", "splitlu",
                                        "laswp", "idamax"], default=None,

@@ -53,7 +53,7 @@ def test_noalloc_null_stream_follows_a_factorization_on_the_library_stream(gb, o
     factorization wrote."""
     torch = pytest.importorskip("torch")
     L = gb.lib()
-    n = 1536
+    n = 1024                           # 8 MiB of gathered rows: within the fixed scratch
     A = ora.gegen(n, n, n * n + n)
     dA1 = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()
     dA2 = dA1.clone()
