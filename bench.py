@@ -1150,6 +1150,8 @@ def run_case(args):
             A0 = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g) / n ** 0.5 + \
                 4 * torch.eye(n, device="cuda", dtype=torch.float64)
         b = torch.randn(n, device="cuda", dtype=torch.float64, generator=g)
+        if args.trsv >= 0:
+            L.atlg_refine_trsv(args.trsv)
         A = A0.clone()
         X = torch.zeros(n, device="cuda", dtype=torch.float64)
         piv = torch.zeros(n, dtype=torch.int32, device="cuda")
@@ -1162,7 +1164,10 @@ def run_case(args):
                                    C.byref(berr), C.byref(ferr), C.byref(it), C.byref(stt), st)
             torch.cuda.synchronize()
             ms = (time.perf_counter() - t0) * 1e3
-    print(json.dumps({"case": args.case, "n": n, "ms": ms, "status": int(L.atlg_status())}), flush=True)
+    extra = {}
+    if args.case == "mixed":
+        extra = {"iters": it.value, "fallback": stt.value == 1, "kappa": args.kappa, "trsv": args.trsv}
+    print(json.dumps(dict({"case": args.case, "n": n, "ms": ms, "status": int(L.atlg_status())}, **extra)), flush=True)
     return 0
 
 
@@ -1178,6 +1183,8 @@ def main():
     ap.add_argument("--leaf", type=int, default=0, help="FP64 leaf width of --case splitlu (0: default)")
     ap.add_argument("--pw", type=int, default=0, help="FP64 LU panel width for --case splitlu/dgetrf (0: default)")
     ap.add_argument("--grid", type=int, default=0, help="grid-panel CTAs for --case splitlu/dgetrf (0: default)")
+    ap.add_argument("--trsv", type=int, default=-1,
+                    help="--case mixed: refinement TRSV, 1 chained (128-row blocks), 0 look-back (64-row); -1 default")
     ap.add_argument("--kappa", type=float, default=0.0,
                     help="--case mixed: A = U diag(s) V^T with condition number kappa (0: G/sqrt(n) + 4I)")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")

@@ -257,6 +257,11 @@ int atlg_dlaswp_noalloc(int N, double *A, int lda, int K1, int K2, const int *ip
  * block cluster's shared memory with the cluster kernel, 0 always uses the
  * cooperative-grid kernel; both give bit-identical factors and pivots */
 void atlg_panel_cluster(int on);
+/* refinement solves of dgesv_mixed with one right-hand side (no reference
+ * counterpart): 1 (default) the chained TRSV over 128-row blocks with block
+ * inverses formed once per factorization, 0 the 64-row look-back TRSV; both
+ * converge to the same FP64-accurate solution */
+void atlg_refine_trsv(int chained);
 /* CTAs of the cooperative-grid LU panel (0: the default, a quarter of the SMs
  * when the factorization overlaps its updates); results do not depend on it */
 void atlg_panel_grid(int ctas);

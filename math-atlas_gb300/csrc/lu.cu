@@ -765,27 +765,77 @@ __global__ void laswp_perm_kernel(const int *ipiv, int K1, int K2, int inci, int
 // the forward result is content[i] = V(prev(i)), or ipiv[i] when i is the
 // first source of its target, or V(i) for a self-interchange (i in [K1,K2));
 // content[x] = V(last(x)), or x when nothing targets x (elsewhere).  The
-// backward order (inci < 0) gives the inverse permutation.  One CTA: warp 0
-// finds prev/last 32 sources at a time (__match_any_sync groups equal
-// targets), pointer jumping resolves V in log2(n) rounds.  Pivot vectors that
-// do not look down run the one-thread chain on the same shared arrays.
+// backward order (inci < 0) gives the inverse permutation.  One CTA.
+// prev/last come from a counting sort of the sources by target: counts per
+// target (shared-memory atomics), an exclusive scan over the targets, each
+// source dropped into its target's bucket, then one thread per target sorts
+// its (few) sources and links them -- every step parallel over the CTA.
+// When some target has more than kBucketMax sources, or the buckets do not
+// fit, warp 0 finds prev/last 32 sources at a time instead
+// (__match_any_sync groups equal targets).  Pointer jumping resolves V in
+// log2(n) rounds.  Pivot vectors that do not look down run the one-thread
+// chain on the same shared arrays.
 // Shared memory: ints r[n] (pivots, then the encoded prev), ptr[n], val[n],
-// ls[nrows] (last(x)).
+// ls[nrows] (last(x)); with buckets also cnt[nrows + 1] and bkt[n].
 constexpr int kChainThreads = 1024;
 constexpr int kChainPer = 16;                       // sources per thread in the jumping rounds
 constexpr size_t kChainSmemMax = 200 * 1024;
+constexpr int kBucketMax = 64;                      // sources per target sorted by one thread
 
-static size_t chain_smem_bytes(int nrows, int n) { return sizeof(int) * (3 * (size_t)n + (size_t)nrows); }
+static size_t chain_smem_bytes(int nrows, int n, bool buckets) {
+  return sizeof(int) * (3 * (size_t)n + (size_t)nrows + (buckets ? (size_t)nrows + 1 + n : 0));
+}
 static bool chain_fits(int nrows, int n) {
-  return n <= kChainThreads * kChainPer && chain_smem_bytes(nrows, n) <= kChainSmemMax;
+  return n <= kChainThreads * kChainPer && chain_smem_bytes(nrows, n, false) <= kChainSmemMax;
+}
+static bool chain_bucket_fits(int nrows, int n) {
+  return n <= kChainThreads * kChainPer && chain_smem_bytes(nrows, n, true) <= kChainSmemMax;
+}
+
+// Exclusive scan of v[0..m) in place by the whole CTA (kChainThreads
+// threads); returns the total.
+__device__ int cta_exclusive_scan(int *v, int m, int *wsum) {
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int per = (m + kChainThreads - 1) / kChainThreads;
+  const int b = tid * per, e = min(b + per, m);
+  int sum = 0;
+  for (int i = b; i < e; ++i) sum += v[i];
+  int incl = sum;                                    // warp inclusive scan of the segment sums
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) wsum[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    int x = wsum[lane], xi = x;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, xi, o);
+      if (lane >= o) xi += t;
+    }
+    wsum[lane] = xi - x;                             // exclusive over warps
+    if (lane == 31) wsum[32] = xi;
+  }
+  __syncthreads();
+  int run = wsum[w] + incl - sum;
+  for (int i = b; i < e; ++i) {
+    const int t = v[i];
+    v[i] = run;
+    run += t;
+  }
+  const int total = wsum[32];
+  __syncthreads();
+  return total;
 }
 
 __global__ void __launch_bounds__(kChainThreads)
-    laswp_chain_kernel(const int *ipiv, int K1, int K2, int inci, int *content_g, int nrows) {
+    laswp_chain_kernel(const int *ipiv, int K1, int K2, int inci, int *content_g, int nrows, int buckets) {
   extern __shared__ int ch_smem[];
+  __shared__ int wsum[33];
   const int n = K2 - K1;
   const int step = inci > 0 ? inci : -inci;
   int *r = ch_smem, *ptr = ch_smem + n, *val = ch_smem + 2 * n, *ls = ch_smem + 3 * n;
+  int *cnt = ls + nrows, *bkt = cnt + nrows + 1;
   const int tid = threadIdx.x;
   int viol = 0;
   for (int x = tid; x < nrows; x += kChainThreads) ls[x] = -1;
@@ -810,7 +860,54 @@ __global__ void __launch_bounds__(kChainThreads)
     for (int x = tid; x < nrows; x += kChainThreads) content_g[x] = ls[x];
     return;
   }
-  if (tid < 32) {                      // prev(j) into r, last(x) into ls, 32 sources at a time
+  bool linked = false;
+  if (buckets) {                       // counting sort of the sources by target
+    for (int x = tid; x <= nrows; x += kChainThreads) cnt[x] = 0;
+    __syncthreads();
+    for (int s = tid; s < n; s += kChainThreads) {
+      const int j = K1 + s, ip = r[s];
+      if (ip != j && ip >= 0 && ip < nrows) atomicAdd(&cnt[ip], 1);
+    }
+    __syncthreads();
+    cta_exclusive_scan(cnt, nrows, wsum);
+    for (int s = tid; s < n; s += kChainThreads) {
+      const int j = K1 + s, ip = r[s];
+      if (ip != j && ip >= 0 && ip < nrows) bkt[atomicAdd(&cnt[ip], 1)] = j;
+    }
+    __syncthreads();
+    // cnt[x] is now the end of bucket x, cnt[x-1] its start
+    int big = 0;
+    for (int x = tid; x < nrows; x += kChainThreads) {
+      const int b0 = x ? cnt[x - 1] : 0, b1 = cnt[x];
+      if (b1 - b0 > kBucketMax) big = 1;
+    }
+    if (!__syncthreads_or(big)) {
+      for (int s = tid; s < n; s += kChainThreads) {   // sources that move nothing: V(j)
+        const int j = K1 + s, ip = r[s];
+        if (!(ip != j && ip >= 0 && ip < nrows)) r[s] = j;
+      }
+      __syncthreads();
+      for (int x = tid; x < nrows; x += kChainThreads) {
+        const int b0 = x ? cnt[x - 1] : 0, b1 = cnt[x];
+        if (b1 == b0) continue;
+        for (int a = b0 + 1; a < b1; ++a) {          // insertion sort by source
+          const int v = bkt[a];
+          int c = a - 1;
+          while (c >= b0 && bkt[c] > v) { bkt[c + 1] = bkt[c]; --c; }
+          bkt[c + 1] = v;
+        }
+        int prev = -2 - x;                             // the first source receives original row x
+        for (int a = b0; a < b1; ++a) {
+          const int j = bkt[a];
+          r[j - K1] = prev;
+          prev = j;
+        }
+        ls[x] = prev;
+      }
+      linked = true;
+    }
+  }
+  if (!linked && tid < 32) {           // prev(j) into r, last(x) into ls, 32 sources at a time
     const int lane = tid;
     for (int s0 = 0; s0 < n; s0 += 32) {
       const int s = s0 + lane, j = K1 + s;
@@ -892,9 +989,13 @@ static void launch_interchange_table(const int *ipiv, int K1, int K2, int inci, 
                                      cudaStream_t st) {
   const int n = K2 - K1;
   if (chain_fits(nrows, n)) {
+    // the warp scan takes n/32 dependent rounds: cheap for a block column's
+    // interchanges, the counting sort wins for a whole pivot vector
+    const bool bk = n > 2048 && chain_bucket_fits(nrows, n);
     ATLG_CHECK(cudaFuncSetAttribute(laswp_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)kChainSmemMax));
-    laswp_chain_kernel<<<1, kChainThreads, chain_smem_bytes(nrows, n), st>>>(ipiv, K1, K2, inci, content, nrows);
+    laswp_chain_kernel<<<1, kChainThreads, chain_smem_bytes(nrows, n, bk), st>>>(ipiv, K1, K2, inci, content,
+                                                                                 nrows, bk ? 1 : 0);
   } else {
     const int mode = ((long)nrows + n <= kPermSmemRows) ? 2 : (nrows <= kPermSmemRows ? 1 : 0);
     const size_t smem = mode == 2 ? sizeof(int) * ((size_t)nrows + n) : mode == 1 ? sizeof(int) * (size_t)nrows : 0;
@@ -1083,6 +1184,15 @@ void dev_sgetrs_perm(int n, const float *LU, int lda, const int *perm, float *x,
   dev_strsv_inv(kUpper, kNoTrans, kNonUnit, n, LU, lda, x, st);
 }
 
+void dev_sgetrs_perm_chain(int n, const float *LU, int lda, const int *perm, float *x, float *tmp, const float *wsL,
+                           const float *wsU, cudaStream_t st) {
+  permute_vec_kernel<float><<<(n + 255) / 256, 256, 0, st>>>(n, perm, x, tmp);
+  note_launch();
+  dev_strsv_chain(kLower, n, LU, lda, wsL, tmp, st);
+  dev_strsv_chain(kUpper, n, LU, lda, wsU, tmp, st);
+  ATLG_CHECK(cudaMemcpyAsync(x, tmp, sizeof(float) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+}
+
 void dev_dlaswp(int N, double *A, int lda, int K1, int K2, const int *ipiv, int inci, int nrows, cudaStream_t st) {
   laswp_impl<double>(N, A, lda, K1, K2, ipiv, inci, nrows, st);
 }
@@ -1248,12 +1358,13 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
         ATLG_CHECK(cudaLaunchCooperativeKernel((const void *)panel_kernel<T, false>, dim3(G), dim3(PT), args, 0, st));
     }
     note_launch();
+    const int c_from = k + jb;
+    const int nxt = (c_from < MN) ? ((MN - c_from < PW) ? MN - c_from : PW) : 0;
     // the interchanges touch every other column: the side update must be done
     if (side_pending) {
       ATLG_CHECK(cudaStreamWaitEvent(st, ev_side, 0));
       side_pending = false;
     }
-    const int c_from = k + jb;
     const int nl = (k + 31) / 32, nr = (N - c_from + 31) / 32;
     if (nl + nr > 0) {
       apply_perm_kernel<T><<<nl + nr, 256, 0, st>>>(A, lda, k, perm, k, c_from, N);
@@ -1275,7 +1386,6 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
           dev_sgemm_tf32x3_pack_a(m, jb, (const float *)L21, lda, Ap, st);
           dev_sgemm_tf32x3_pack_b(jb, ntot, (const float *)U12, lda, Bp, st);
         }
-        const int nxt = (c_from < MN) ? ((MN - c_from < PW) ? MN - c_from : PW) : 0;
         if (lookahead && nxt > 0 && c_from + nxt < N) {
           trailing_update<T>(use_tc, m, nxt, jb, L21, U12, C, lda, 0, ntot, Ap, Bp, st);
           ATLG_CHECK(cudaEventRecord(ev_ready, st));

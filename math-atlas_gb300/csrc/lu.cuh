@@ -33,6 +33,9 @@ void dev_sgetrs(int order, int trans, int N, int NRHS, const float *A, int lda, 
                 cudaStream_t st);
 void dev_perm_from_ipiv(const int *ipiv, int n, int *perm, cudaStream_t st);
 void dev_sgetrs_perm(int n, const float *LU, int lda, const int *perm, float *x, float *tmp, cudaStream_t st);
+// the same solve through the chained TRSV (wsL, wsU from dev_strsv_chain_prepare)
+void dev_sgetrs_perm_chain(int n, const float *LU, int lda, const int *perm, float *x, float *tmp, const float *wsL,
+                           const float *wsU, cudaStream_t st);
 unsigned lu_status_read_and_clear();
 
 }  // namespace atlg

@@ -27,6 +27,7 @@
 #include "lu.cuh"
 #include "lu_split.cuh"
 #include "mixed.cuh"
+#include "trsm.cuh"
 
 namespace atlg {
 
@@ -115,6 +116,9 @@ static std::vector<double> colmax_host(int M, int N, const double *V, int ldv, d
   return h;
 }
 
+static bool g_refine_chained = true;
+void set_refine_trsv_chained(bool on) { g_refine_chained = on; }
+
 int dev_dgesv_mixed(int n, int nrhs, double *A, int lda, int *ipiv, const double *B, int ldb, double *X, int ldx,
                     MixedResult *res, cudaStream_t st) {
   Context &c = ctx();
@@ -156,15 +160,25 @@ int dev_dgesv_mixed(int n, int nrhs, double *A, int lda, int *ipiv, const double
   if (!fallback) {
     // one right-hand side: the row permutation is computed once and every
     // solve is a gather plus two single-launch triangular solves
+    // (a gather plus two chained triangular solves whose 128 x 128 block
+    // inverses and couplings are formed once here)
     int *perm = nullptr;
-    float *tmp32 = nullptr;
+    float *tmp32 = nullptr, *wsL = nullptr, *wsU = nullptr;
+    const bool chained = g_refine_chained;
     if (nrhs == 1) {
       perm = static_cast<int *>(c.buffer(kBufV1, sizeof(int) * (size_t)n + sizeof(float) * (size_t)n + 256));
       tmp32 = reinterpret_cast<float *>(perm + ((n + 63) & ~63));
       dev_perm_from_ipiv(ipiv, n, perm, st);
+      if (chained) {
+        wsL = static_cast<float *>(c.buffer(kBufTrsvL, sizeof(float) * strsv_chain_ws_floats(n)));
+        wsU = static_cast<float *>(c.buffer(kBufTrsvU, sizeof(float) * strsv_chain_ws_floats(n)));
+        dev_strsv_chain_prepare(kLower, kUnit, n, S, lds, wsL, st);
+        dev_strsv_chain_prepare(kUpper, kNonUnit, n, S, lds, wsU, st);
+      }
     }
     auto solve32 = [&](float *v) {
-      if (nrhs == 1) dev_sgetrs_perm(n, S, lds, perm, v, tmp32, st);
+      if (nrhs == 1 && chained) dev_sgetrs_perm_chain(n, S, lds, perm, v, tmp32, wsL, wsU, st);
+      else if (nrhs == 1) dev_sgetrs_perm(n, S, lds, perm, v, tmp32, st);
       else dev_sgetrs(kColMajor, kNoTrans, n, nrhs, S, lds, ipiv, v, lds, st);
     };
     // x0 = (A32)^-1 b in FP32, promoted

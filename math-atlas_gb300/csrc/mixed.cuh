@@ -16,5 +16,8 @@ struct MixedResult {
 // (then it holds the FP64 factors); B is unchanged; X receives the solution.
 int dev_dgesv_mixed(int n, int nrhs, double *A, int lda, int *ipiv, const double *B, int ldb, double *X, int ldx,
                     MixedResult *res, cudaStream_t st);
+// Single right-hand side refinement solves: the chained 128-row TRSV (true)
+// or the tagged 64-row look-back TRSV (false).
+void set_refine_trsv_chained(bool on);
 
 }  // namespace atlg

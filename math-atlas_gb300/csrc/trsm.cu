@@ -525,6 +525,8 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+static unsigned long long *trsv_pub_words(int n, unsigned *epoch, cudaStream_t st);
+
 // op(A) x = x for one right-hand side (incx = 1), cblas Uplo/Trans/Diag.
 template <typename T>
 static void trsv_impl(int uplo, int tA, int diag, int n, const T *A, int lda, T *x, cudaStream_t st,
@@ -556,12 +558,285 @@ void dev_strsv_inv(int uplo, int ta, int diag, int n, const float *A, int lda, f
     trsv_impl<float>(uplo, ta, diag, n, A, lda, x, st, true);
     return;
   }
-  // published words: zeroed whenever the buffer is new, epochs from 1
+  const int nb = (n + TV_B - 1) / TV_B;
+  int *tk = static_cast<int *>(ctx().buffer(kBufV0, sizeof(int) * (size_t)(nb + 32)));
+  unsigned epoch = 0;
+  unsigned long long *pub = trsv_pub_words(n, &epoch, st);
+  ATLG_CHECK(cudaMemsetAsync(tk, 0, sizeof(int), st));
+  trsv_tagged_kernel<<<nb, 256, 0, st>>>(n, A, lda, uplo == kLower ? 1 : 0, diag == kUnit ? 1 : 0, x, pub, epoch,
+                                         tk);
+  note_launch();
+  ATLG_CHECK(cudaGetLastError());
+}
+
+// ------------------------------------------------------------ chained TRSV
+// The mixed solver solves with one pair of FP32 triangular factors for up to
+// 30 right-hand sides in a row.  trsv_chain_prep_kernel forms, once per
+// factorization and for every 128-row block b of a triangle T, the inverse of
+// its diagonal block Inv_b = T_bb^-1 and its coupling M_b = Inv_b T_bp to the
+// block p solved just before it (p = b-1 for a lower triangle, b+1 for an
+// upper one).  trsv_chain_kernel then solves with one CTA per block, blocks
+// taken in solve order from an atomic ticket.  While the chain advances, a
+// CTA streams the blocks solved two or more steps earlier and forms
+// z_b = Inv_b (x_b - sum_c T_bc x_c); when x_p is published its own step is
+// x_b = z_b - M_b x_p, one 128 x 128 product from shared memory.  Published
+// values are 64-bit words (float value, call epoch), polled directly, so a
+// value arrives with its signal.  A CTA only waits on blocks whose tickets
+// were taken before its own; every wait is bounded.
+constexpr int TC_B = 128;                  // rows per block
+constexpr int TC_T = 512;                  // threads per CTA
+constexpr int TC_LD = 132;                 // shared row stride: four 32-float quarters, each padded by one
+constexpr size_t kChainPrepSmem = sizeof(float) * 3 * TC_B * (TC_B + 1);
+constexpr size_t kChainSmem = sizeof(float) * 2 * TC_B * TC_LD;
+
+__global__ void __launch_bounds__(TC_T)
+    trsv_chain_prep_kernel(int n, const float *__restrict__ A, int lda, int lower, int unit, float *ws) {
+  extern __shared__ float sm[];
+  float *tri = sm;                         // [128][129]: the diagonal block
+  float *inv = tri + TC_B * (TC_B + 1);    // [128][129]: its inverse
+  float *cpl = inv + TC_B * (TC_B + 1);    // [128][129]: the coupling block T_bp
+  __shared__ float rinv[TC_B];
+  constexpr int L = TC_B + 1;
+  const int nb = (n + TC_B - 1) / TC_B;
+  const int b = blockIdx.x;
+  const int r0 = b * TC_B, nr = min(TC_B, n - r0);
+  const int p = lower ? b - 1 : b + 1;
+  const int c0 = p * TC_B, nc = (p >= 0 && p < nb) ? min(TC_B, n - c0) : 0;
+  for (int e = threadIdx.x; e < TC_B * TC_B; e += TC_T) {
+    const int i = e % TC_B, k = e / TC_B;
+    tri[i * L + k] = (i < nr && k < nr) ? A[(r0 + i) + (size_t)(r0 + k) * lda] : 0.0f;
+    cpl[i * L + k] = (i < nr && k < nc) ? A[(r0 + i) + (size_t)(c0 + k) * lda] : 0.0f;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < TC_B; i += TC_T) rinv[i] = (i < nr) ? (unit ? 1.0f : 1.0f / tri[i * L + i]) : 0.0f;
+  __syncthreads();
+  if (threadIdx.x < TC_B) {   // column j of the inverse by substitution, four partial sums
+    const int j = threadIdx.x;
+    for (int i = 0; i < TC_B; ++i) inv[i * L + j] = 0.0f;
+    if (j < nr) {
+      inv[j * L + j] = rinv[j];
+      if (lower) {
+        for (int i = j + 1; i < nr; ++i) {
+          float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+          int k = j;
+          for (; k + 3 < i; k += 4) {
+            s0 = fmaf(tri[i * L + k], inv[k * L + j], s0);
+            s1 = fmaf(tri[i * L + k + 1], inv[(k + 1) * L + j], s1);
+            s2 = fmaf(tri[i * L + k + 2], inv[(k + 2) * L + j], s2);
+            s3 = fmaf(tri[i * L + k + 3], inv[(k + 3) * L + j], s3);
+          }
+          for (; k < i; ++k) s0 = fmaf(tri[i * L + k], inv[k * L + j], s0);
+          inv[i * L + j] = -((s0 + s1) + (s2 + s3)) * rinv[i];
+        }
+      } else {
+        for (int i = j - 1; i >= 0; --i) {
+          float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+          int k = i + 1;
+          for (; k + 3 <= j; k += 4) {
+            s0 = fmaf(tri[i * L + k], inv[k * L + j], s0);
+            s1 = fmaf(tri[i * L + k + 1], inv[(k + 1) * L + j], s1);
+            s2 = fmaf(tri[i * L + k + 2], inv[(k + 2) * L + j], s2);
+            s3 = fmaf(tri[i * L + k + 3], inv[(k + 3) * L + j], s3);
+          }
+          for (; k <= j; ++k) s0 = fmaf(tri[i * L + k], inv[k * L + j], s0);
+          inv[i * L + j] = -((s0 + s1) + (s2 + s3)) * rinv[i];
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // row-major Inv_b, then M_b = Inv_b T_bp (zero where the block is ragged or absent)
+  float *wi = ws + (size_t)b * 2 * TC_B * TC_B;
+  float *wm = wi + TC_B * TC_B;
+  for (int e = threadIdx.x; e < TC_B * TC_B; e += TC_T) wi[e] = inv[(e / TC_B) * L + (e % TC_B)];
+  for (int e = threadIdx.x; e < TC_B * TC_B; e += TC_T) {
+    const int i = e / TC_B, k = e % TC_B;
+    float s0 = 0.0f, s1 = 0.0f;
+    for (int j = 0; j < TC_B; j += 2) {
+      s0 = fmaf(inv[i * L + j], cpl[j * L + k], s0);
+      s1 = fmaf(inv[i * L + j + 1], cpl[(j + 1) * L + k], s1);
+    }
+    wm[e] = s0 + s1;
+  }
+}
+
+// sum_k c[k] * v[k] over the 32 published words pub[0..31] (those with index
+// < lim), each v[k] the float in its low half; polls until every word
+// carries `epoch`.  Returns false (sum 0) when the bounded wait gave up or
+// another warp of the CTA already did.
+//
+// Every warp of a CTA reads the published words of every earlier block, so
+// the waiting is done cheaply first: lane 0 alone polls the first word until
+// it carries `epoch` (sleeping `ns` between polls), and only then does the
+// warp read all 32 words (retrying the few stragglers of the same block).
+// All warps polling all their words would flood L2 with requests while the
+// chain advances.  ns = 0 skips the first phase: the wait for the block
+// solved just before (the step on the critical path, taken by one or two CTAs
+// at a time) polls all words directly.
+__device__ __forceinline__ bool chain_dot32(const unsigned long long *pub, int lim, unsigned epoch, const float *c,
+                                            float *sum, volatile int *fail, unsigned ns) {
+  const volatile unsigned long long *src = pub;
+  unsigned tries = 0;
+  if (ns) {
+    // every lane reaches the shuffle; lane 0's words start at its block's
+    // first row, which every caller's block has
+    int ok = 1;
+    if ((threadIdx.x & 31) == 0 && lim > 0) {
+      while ((unsigned)(src[0] >> 32) != epoch) {
+        if (*fail) {
+          ok = 0;
+          break;
+        }
+        if (++tries > kFlagPollLimit) {
+          atomicOr(&g_trsv_status, kErrGridTimeout);
+          *fail = 1;
+          ok = 0;
+          break;
+        }
+        __nanosleep(ns);
+      }
+    }
+    if (!__shfl_sync(0xffffffffu, ok, 0)) {
+      *sum = 0.0f;
+      return false;
+    }
+    tries = 0;
+  }
+  for (;;) {
+    bool ok = true;
+    float t = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+      if (k < lim) {
+        const unsigned long long w = src[k];
+        t = fmaf(c[k], __uint_as_float((unsigned)(w & 0xffffffffull)), t);
+        ok = ok && (unsigned)(w >> 32) == epoch;
+      }
+    }
+    if (ok) {
+      *sum = t;
+      return true;
+    }
+    if (*fail) break;
+    if (++tries > kFlagPollLimit) {
+      atomicOr(&g_trsv_status, kErrGridTimeout);
+      *fail = 1;
+      break;
+    }
+    if (tries > 16) __nanosleep(32);
+  }
+  *sum = 0.0f;
+  return false;
+}
+
+__device__ __forceinline__ void chain_load32(const float *__restrict__ A, int lda, int n, int r0, int ri, int nr, int c0,
+                                             int kq, float *dst) {
+  const int nc = min(TC_B, n - c0);
+  const float *col = A + (r0 + ri) + (size_t)(c0 + kq * 32) * lda;
+#pragma unroll
+  for (int k = 0; k < 32; ++k) dst[k] = (ri < nr && kq * 32 + k < nc) ? __ldcs(col + (size_t)k * lda) : 0.0f;
+}
+
+__global__ void __launch_bounds__(TC_T, 1)
+    trsv_chain_kernel(int n, const float *__restrict__ A, int lda, int lower, const float *__restrict__ ws, float *x,
+                      unsigned long long *pub, unsigned epoch, int *ticket) {
+  extern __shared__ float sm[];
+  float *sinv = sm;                        // [128][TC_LD] Inv_b, quarter-padded rows
+  float *smc = sm + TC_B * TC_LD;          // [128][TC_LD] M_b
+  __shared__ float part[4][TC_B];
+  __shared__ float ys[4 * 33];             // quarter-padded
+  __shared__ int s_pos;
+  __shared__ volatile int s_fail;
+  const int nb = (n + TC_B - 1) / TC_B;
+  if (threadIdx.x == 0) {
+    s_pos = atomicAdd(ticket, 1);
+    s_fail = 0;
+  }
+  __syncthreads();
+  const int pos = s_pos;                   // position in solve order
+  const int b = lower ? pos : nb - 1 - pos;
+  const int r0 = b * TC_B, nr = min(TC_B, n - r0);
+  // stage Inv_b and M_b
+  {
+    const float4 *w4 = reinterpret_cast<const float4 *>(ws + (size_t)b * 2 * TC_B * TC_B);
+    for (int e = threadIdx.x; e < 2 * TC_B * TC_B / 4; e += TC_T) {
+      const int m = e / (TC_B * TC_B / 4);
+      const int f = (e % (TC_B * TC_B / 4)) * 4;
+      const int i = f / TC_B, k = f % TC_B;
+      const float4 v = __ldg(w4 + e);
+      float *d = (m ? smc : sinv) + i * TC_LD + (k >> 5) * 33 + (k & 31);
+      d[0] = v.x;
+      d[1] = v.y;
+      d[2] = v.z;
+      d[3] = v.w;
+    }
+  }
+  // stream phase: blocks at solve positions 0 .. pos-2, rows ri, columns kq*32..kq*32+31
+  const int ri = threadIdx.x & (TC_B - 1), kq = threadIdx.x >> 7;
+  const float rhs = (threadIdx.x < TC_B && ri < nr) ? x[r0 + ri] : 0.0f;   // own rows: written only by this CTA
+  float acc = 0.0f;
+  const int nstream = pos - 1;
+  if (nstream > 0) {
+    float pa[32], pb[32], t;
+    auto blk = [&](int q) { return lower ? q : nb - 1 - q; };
+    chain_load32(A, lda, n, r0, ri, nr, blk(0) * TC_B, kq, pa);
+    for (int q = 0; q < nstream; q += 2) {
+      if (q + 1 < nstream) chain_load32(A, lda, n, r0, ri, nr, blk(q + 1) * TC_B, kq, pb);
+      {
+        const int c0 = blk(q) * TC_B;
+        chain_dot32(pub + c0 + kq * 32, min(TC_B, n - c0) - kq * 32, epoch, pa, &t, &s_fail, 128);
+        acc += t;
+      }
+      if (q + 1 >= nstream) break;
+      if (q + 2 < nstream) chain_load32(A, lda, n, r0, ri, nr, blk(q + 2) * TC_B, kq, pa);
+      {
+        const int c0 = blk(q + 1) * TC_B;
+        chain_dot32(pub + c0 + kq * 32, min(TC_B, n - c0) - kq * 32, epoch, pb, &t, &s_fail, 128);
+        acc += t;
+      }
+    }
+  }
+  part[kq][ri] = acc;
+  __syncthreads();
+  if (threadIdx.x < TC_B)
+    ys[(ri >> 5) * 33 + (ri & 31)] = rhs - ((part[0][ri] + part[1][ri]) + (part[2][ri] + part[3][ri]));
+  __syncthreads();
+  // (after a wait that gave up the block is still published, with the status
+  // bit set, so that later blocks do not wait out their own limits)
+  // z = Inv_b y: four threads per row, 32 terms each
+  const int hi = threadIdx.x >> 2, hq = threadIdx.x & 3;
+  float z = 0.0f;
+  {
+    const float *irow = sinv + hi * TC_LD + hq * 33;
+    const float *yq = ys + hq * 33;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) z = fmaf(irow[k], yq[k], z);
+    z += __shfl_xor_sync(0xffffffffu, z, 1);
+    z += __shfl_xor_sync(0xffffffffu, z, 2);
+  }
+  // the hop: x_b = z - M_b x_p
+  if (pos > 0) {
+    const int c0 = (lower ? b - 1 : b + 1) * TC_B;
+    float mrow[32], t;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) mrow[k] = smc[hi * TC_LD + hq * 33 + k];
+    chain_dot32(pub + c0 + hq * 32, min(TC_B, n - c0) - hq * 32, epoch, mrow, &t, &s_fail, 0);
+    t += __shfl_xor_sync(0xffffffffu, t, 1);
+    t += __shfl_xor_sync(0xffffffffu, t, 2);
+    z -= t;
+  }
+  if (hq == 0 && hi < nr) {
+    x[r0 + hi] = z;
+    pub[r0 + hi] = ((unsigned long long)epoch << 32) | (unsigned long long)__float_as_uint(z);
+  }
+}
+
+// The published-word buffer shared by the tagged and chained TRSV: zeroed
+// whenever it is new, epochs counting from 1.
+static unsigned long long *trsv_pub_words(int n, unsigned *epoch, cudaStream_t st) {
   static unsigned long long *s_pub = nullptr;
   static size_t s_len = 0;
   static unsigned s_epoch = 0;
-  const int nb = (n + TV_B - 1) / TV_B;
-  int *tk = static_cast<int *>(ctx().buffer(kBufV0, sizeof(int) * (size_t)(nb + 32)));
   unsigned long long *pub =
       static_cast<unsigned long long *>(ctx().buffer(kBufV2, sizeof(unsigned long long) * (size_t)n));
   if (pub != s_pub || (size_t)n > s_len || s_epoch == 0xffffffffu) {
@@ -570,10 +845,37 @@ void dev_strsv_inv(int uplo, int ta, int diag, int n, const float *A, int lda, f
     s_len = (size_t)n > s_len ? (size_t)n : s_len;
     s_epoch = 0;
   }
-  ++s_epoch;
+  *epoch = ++s_epoch;
+  return pub;
+}
+
+size_t strsv_chain_ws_floats(int n) { return (size_t)((n + TC_B - 1) / TC_B) * 2 * TC_B * TC_B; }
+
+void dev_strsv_chain_prepare(int uplo, int diag, int n, const float *A, int lda, float *ws, cudaStream_t st) {
+  if (n <= 0) return;
+  static bool attr = false;
+  if (!attr) {
+    ATLG_CHECK(cudaFuncSetAttribute(trsv_chain_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kChainPrepSmem));
+    ATLG_CHECK(cudaFuncSetAttribute(trsv_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kChainSmem));
+    attr = true;
+  }
+  const int nb = (n + TC_B - 1) / TC_B;
+  trsv_chain_prep_kernel<<<nb, TC_T, kChainPrepSmem, st>>>(n, A, lda, uplo == kLower ? 1 : 0, diag == kUnit ? 1 : 0,
+                                                           ws);
+  note_launch();
+  ATLG_CHECK(cudaGetLastError());
+}
+
+void dev_strsv_chain(int uplo, int n, const float *A, int lda, const float *ws, float *x, cudaStream_t st) {
+  if (n <= 0) return;
+  const int nb = (n + TC_B - 1) / TC_B;
+  unsigned epoch = 0;
+  unsigned long long *pub = trsv_pub_words(n, &epoch, st);
+  int *tk = static_cast<int *>(ctx().buffer(kBufV0, sizeof(int) * (size_t)(nb + 32)));
   ATLG_CHECK(cudaMemsetAsync(tk, 0, sizeof(int), st));
-  trsv_tagged_kernel<<<nb, 256, 0, st>>>(n, A, lda, uplo == kLower ? 1 : 0, diag == kUnit ? 1 : 0, x, pub, s_epoch,
-                                         tk);
+  trsv_chain_kernel<<<nb, TC_T, kChainSmem, st>>>(n, A, lda, uplo == kLower ? 1 : 0, ws, x, pub, epoch, tk);
   note_launch();
   ATLG_CHECK(cudaGetLastError());
 }

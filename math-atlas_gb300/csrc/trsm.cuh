@@ -20,6 +20,14 @@ void dev_strsv(int uplo, int ta, int diag, int n, const float *A, int lda, float
 // while each block waits (for the mixed solver's FP32 refinement solves;
 // rounding differs from substitution)
 void dev_strsv_inv(int uplo, int ta, int diag, int n, const float *A, int lda, float *x, cudaStream_t st);
+// Chained FP32 TRSV for one triangle solved many times (op(A) = A, one
+// right-hand side): dev_strsv_chain_prepare forms the 128 x 128 diagonal-block
+// inverses and couplings into ws (strsv_chain_ws_floats(n) floats) once per
+// factorization; dev_strsv_chain solves with them (rounding differs from
+// substitution).
+size_t strsv_chain_ws_floats(int n);
+void dev_strsv_chain_prepare(int uplo, int diag, int n, const float *A, int lda, float *ws, cudaStream_t st);
+void dev_strsv_chain(int uplo, int n, const float *A, int lda, const float *ws, float *x, cudaStream_t st);
 unsigned trsv_status_read_and_clear();
 
 }  // namespace atlg

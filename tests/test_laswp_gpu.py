@@ -80,3 +80,28 @@ def test_laswp_pivots_that_look_up(gb, ora, inci):
     ref = A.copy(order="F")
     ora.laswp(N, ref, K1, K2, piv, inci)
     assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("kind", ["one target", "few targets", "clustered"])
+@pytest.mark.parametrize("inci", [1, -1])
+def test_laswp_table_buckets_and_crowded_targets(gb, ora, kind, inci):
+    """Pivots that look down with many sources per target: the table's
+    counting sort sorts each target's sources in one thread up to 64 of them
+    and falls back to the warp scan beyond; both give the reference's
+    permutation."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(len(kind) + inci)
+    m, N, K1, K2 = 4096, 6, 0, 4000
+    piv = np.arange(m, dtype=np.int32)
+    if kind == "one target":          # every interchange with the last row
+        piv[K1:K2] = m - 1
+    elif kind == "few targets":       # about 50 sources per target, around the bucket limit
+        tg = np.sort(rng.choice(np.arange(K2, m), size=80, replace=False))
+        piv[K1:K2] = [tg[rng.integers(0, 80)] for _ in range(K1, K2)]
+    else:                             # targets just below each source
+        piv[K1:K2] = [min(m - 1, i + int(rng.integers(0, 4))) for i in range(K1, K2)]
+    A = ora.gegen(m, N, 5 * m + N)
+    got = _run(torch, gb, A, N, K1, K2, piv, inci, m)
+    ref = A.copy(order="F")
+    ora.laswp(N, ref, K1, K2, piv, inci)
+    assert np.array_equal(got, ref), kind

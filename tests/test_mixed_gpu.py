@@ -84,3 +84,61 @@ def test_tf32x3_update_is_fp32_accurate(gb):
         err = (C.double().T - ref).abs().max().item() / ref.abs().max().item()
         assert err < 1e-5, (M, N, K, err)
         assert gb.lib().atlg_status() == 0
+
+
+@pytest.mark.parametrize("n", [1, 127, 129, 1000, 2049])
+def test_dgesv_mixed_ragged_sizes(gb, ora, n):
+    """Sizes that leave a partial 128-row block in the chained refinement
+    solves (and the degenerate n = 1)."""
+    A, b = make_system(n, 1e4, 300 + n)
+    A0 = A.copy(order="F")
+    X = np.zeros((n, 1), order="F")
+    info, berr, ferr, iters, status = gb.dgesv_mixed(A, np.zeros(n, dtype=np.int32), b.copy(order="F"), X)
+    assert info == 0 and status == 0, (status, iters)
+    assert ora.backward_error(A0, X[:, 0], b[:, 0]) <= max(n, 16) * np.finfo(float).eps
+
+
+def test_dgesv_mixed_n16384_kappa1e6(gb):
+    """The mixed-precision configuration at its own size: n = 16384,
+    kappa = 1e6, A = U diag(s) V^T (U, V from Householder QR of seeded
+    Gaussian matrices on the GPU), b Gaussian.  The backward error is computed
+    here from b - A x in FP64 on the untouched matrix (not the solver's
+    estimate) and must be <= n eps; the forward error is compared with the
+    plain FP64 LU solve of the same system."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    n, kappa = 16384, 1e6
+    L = gb.lib()
+    g = torch.Generator(device="cuda").manual_seed(16384)
+    U, _ = torch.linalg.qr(torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g))
+    V, _ = torch.linalg.qr(torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g))
+    s = torch.logspace(0, -np.log10(kappa), n, device="cuda", dtype=torch.float64)
+    Acm = ((U * s) @ V.T).t().contiguous()      # column-major storage of A
+    del U, V
+    Am = Acm.T                                   # the matrix
+    b = torch.randn(n, device="cuda", dtype=torch.float64, generator=g)
+    A = Acm.clone()
+    X = torch.zeros(n, device="cuda", dtype=torch.float64)
+    piv = torch.zeros(n, dtype=torch.int32, device="cuda")
+    berr, ferr, it, stt = C.c_double(), C.c_double(), C.c_int(), C.c_int()
+    torch.cuda.synchronize()
+    info = L.atlg_dgesv_mixed_dev(n, 1, A.data_ptr(), n, piv.data_ptr(), b.data_ptr(), n, X.data_ptr(), n,
+                                  C.byref(berr), C.byref(ferr), C.byref(it), C.byref(stt), None)
+    torch.cuda.synchronize()
+    assert info == 0 and stt.value == 0, (info, stt.value, it.value)
+    assert 1 <= it.value <= 30
+    assert torch.equal(A, Acm)                   # refinement converged: A untouched
+    r = b - Am @ X
+    be = float(r.abs().max() / (Am.abs().sum(dim=1).max() * X.abs().max() + b.abs().max()))
+    assert be <= n * np.finfo(float).eps, be
+    # plain FP64 LU solve of the same system
+    inf = torch.zeros(4, dtype=torch.int32, device="cuda")
+    A.copy_(Acm)
+    xp = b.clone()
+    torch.cuda.synchronize()
+    L.atlg_dgetrf_dev(n, n, A.data_ptr(), n, piv.data_ptr(), inf.data_ptr(), None)
+    L.atlg_dgetrs_dev(102, 111, n, 1, A.data_ptr(), n, piv.data_ptr(), xp.data_ptr(), n, None)
+    torch.cuda.synchronize()
+    fe = float((X - xp).abs().max() / xp.abs().max())
+    assert fe <= 1e3 * kappa * np.finfo(float).eps, fe
+    assert L.atlg_status() == 0
