@@ -304,12 +304,19 @@ def measure_forms(G, O, torch, n=16384, kappas=(1e2, 1e6, 1e10), nslices=8, reps
 
         mts = event_ms(torch, s, prep_mixed, run_mixed, reps)
         mms = statistics.median(mts)
+        lookback = None
+        if kappa == 1e6:      # the same solve with the 64-row look-back refinement TRSV, for comparison
+            L.atlg_refine_trsv(0)
+            lookback = statistics.median(event_ms(torch, s, prep_mixed, run_mixed, reps))
+            L.atlg_refine_trsv(1)
         rows.append({"kappa": kappa, "ms": mms, "ms_all": mts, "tflops": dgesv_flops(n) / mms / 1e9,
                      "info": infos[-1], "iters": it.value, "fallback_fp64": stt.value == 1,
                      "backward_error": backward_error_dev(Am, X, b), "backward_error_solver_estimate": berr.value,
                      "forward_error_vs_plain_fp64": float((X - x_plain).abs().max() / x_plain.abs().max()),
                      "plain_fp64_backward_error": plain_berr, "n_eps": n * feps,
                      "speedup_vs_plain_fp64": plain["ms"] / mms})
+        if lookback is not None:
+            rows[-1]["ms_with_lookback_trsv"] = lookback
 
         # split-DGEMM form: FP64 LU with tensor-core (integer-slice) updates
         xs = torch.empty_like(b)
@@ -739,8 +746,10 @@ def measure_memory(G, O, torch, reps=5):
     L = G.lib()
     st = L.atlg_stream()
     s = torch.cuda.ExternalStream(st)
-    peak = load_peaks().get("hbm_gbs") or 6800.0
-    out = {}
+    pk = load_peaks()
+    peak = pk.get("hbm_gbs") or 6800.0
+    out = {"hbm_peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if pk.get("hbm_gbs")
+           else "fallback 6800 GB/s (MEASURED_PEAKS.json absent)"}
 
     def timed(fn):
         ts = []
@@ -783,6 +792,36 @@ def measure_memory(G, O, torch, reps=5):
                                "sample": f"oracle laswp {mc} x {Nc}, full pivot vector (32-column blocks)"}
         out[name] = row
         del A
+    torch.cuda.empty_cache()
+    # chained FP32 TRSV on the factors of an FP32 LU at n = 16384 (the mixed
+    # solver's refinement solve): n^2/2 FP32 elements of the triangle read once
+    n = 16384
+    g = torch.Generator(device="cuda").manual_seed(41)
+    S = torch.randn(n, n, device="cuda", dtype=torch.float32, generator=g)
+    piv = torch.zeros(n, dtype=torch.int32, device="cuda")
+    inf = torch.zeros(4, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    L.atlg_sgetrf_dev(n, n, S.data_ptr(), n, piv.data_ptr(), inf.data_ptr(), st)
+    ws = torch.empty(L.atlg_strsv_chain_ws(n) // 4, dtype=torch.float32, device="cuda")
+    xv = torch.randn(n, device="cuda", dtype=torch.float32, generator=g)
+    x0 = xv.clone()
+    torch.cuda.synchronize()
+    for (uplo, diag, name) in ((122, 132, "strsv_chain_lower_unit_n16384"), (121, 131, "strsv_chain_upper_n16384")):
+        prep = timed(lambda: L.atlg_strsv_chain_prepare_dev(uplo, diag, n, S.data_ptr(), n, ws.data_ptr(), st))
+
+        def solve():
+            xv.copy_(x0)
+            torch.cuda.synchronize()
+        ts = event_ms(torch, s, solve, lambda: L.atlg_strsv_chain_dev(uplo, n, S.data_ptr(), n, ws.data_ptr(),
+                                                                     xv.data_ptr(), st), 10)
+        ms = statistics.median(ts)
+        alg = 4.0 * n * (n + 1) / 2
+        out[name] = {"n": n, "prepare_ms": prep, "ms": ms, "ms_all": ts, "algorithmic_bytes": alg,
+                     "gbs": alg / (ms * 1e-3) / 1e9, "peak_gbs": peak, "frac": alg / (ms * 1e-3) / 1e9 / peak,
+                     "finite": bool(torch.isfinite(xv).all()),
+                     "timing": "CUDA events on the library stream around one atlg_strsv_chain_dev, median of 10 "
+                               "after one warm-up (the FP32 factors, 1 GiB, exceed L2); prepare: best of %d" % reps}
+    del S, ws
     torch.cuda.empty_cache()
     # iamax over 2^27 doubles (1 GiB) and one pivot-column-sized call
     res = torch.zeros(1, dtype=torch.int32, device="cuda")

@@ -298,6 +298,19 @@ int atlg_dgemv_dev(int TA, int M, int N, double alpha, const double *A, int lda,
                    const double *X, int incX, double beta, double *Y, void *stream);
 int atlg_dtrsv_dev(int Uplo, int TA, int Diag, int N, const double *A, int lda, double *X,
                    void *stream);
+/* FP32 triangular solve A x = x (no transpose, incX = 1) for a triangle solved
+ * many times, as in iterative refinement (no reference counterpart; the
+ * single-solve form is cblas_strsv, AtlasBase/Clint/cblas-lvl2.base:273).
+ * _prepare forms the 128 x 128 diagonal-block inverses and the couplings to
+ * the block solved before each into ws (atlg_strsv_chain_ws(N) bytes,
+ * 16-byte aligned); _dev then solves with one launch.  ws must be prepared
+ * again after A changes.  Rounding differs from substitution.  Returns 0, -1
+ * on a bad argument. */
+size_t atlg_strsv_chain_ws(int N);
+int atlg_strsv_chain_prepare_dev(int Uplo, int Diag, int N, const float *A, int lda, float *ws,
+                                 void *stream);
+int atlg_strsv_chain_dev(int Uplo, int N, const float *A, int lda, const float *ws, float *X,
+                         void *stream);
 /* trtri returns its info (synchronizes once); getri reads the 0-based
  * device pivots back to the host first */
 int atlg_dtrtri_dev(int Order, int Uplo, int Diag, int N, double *A, int lda, void *stream);

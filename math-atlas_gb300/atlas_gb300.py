@@ -32,7 +32,8 @@ EXPORTS = [
     "cblas_dsyrk", "cblas_ssyrk", "clapack_dpotrf", "clapack_spotrf", "clapack_dpotrs", "clapack_spotrs",
     "clapack_dposv", "clapack_sposv", "atlg_dsyrk_dev", "atlg_dpotrf_dev", "atlg_dpotrs_dev",
     "cblas_dtrmm", "cblas_strmm", "cblas_dgemv", "cblas_sgemv", "cblas_dtrsv", "cblas_strsv",
-    "atlg_dtrmm_dev", "atlg_dgemv_dev", "atlg_dtrsv_dev",
+    "atlg_dtrmm_dev", "atlg_dgemv_dev", "atlg_dtrsv_dev", "atlg_strsv_chain_ws", "atlg_strsv_chain_prepare_dev",
+    "atlg_strsv_chain_dev",
     "clapack_dtrtri", "clapack_strtri", "clapack_dgetri", "clapack_sgetri", "atlg_dtrtri_dev", "atlg_dgetri_dev",
     "atlg_panel_cluster", "atlg_refine_trsv", "dgesv_split", "atlg_dgetrf_split_dev", "atlg_panel_grid", "atlg_split_lu_leaf", "atlg_panel_width",
     "cblas_idamax", "cblas_isamax", "atlg_idamax_dev", "atlg_isamax_dev",
@@ -95,6 +96,9 @@ def _declare(L):
         "atlg_dtrmm_dev": (_i, [_i, _i, _i, _i, _i, _i, _d, _v, _i, _v, _i, _v]),
         "atlg_dgemv_dev": (_i, [_i, _i, _i, _d, _v, _i, _v, _i, _d, _v, _v]),
         "atlg_dtrsv_dev": (_i, [_i, _i, _i, _i, _v, _i, _v, _v]),
+        "atlg_strsv_chain_ws": (C.c_size_t, [_i]),
+        "atlg_strsv_chain_prepare_dev": (_i, [_i, _i, _i, _v, _i, _v, _v]),
+        "atlg_strsv_chain_dev": (_i, [_i, _i, _v, _i, _v, _v, _v]),
         "clapack_dtrtri": (_i, [_i, _i, _i, _i, _dp, _i]),
         "clapack_strtri": (_i, [_i, _i, _i, _i, _sp, _i]),
         "clapack_dgetri": (_i, [_i, _i, _dp, _i, _ip]),

@@ -1211,6 +1211,20 @@ int atlg_dtrsv_dev(int Uplo, int TA, int Diag, int N, const double *A, int lda, 
   dev_dtrsv(Uplo, TA, Diag, N, A, lda, X, stream_of(stream));
   return 0;
 }
+size_t atlg_strsv_chain_ws(int N) { return N > 0 ? sizeof(float) * strsv_chain_ws_floats(N) : 0; }
+int atlg_strsv_chain_prepare_dev(int Uplo, int Diag, int N, const float *A, int lda, float *ws, void *stream) {
+  if (N < 0 || lda < (N > 1 ? N : 1) || (Uplo != kUpper && Uplo != kLower) || (Diag != kUnit && Diag != kNonUnit))
+    return -1;
+  if (N > 0 && (reinterpret_cast<uintptr_t>(ws) & 15) != 0) return -1;
+  dev_strsv_chain_prepare(Uplo, Diag, N, A, lda, ws, stream_of(stream));
+  return 0;
+}
+int atlg_strsv_chain_dev(int Uplo, int N, const float *A, int lda, const float *ws, float *X, void *stream) {
+  if (N < 0 || lda < (N > 1 ? N : 1) || (Uplo != kUpper && Uplo != kLower)) return -1;
+  if (N > 0 && (reinterpret_cast<uintptr_t>(ws) & 15) != 0) return -1;
+  dev_strsv_chain(Uplo, N, A, lda, ws, X, stream_of(stream));
+  return 0;
+}
 int atlg_dtrtri_dev(int Order, int Uplo, int Diag, int N, double *A, int lda, void *stream) {
   if (N < 0 || lda < (N > 1 ? N : 1)) return -1;
   return dev_dtrtri(Order, Uplo, Diag, N, A, lda, stream_of(stream));

@@ -119,6 +119,20 @@ static std::vector<double> colmax_host(int M, int N, const double *V, int ldv, d
 static bool g_refine_chained = true;
 void set_refine_trsv_chained(bool on) { g_refine_chained = on; }
 
+// column maxima of two M x N blocks with one host synchronisation:
+// v[j] = max_i |V(i,j)|, w[j] = max_i |W(i,j)| (dtmp holds 2N doubles)
+static void colmax2_host(int M, int N, const double *V, int ldv, const double *W, int ldw, double *dtmp,
+                         std::vector<double> &v, std::vector<double> &w, cudaStream_t st) {
+  colmax_kernel<double><<<N, 256, 0, st>>>(M, V, ldv, dtmp);
+  colmax_kernel<double><<<N, 256, 0, st>>>(M, W, ldw, dtmp + N);
+  note_launch(2);
+  std::vector<double> h(2 * (size_t)N);
+  ATLG_CHECK(cudaMemcpyAsync(h.data(), dtmp, sizeof(double) * 2 * N, cudaMemcpyDeviceToHost, st));
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  v.assign(h.begin(), h.begin() + N);
+  w.assign(h.begin() + N, h.end());
+}
+
 int dev_dgesv_mixed(int n, int nrhs, double *A, int lda, int *ipiv, const double *B, int ldb, double *X, int ldx,
                     MixedResult *res, cudaStream_t st) {
   Context &c = ctx();
@@ -196,8 +210,8 @@ int dev_dgesv_mixed(int n, int nrhs, double *A, int lda, int *ipiv, const double
       copy_d_kernel<<<grid_for((long)n * nrhs), 256, 0, st>>>(n, nrhs, B, ldb, R, ldr);
       note_launch();
       dev_dgemm(kNoTrans, kNoTrans, n, nrhs, n, -1.0, A, lda, X, ldx, 1.0, R, ldr, st);
-      std::vector<double> rn = colmax_host(n, nrhs, R, ldr, dtmp, st);
-      std::vector<double> xn = colmax_host(n, nrhs, X, ldx, dtmp, st);
+      std::vector<double> rn, xn;
+      colmax2_host(n, nrhs, R, ldr, X, ldx, dtmp, rn, xn, st);   // (dtmp spans the row sums, used only above)
       conv = true;
       double rmax = 0.0;
       for (int j = 0; j < nrhs; ++j) {
@@ -219,14 +233,15 @@ int dev_dgesv_mixed(int n, int nrhs, double *A, int lda, int *ipiv, const double
       solve32(R32);
       axpy_s2d_kernel<<<grid_for((long)n * nrhs), 256, 0, st>>>(n, nrhs, R32, lds, X, ldx);
       note_launch();
-      {
-        // forward-error estimate ||d||/||x|| from the FP32 correction
-        s2d_kernel<<<grid_for((long)n * nrhs), 256, 0, st>>>(n, nrhs, R32, lds, R, ldr);
-        note_launch();
-        std::vector<double> d2 = colmax_host(n, nrhs, R, ldr, dtmp, st);
-        std::vector<double> x2 = colmax_host(n, nrhs, X, ldx, dtmp, st);
-        for (int j = 0; j < nrhs; ++j) res->ferr[j] = x2[j] > 0 ? d2[j] / x2[j] : 0.0;
-      }
+    }
+    if (iter > 0) {
+      // forward-error estimate ||d||/||x|| from the last FP32 correction (R32
+      // still holds it: the loop ends on a residual, before another solve)
+      s2d_kernel<<<grid_for((long)n * nrhs), 256, 0, st>>>(n, nrhs, R32, lds, R, ldr);
+      note_launch();
+      std::vector<double> d2, x2;
+      colmax2_host(n, nrhs, R, ldr, X, ldx, dtmp, d2, x2, st);
+      for (int j = 0; j < nrhs; ++j) res->ferr[j] = x2[j] > 0 ? d2[j] / x2[j] : 0.0;
     }
     res->iters = iter;
     fallback = !conv;

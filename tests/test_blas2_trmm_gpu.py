@@ -175,3 +175,45 @@ def test_strsv(gb, ora):
     xt = x0.copy()
     ora.trsv(122, 111, 131, n, A, xt, 1)
     assert np.allclose(xg, xt, rtol=1e-4, atol=1e-5)
+
+
+@pytest.mark.parametrize("n", [1, 100, 128, 129, 1000, 2500])
+@pytest.mark.parametrize("uplo,diag", [(122, 132), (121, 131)])
+def test_strsv_chain_on_lu_factors(gb, n, uplo, diag):
+    """The chained FP32 TRSV (block inverses prepared once, then solves)
+    on the factors of a partial-pivoting LU: against an FP64 triangular solve
+    of the same FP32 factors, to FP32 accuracy; two solves with one
+    preparation give identical results."""
+    torch = pytest.importorskip("torch")
+    L = gb.lib()
+    g = torch.Generator(device="cuda").manual_seed(n + uplo)
+    A = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g)
+    LU, _ = torch.linalg.lu_factor(A)
+    T = LU.float()                                       # row-major n x n holding the factors
+    Tcm = T.t().contiguous()                             # column-major storage
+    ws = torch.empty(max(1, L.atlg_strsv_chain_ws(n) // 4), dtype=torch.float32, device="cuda")
+    b = torch.randn(n, device="cuda", dtype=torch.float32, generator=g)
+    x1, x2 = b.clone(), b.clone()
+    torch.cuda.synchronize()
+    assert L.atlg_strsv_chain_prepare_dev(uplo, diag, n, Tcm.data_ptr(), n, ws.data_ptr(), None) == 0
+    assert L.atlg_strsv_chain_dev(uplo, n, Tcm.data_ptr(), n, ws.data_ptr(), x1.data_ptr(), None) == 0
+    assert L.atlg_strsv_chain_dev(uplo, n, Tcm.data_ptr(), n, ws.data_ptr(), x2.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    assert L.atlg_status() == 0
+    assert torch.equal(x1, x2)
+    Td = T.double()
+    if uplo == 122:
+        Tt = torch.tril(Td, -1) + torch.eye(n, dtype=torch.float64, device="cuda")
+    else:
+        Tt = torch.triu(Td)
+    ref = torch.linalg.solve_triangular(Tt, b.double().unsqueeze(1), upper=(uplo == 121),
+                                        unitriangular=(diag == 132)).squeeze(1)
+    err = float((x1.double() - ref).abs().max() / ref.abs().max())
+    assert err < 2e-2, err       # FP32 forward error of a Gaussian matrix's factors (bugs give O(1))
+
+
+def test_strsv_chain_rejects_bad_arguments(gb):
+    L = gb.lib()
+    assert L.atlg_strsv_chain_prepare_dev(122, 132, -1, None, 1, None, None) == -1
+    assert L.atlg_strsv_chain_prepare_dev(123, 132, 10, None, 10, None, None) == -1
+    assert L.atlg_strsv_chain_dev(122, 10, None, 5, None, None, None) == -1
