@@ -660,28 +660,23 @@ __global__ void __launch_bounds__(TC_T)
   }
 }
 
-// sum_k c[k] * v[k] over the 32 published words pub[0..31] (those with index
-// < lim), each v[k] the float in its low half; polls until every word
-// carries `epoch`.  Returns false (sum 0) when the bounded wait gave up or
-// another warp of the CTA already did.
-//
-// Every warp of a CTA reads the published words of every earlier block, so
-// the waiting is done cheaply first: lane 0 alone polls the first word until
-// it carries `epoch` (sleeping `ns` between polls), and only then does the
-// warp read all 32 words (retrying the few stragglers of the same block).
-// All warps polling all their words would flood L2 with requests while the
-// chain advances.  ns = 0 skips the first phase: the wait for the block
-// solved just before (the step on the critical path, taken by one or two CTAs
-// at a time) polls all words directly.
-__device__ __forceinline__ bool chain_dot32(const unsigned long long *pub, int lim, unsigned epoch, const float *c,
-                                            float *sum, volatile int *fail, unsigned ns) {
+// Waits until the 32 published words pub[0..31] (those with index < lim)
+// carry `epoch` and returns in *v the float of word `lane` (0 past lim): the
+// warp reads the 32 words with one coalesced load per lane per poll, and the
+// callers broadcast them by shuffles (32 separate loads per lane of one word
+// each, as in a per-thread loop, serialise on the volatile accesses).  With
+// ns > 0, lane 0 first waits on word 0 alone, sleeping ns between polls, so
+// that the many warps waiting on a block not yet solved poll cheaply.
+// Returns false when the bounded wait gave up or another warp of the CTA
+// already did (then *v = 0).
+__device__ __forceinline__ bool chain_wait32(const unsigned long long *pub, int lim, unsigned epoch, float *v,
+                                             volatile int *fail, unsigned ns) {
   const volatile unsigned long long *src = pub;
+  const int lane = threadIdx.x & 31;
   unsigned tries = 0;
+  int ok = 1;
   if (ns) {
-    // every lane reaches the shuffle; lane 0's words start at its block's
-    // first row, which every caller's block has
-    int ok = 1;
-    if ((threadIdx.x & 31) == 0 && lim > 0) {
+    if (lane == 0 && lim > 0) {
       while ((unsigned)(src[0] >> 32) != epoch) {
         if (*fail) {
           ok = 0;
@@ -696,37 +691,32 @@ __device__ __forceinline__ bool chain_dot32(const unsigned long long *pub, int l
         __nanosleep(ns);
       }
     }
-    if (!__shfl_sync(0xffffffffu, ok, 0)) {
-      *sum = 0.0f;
-      return false;
-    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
     tries = 0;
   }
-  for (;;) {
-    bool ok = true;
-    float t = 0.0f;
-#pragma unroll
-    for (int k = 0; k < 32; ++k) {
-      if (k < lim) {
-        const unsigned long long w = src[k];
-        t = fmaf(c[k], __uint_as_float((unsigned)(w & 0xffffffffull)), t);
-        ok = ok && (unsigned)(w >> 32) == epoch;
-      }
+  float val = 0.0f;
+  while (ok) {
+    bool mine = true;
+    if (lane < lim) {
+      const unsigned long long w = src[lane];
+      val = __uint_as_float((unsigned)(w & 0xffffffffull));
+      mine = (unsigned)(w >> 32) == epoch;
     }
-    if (ok) {
-      *sum = t;
-      return true;
-    }
-    if (*fail) break;
-    if (++tries > kFlagPollLimit) {
-      atomicOr(&g_trsv_status, kErrGridTimeout);
-      *fail = 1;
+    if (__all_sync(0xffffffffu, mine)) break;
+    if (*fail) {
+      ok = 0;
       break;
     }
-    if (tries > 16) __nanosleep(32);
+    if (++tries > kFlagPollLimit) {
+      if (lane == 0) atomicOr(&g_trsv_status, kErrGridTimeout);
+      *fail = 1;
+      ok = 0;
+      break;
+    }
+    if (tries > 8) __nanosleep(32);
   }
-  *sum = 0.0f;
-  return false;
+  *v = ok ? val : 0.0f;
+  return ok != 0;
 }
 
 __device__ __forceinline__ void chain_load32(const float *__restrict__ A, int lda, int n, int r0, int ri, int nr, int c0,
@@ -745,6 +735,7 @@ __global__ void __launch_bounds__(TC_T, 1)
   float *smc = sm + TC_B * TC_LD;          // [128][TC_LD] M_b
   __shared__ float part[4][TC_B];
   __shared__ float ys[4 * 33];             // quarter-padded
+  __shared__ float xs[4 * 33];             // x of the block solved just before, quarter-padded
   __shared__ int s_pos;
   __shared__ volatile int s_fail;
   const int nb = (n + TC_B - 1) / TC_B;
@@ -777,22 +768,29 @@ __global__ void __launch_bounds__(TC_T, 1)
   float acc = 0.0f;
   const int nstream = pos - 1;
   if (nstream > 0) {
-    float pa[32], pb[32], t;
+    // (a warp's lanes share kq: the 32 words of its quarter, one per lane)
+    float pa[32], pb[32], xl;
     auto blk = [&](int q) { return lower ? q : nb - 1 - q; };
+    auto fold = [&](const float *c) {
+      float t = 0.0f;
+#pragma unroll
+      for (int k = 0; k < 32; ++k) t = fmaf(c[k], __shfl_sync(0xffffffffu, xl, k), t);
+      acc += t;
+    };
     chain_load32(A, lda, n, r0, ri, nr, blk(0) * TC_B, kq, pa);
     for (int q = 0; q < nstream; q += 2) {
       if (q + 1 < nstream) chain_load32(A, lda, n, r0, ri, nr, blk(q + 1) * TC_B, kq, pb);
       {
         const int c0 = blk(q) * TC_B;
-        chain_dot32(pub + c0 + kq * 32, min(TC_B, n - c0) - kq * 32, epoch, pa, &t, &s_fail, 128);
-        acc += t;
+        chain_wait32(pub + c0 + kq * 32, min(TC_B, n - c0) - kq * 32, epoch, &xl, &s_fail, 128);
+        fold(pa);
       }
       if (q + 1 >= nstream) break;
       if (q + 2 < nstream) chain_load32(A, lda, n, r0, ri, nr, blk(q + 2) * TC_B, kq, pa);
       {
         const int c0 = blk(q + 1) * TC_B;
-        chain_dot32(pub + c0 + kq * 32, min(TC_B, n - c0) - kq * 32, epoch, pb, &t, &s_fail, 128);
-        acc += t;
+        chain_wait32(pub + c0 + kq * 32, min(TC_B, n - c0) - kq * 32, epoch, &xl, &s_fail, 128);
+        fold(pb);
       }
     }
   }
@@ -814,13 +812,22 @@ __global__ void __launch_bounds__(TC_T, 1)
     z += __shfl_xor_sync(0xffffffffu, z, 1);
     z += __shfl_xor_sync(0xffffffffu, z, 2);
   }
-  // the hop: x_b = z - M_b x_p
+  // the hop: x_b = z - M_b x_p; warps 0-3 wait for x_p, a quarter each, and
+  // stage it in shared memory
   if (pos > 0) {
     const int c0 = (lower ? b - 1 : b + 1) * TC_B;
-    float mrow[32], t;
+    float mrow[32], t = 0.0f;
 #pragma unroll
     for (int k = 0; k < 32; ++k) mrow[k] = smc[hi * TC_LD + hq * 33 + k];
-    chain_dot32(pub + c0 + hq * 32, min(TC_B, n - c0) - hq * 32, epoch, mrow, &t, &s_fail, 0);
+    const int w = threadIdx.x >> 5;
+    if (w < 4) {
+      float xl;
+      chain_wait32(pub + c0 + w * 32, min(TC_B, n - c0) - w * 32, epoch, &xl, &s_fail, 0);
+      xs[w * 33 + (threadIdx.x & 31)] = xl;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 32; ++k) t = fmaf(mrow[k], xs[hq * 33 + k], t);
     t += __shfl_xor_sync(0xffffffffu, t, 1);
     t += __shfl_xor_sync(0xffffffffu, t, 2);
     z -= t;
