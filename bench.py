@@ -1195,17 +1195,26 @@ def run_case(args):
         X = torch.zeros(n, device="cuda", dtype=torch.float64)
         piv = torch.zeros(n, dtype=torch.int32, device="cuda")
         berr, ferr, it, stt = C.c_double(), C.c_double(), C.c_int(), C.c_int()
-        for _ in range(2):
+        for rep in range(2):
             A.copy_(A0)
             torch.cuda.synchronize()
+            if rep == 1 and args.panels:
+                L.atlg_prof_panels(1)
             t0 = time.perf_counter()
             L.atlg_dgesv_mixed_dev(n, 1, A.data_ptr(), n, piv.data_ptr(), b.data_ptr(), n, X.data_ptr(), n,
                                    C.byref(berr), C.byref(ferr), C.byref(it), C.byref(stt), st)
             torch.cuda.synchronize()
             ms = (time.perf_counter() - t0) * 1e3
+        if args.panels:
+            L.atlg_prof_panels(0)
+            pm, gm, pc = C.c_double(), C.c_double(), C.c_int()
+            L.atlg_prof_panels_collect(C.byref(pm), C.byref(gm), C.byref(pc))
+            panels = {"panel_ms": pm.value, "gap_ms": gm.value, "panels": pc.value}
     extra = {}
     if args.case == "mixed":
         extra = {"iters": it.value, "fallback": stt.value == 1, "kappa": args.kappa, "trsv": args.trsv}
+        if args.panels:
+            extra.update(panels)
     print(json.dumps(dict({"case": args.case, "n": n, "ms": ms, "status": int(L.atlg_status())}, **extra)), flush=True)
     return 0
 
@@ -1222,6 +1231,8 @@ def main():
     ap.add_argument("--leaf", type=int, default=0, help="FP64 leaf width of --case splitlu (0: default)")
     ap.add_argument("--pw", type=int, default=0, help="FP64 LU panel width for --case splitlu/dgetrf (0: default)")
     ap.add_argument("--grid", type=int, default=0, help="grid-panel CTAs for --case splitlu/dgetrf (0: default)")
+    ap.add_argument("--panels", action="store_true",
+                    help="--case mixed: CUDA events around every LU panel of the second solve (panel and gap sums)")
     ap.add_argument("--trsv", type=int, default=-1,
                     help="--case mixed: refinement TRSV, 1 chained (128-row blocks), 0 look-back (64-row); -1 default")
     ap.add_argument("--kappa", type=float, default=0.0,

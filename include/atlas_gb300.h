@@ -215,6 +215,12 @@ void atlg_probe_peaks(double *fp64_tflops, double *fp32_tflops);
  * in TFLOP/s of mma.sync with f64 operands, shapes m8n8k4, m16n8k4 and
  * m16n8k16 (any pointer may be NULL) */
 void atlg_probe_fp64_mma(double *m8n8k4, double *m16n8k4, double *m16n8k16);
+/* benchmark support (no reference counterpart): CUDA events around every LU
+ * panel launch; collect returns the summed panel time, the summed gaps
+ * between consecutive panels on the factorization's stream, and the count
+ * (synchronizes) */
+void atlg_prof_panels(int on);
+int atlg_prof_panels_collect(double *panel_ms, double *gap_ms, int *count);
 int atlg_dgemm_dev(int TA, int TB, int M, int N, int K, double alpha, const double *A, int lda,
                    const double *B, int ldb, double beta, double *C, int ldc, void *stream);
 int atlg_dgemm_dev_opts(int TA, int TB, int M, int N, int K, double alpha, const double *A,

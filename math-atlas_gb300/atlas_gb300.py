@@ -27,7 +27,7 @@ EXPORTS = [
     "clapack_sgesv", "atlg_num_sms", "atlg_stream", "atlg_status", "atlg_dgemm_dev",
     "atlg_dgemm_dev_opts", "atlg_sgemm_dev", "atlg_dtrsm_dev", "atlg_dlaswp_dev", "atlg_dgetrf_dev",
     "atlg_sgetrf_dev", "atlg_dgetrs_dev", "atlg_launch_count", "atlg_prof_enable", "atlg_prof_collect",
-    "atlg_probe_peaks", "atlg_probe_fp64_mma", "dgesv_mixed", "dgesv_adjoint", "atlg_dgesv_mixed_dev", "atlg_dgesv_adjoint_dev",
+    "atlg_probe_peaks", "atlg_probe_fp64_mma", "atlg_prof_panels", "atlg_prof_panels_collect", "dgesv_mixed", "dgesv_adjoint", "atlg_dgesv_mixed_dev", "atlg_dgesv_adjoint_dev",
     "atlg_dlaswp_noalloc", "dgemm_split", "atlg_dgemm_split_dev", "atlg_sgemm_tf32x3_dev",
     "cblas_dsyrk", "cblas_ssyrk", "clapack_dpotrf", "clapack_spotrf", "clapack_dpotrs", "clapack_spotrs",
     "clapack_dposv", "clapack_sposv", "atlg_dsyrk_dev", "atlg_dpotrf_dev", "atlg_dpotrs_dev",
@@ -142,6 +142,8 @@ def _declare(L):
         "atlg_prof_collect": (_i, [C.POINTER(_d), C.POINTER(_d), C.POINTER(_i)]),
         "atlg_probe_peaks": (None, [C.POINTER(_d), C.POINTER(_d)]),
         "atlg_probe_fp64_mma": (None, [C.POINTER(_d), C.POINTER(_d), C.POINTER(_d)]),
+        "atlg_prof_panels": (None, [_i]),
+        "atlg_prof_panels_collect": (_i, [C.POINTER(_d), C.POINTER(_d), C.POINTER(_i)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

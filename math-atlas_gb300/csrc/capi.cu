@@ -1106,6 +1106,41 @@ int atlg_prof_collect(double *ms, double *flops, int *count) {
   return 0;
 }
 
+void atlg_prof_panels(int on) { ctx().prof_panels = on != 0; }
+
+// LU panel launches recorded since the last collect, in stream order: the
+// summed panel time (event before to event after each launch on the
+// factorization's stream) and the summed gaps between one panel's end and the
+// next panel's start (the step's remaining work on that stream, including
+// waits for the side stream).  Synchronizes.
+int atlg_prof_panels_collect(double *panel_ms, double *gap_ms, int *count) {
+  Context &c = ctx();
+  double p = 0.0, g = 0.0;
+  int n = 0;
+  for (size_t i = 0; i < c.panel_recs.size(); ++i) {
+    auto &r = c.panel_recs[i];
+    ATLG_CHECK(cudaEventSynchronize(r.end));
+    float x = 0.f;
+    ATLG_CHECK(cudaEventElapsedTime(&x, r.beg, r.end));
+    p += x;
+    if (i + 1 < c.panel_recs.size()) {
+      ATLG_CHECK(cudaEventSynchronize(c.panel_recs[i + 1].beg));
+      ATLG_CHECK(cudaEventElapsedTime(&x, r.end, c.panel_recs[i + 1].beg));
+      g += x;
+    }
+    ++n;
+  }
+  for (auto &r : c.panel_recs) {
+    c.pool.push_back(r.beg);
+    c.pool.push_back(r.end);
+  }
+  c.panel_recs.clear();
+  if (panel_ms) *panel_ms = p;
+  if (gap_ms) *gap_ms = g;
+  if (count) *count = n;
+  return 0;
+}
+
 void atlg_probe_fp64_mma(double *m8n8k4, double *m16n8k4, double *m16n8k16) {
   probe_fp64_mma_tflops(m8n8k4, m16n8k4, m16n8k16);
 }

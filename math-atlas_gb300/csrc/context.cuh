@@ -31,6 +31,8 @@ struct Context {
   unsigned long long launches = 0;
   bool prof = false;
   std::vector<ProfRec> recs;
+  bool prof_panels = false;          // LU panels: events before and after each panel launch
+  std::vector<ProfRec> panel_recs;
   std::vector<cudaEvent_t> pool;
   cudaEvent_t event();
   cudaStream_t side = nullptr;       // low-priority stream for overlapped updates

@@ -91,11 +91,49 @@ __device__ void ia_block_reduce(unsigned long long &key, long long &idx, long lo
   }
 }
 
+template <typename T> struct IaVec;
+template <> struct IaVec<double> { using type = double2; };
+template <> struct IaVec<float> { using type = float4; };
+
 // First maximum and last NaN over elements [b, e) of X (stride inc), this
-// CTA's threads, coalesced for inc = 1.
+// CTA's threads, coalesced for inc = 1.  Every thread visits its elements in
+// increasing index order, so `k > key` keeps a thread's first maximum and
+// `nan = i` its last NaN.  Unit stride from a 16-byte aligned start reads
+// 16-byte vectors (kIaUnroll of them in flight per thread), the rest one
+// element at a time.
 template <typename T>
 __device__ void ia_scan(const T *__restrict__ X, long long inc, long long b, long long e, unsigned long long &key,
                         long long &idx, long long &nan) {
+  auto visit = [&](T x, long long i) {
+    const unsigned long long k = IaKey<T>::key(x);
+    if (k > IaKey<T>::kInf) nan = i;
+    else if (k > key) { key = k; idx = i; }
+  };
+  if (inc == 1 && (reinterpret_cast<uintptr_t>(X + b) & 15) == 0) {
+    using V = typename IaVec<T>::type;
+    constexpr int VE = 16 / (int)sizeof(T);
+    const long long nv = (e - b) / VE;
+    const V *xv = reinterpret_cast<const V *>(X + b);
+    for (long long q0 = threadIdx.x; q0 < nv; q0 += (long long)kIaUnroll * kIaThreads) {
+      V v[kIaUnroll];
+#pragma unroll
+      for (int u = 0; u < kIaUnroll; ++u) {
+        const long long q = q0 + (long long)u * kIaThreads;
+        if (q < nv) v[u] = xv[q];
+      }
+#pragma unroll
+      for (int u = 0; u < kIaUnroll; ++u) {
+        const long long q = q0 + (long long)u * kIaThreads;
+        if (q < nv) {
+          const T *ve = reinterpret_cast<const T *>(&v[u]);
+#pragma unroll
+          for (int t = 0; t < VE; ++t) visit(ve[t], b + q * VE + t);
+        }
+      }
+    }
+    for (long long i = b + nv * VE + threadIdx.x; i < e; i += kIaThreads) visit(X[i], i);
+    return;
+  }
   for (long long i0 = b + threadIdx.x; i0 < e; i0 += (long long)kIaUnroll * kIaThreads) {
     T v[kIaUnroll];
 #pragma unroll
@@ -207,7 +245,9 @@ static void iamax_impl(int N, const T *X, int incX, int unit, int *result, cudaS
   const long long cap = 4LL * c.num_sms;   // one wave at 4 CTAs per SM
   if (grid > cap) grid = cap;
   if (grid < 1) grid = 1;
-  const long long chunk = ((long long)N + grid - 1) / grid;
+  // chunks of a multiple of 8 elements keep every chunk's start 16-byte
+  // aligned when X is (the vector path of ia_scan)
+  const long long chunk = (((long long)N + grid - 1) / grid + 7) / 8 * 8;
   grid = ((long long)N + chunk - 1) / chunk;
   IamaxRec *rec = static_cast<IamaxRec *>(c.buffer(kBufIamax, sizeof(IamaxRec) * (size_t)grid));
   iamax_kernel<T><<<(int)grid, kIaThreads, 0, st>>>(N, X, incX, unit, chunk, rec, result);

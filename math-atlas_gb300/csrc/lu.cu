@@ -1325,6 +1325,11 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     int *ipk = ipiv + k;
     int koff = k;
     void *args[] = {&Ap, (void *)&lda, &Mp, (void *)&jb, &koff, &ipk, &info, &rec, &jrow, &bar, &perm};
+    cudaEvent_t prof_b = nullptr;
+    if (c.prof_panels) {
+      prof_b = c.event();
+      ATLG_CHECK(cudaEventRecord(prof_b, st));
+    }
     // one cluster when the panel fits its shared memory (panels only shrink,
     // so the grid path below is never needed after it)
     const size_t ctile = cn ? sizeof(T) * (size_t)((Mp + cn - 1) / cn) * cl_rs<T>(jb) : 0;
@@ -1358,6 +1363,11 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
         ATLG_CHECK(cudaLaunchCooperativeKernel((const void *)panel_kernel<T, false>, dim3(G), dim3(PT), args, 0, st));
     }
     note_launch();
+    if (prof_b) {
+      cudaEvent_t prof_e = c.event();
+      ATLG_CHECK(cudaEventRecord(prof_e, st));
+      c.panel_recs.push_back({prof_b, prof_e, (double)jb});
+    }
     const int c_from = k + jb;
     const int nxt = (c_from < MN) ? ((MN - c_from < PW) ? MN - c_from : PW) : 0;
     // the interchanges touch every other column: the side update must be done
