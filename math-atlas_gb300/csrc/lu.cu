@@ -839,10 +839,23 @@ __global__ void __launch_bounds__(kChainThreads)
   const int tid = threadIdx.x;
   int viol = 0;
   for (int x = tid; x < nrows; x += kChainThreads) ls[x] = -1;
-  for (int s = tid; s < n; s += kChainThreads) {
-    const int j = K1 + s, ip = ipiv[(size_t)j * step];
-    r[s] = ip;
-    if (ip != j && ip >= 0 && ip < nrows && ip < j) viol = 1;
+  // the pivots, 8 loads in flight per thread (one dependent round trip per
+  // batch instead of per pivot)
+  for (int s0 = tid; s0 < n; s0 += 8 * kChainThreads) {
+    int ipb[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int s = s0 + u * kChainThreads;
+      ipb[u] = s < n ? ipiv[(size_t)(K1 + s) * step] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int s = s0 + u * kChainThreads, j = K1 + s, ip = ipb[u];
+      if (s < n) {
+        r[s] = ip;
+        if (ip != j && ip >= 0 && ip < nrows && ip < j) viol = 1;
+      }
+    }
   }
   if (__syncthreads_or(viol)) {        // general pivots: the chain, one thread
     for (int x = tid; x < nrows; x += kChainThreads) ls[x] = x;
@@ -1061,10 +1074,21 @@ __global__ void __launch_bounds__(kLcThreads)
   if (tid == 0) { s_lo = nrows; s_hi = 0; s_mv = 0; s_cnt = 0; }
   __syncthreads();
   int lo = nrows, hi = 0, mv = 0;
-  for (int r = tid; r < nrows; r += kLcThreads) {
-    const int s = content_g[r];
-    content[r] = s;
-    if (s != r) { lo = min(lo, r); hi = max(hi, r + 1); ++mv; }
+  for (int r0 = tid; r0 < nrows; r0 += 8 * kLcThreads) {   // 8 table loads in flight per thread
+    int sb[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int r = r0 + u * kLcThreads;
+      sb[u] = r < nrows ? __ldg(content_g + r) : r;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int r = r0 + u * kLcThreads, s = sb[u];
+      if (r < nrows) {
+        content[r] = s;
+        if (s != r) { lo = min(lo, r); hi = max(hi, r + 1); ++mv; }
+      }
+    }
   }
   lo = __reduce_min_sync(0xffffffffu, lo);
   hi = __reduce_max_sync(0xffffffffu, hi);
