@@ -793,6 +793,22 @@ def measure_memory(G, O, torch, reps=5):
         out[name] = row
         del A
     torch.cuda.empty_cache()
+    # FP64 GEMV y = b - A x at n = 16384 (the mixed solver's refinement
+    # residual): the 2 GiB matrix read once
+    n = 16384
+    g = torch.Generator(device="cuda").manual_seed(43)
+    Ad = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g)
+    xd = torch.randn(n, device="cuda", dtype=torch.float64, generator=g)
+    yd = torch.randn(n, device="cuda", dtype=torch.float64, generator=g)
+    torch.cuda.synchronize()
+    ms = timed(lambda: L.atlg_dgemv_dev(111, n, n, -1.0, Ad.data_ptr(), n, xd.data_ptr(), 1, 1.0, yd.data_ptr(), st))
+    alg = 8.0 * n * n
+    out["dgemv_n16384"] = {"n": n, "ms": ms, "algorithmic_bytes": alg, "gbs": alg / (ms * 1e-3) / 1e9,
+                           "peak_gbs": peak, "frac": alg / (ms * 1e-3) / 1e9 / peak,
+                           "timing": "CUDA events on the library stream around atlg_dgemv_dev (NoTrans, "
+                                     "alpha -1, beta 1), best of %d after one warm-up" % reps}
+    del Ad, xd, yd
+    torch.cuda.empty_cache()
     # chained FP32 TRSV on the factors of an FP32 LU at n = 16384 (the mixed
     # solver's refinement solve): n^2/2 FP32 elements of the triangle read once
     n = 16384

@@ -360,13 +360,17 @@ __global__ void __launch_bounds__(256)
   if (i < M) {
     const T *a = A + i;
     int k = w;
-    for (; k + 24 < K; k += 32) {
-      const T a0 = a[(size_t)k * lda], a1 = a[(size_t)(k + 8) * lda];
-      const T a2 = a[(size_t)(k + 16) * lda], a3 = a[(size_t)(k + 24) * lda];
-      acc = fma(a0, x[(size_t)k * incx], acc);
-      acc = fma(a1, x[(size_t)(k + 8) * incx], acc);
-      acc = fma(a2, x[(size_t)(k + 16) * incx], acc);
-      acc = fma(a3, x[(size_t)(k + 24) * incx], acc);
+    // 8 columns' loads in flight per thread before their FMAs (the same
+    // per-thread summation order as one column at a time)
+    for (; k + 56 < K; k += 64) {
+      T av[8], xv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        av[u] = a[(size_t)(k + 8 * u) * lda];
+        xv[u] = x[(size_t)(k + 8 * u) * incx];
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) acc = fma(av[u], xv[u], acc);
     }
     for (; k < K; k += 8) acc = fma(a[(size_t)k * lda], x[(size_t)k * incx], acc);
   }
@@ -399,9 +403,69 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// y = alpha A x + beta y for a large column-major A (NoTrans): a CTA takes a
+// 2048-row x 128-column tile, so each column piece it reads is 16 KB
+// contiguous (a 32-row strip per column, as gemv_n_kernel reads, leaves the
+// HBM rows mostly unused); the per-tile partial sums go to `part` and one
+// more kernel adds the column tiles in a fixed order.
+constexpr int GV_RB = 2048, GV_CB = 128, GV_U = 4;
+template <typename T>
+__global__ void __launch_bounds__(256, 2)
+    gemv_n_tile_kernel(int M, int K, const T *__restrict__ A, int lda, const T *__restrict__ x, int incx,
+                       T *__restrict__ part, int ldp) {
+  const int r0 = blockIdx.x * GV_RB, c0 = blockIdx.y * GV_CB;
+  const int ce = (c0 + GV_CB < K) ? c0 + GV_CB : K;
+  T acc[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc[q] = T(0);
+  for (int c = c0; c < ce; c += GV_U) {
+    T av[GV_U][8], xv[GV_U];
+#pragma unroll
+    for (int u = 0; u < GV_U; ++u) {
+      const bool cok = c + u < ce;
+      xv[u] = cok ? x[(size_t)(c + u) * incx] : T(0);
+      const T *col = A + (size_t)(c + u) * lda;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int i = r0 + threadIdx.x + 256 * q;
+        av[u][q] = (cok && i < M) ? col[i] : T(0);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < GV_U; ++u)
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[q] = fma(av[u][q], xv[u], acc[q]);
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int i = r0 + threadIdx.x + 256 * q;
+    if (i < M) part[i + (size_t)blockIdx.y * ldp] = acc[q];
+  }
+}
+template <typename T>
+__global__ void __launch_bounds__(256)
+    gemv_reduce_kernel(int M, int S, T alpha, const T *__restrict__ part, int ldp, T beta, T *__restrict__ y) {
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  if (i >= M) return;
+  T s = T(0);
+  for (int g = 0; g < S; ++g) s += part[i + (size_t)g * ldp];
+  const T v = alpha * s;
+  y[i] = (beta == T(0)) ? v : fma(beta, y[i], v);
+}
+
 template <typename T>
 static void gemv_launch(int TA, int M, int K, T alpha, const T *A, int lda, const T *x, int incx, T beta, T *y,
                         cudaStream_t st) {
+  if (TA == kNoTrans && M >= GV_RB && K >= 8 * GV_CB) {
+    const int S = (K + GV_CB - 1) / GV_CB;
+    const int ldp = (M + 31) & ~31;
+    T *part = static_cast<T *>(ctx().buffer(kBufGemv, sizeof(T) * (size_t)ldp * S));
+    gemv_n_tile_kernel<T><<<dim3((M + GV_RB - 1) / GV_RB, S), 256, 0, st>>>(M, K, A, lda, x, incx, part, ldp);
+    gemv_reduce_kernel<T><<<(M + 255) / 256, 256, 0, st>>>(M, S, alpha, part, ldp, beta, y);
+    note_launch(2);
+    ATLG_CHECK(cudaGetLastError());
+    return;
+  }
   if (TA == kNoTrans)
     gemv_n_kernel<T><<<(M + 31) / 32, 256, 0, st>>>(M, K, alpha, A, lda, x, incx, beta, y);
   else

@@ -828,6 +828,9 @@ __device__ int cta_exclusive_scan(int *v, int m, int *wsum) {
   return total;
 }
 
+// PER: sources per thread in the jumping rounds (8 when n <= 8192: half the
+// predicated-off work of 16 for the common sizes)
+template <int PER>
 __global__ void __launch_bounds__(kChainThreads)
     laswp_chain_kernel(const int *ipiv, int K1, int K2, int inci, int *content_g, int nrows, int buckets) {
   extern __shared__ int ch_smem[];
@@ -954,10 +957,10 @@ __global__ void __launch_bounds__(kChainThreads)
   }
   __syncthreads();
   for (;;) {                           // pointer jumping: V(i) = V(last(i))
-    int np[kChainPer], nv[kChainPer];
+    int np[PER], nv[PER];
     int any = 0;
 #pragma unroll
-    for (int k = 0; k < kChainPer; ++k) {
+    for (int k = 0; k < PER; ++k) {
       const int s = tid + k * kChainThreads;
       np[k] = -1;
       nv[k] = 0;
@@ -974,7 +977,7 @@ __global__ void __launch_bounds__(kChainThreads)
     }
     if (!__syncthreads_or(any)) break;
 #pragma unroll
-    for (int k = 0; k < kChainPer; ++k) {
+    for (int k = 0; k < PER; ++k) {
       const int s = tid + k * kChainThreads;
       if (s < n) {
         ptr[s] = np[k];
@@ -1005,10 +1008,17 @@ static void launch_interchange_table(const int *ipiv, int K1, int K2, int inci, 
     // the warp scan takes n/32 dependent rounds: cheap for a block column's
     // interchanges, the counting sort wins for a whole pivot vector
     const bool bk = n > 2048 && chain_bucket_fits(nrows, n);
-    ATLG_CHECK(cudaFuncSetAttribute(laswp_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)kChainSmemMax));
-    laswp_chain_kernel<<<1, kChainThreads, chain_smem_bytes(nrows, n, bk), st>>>(ipiv, K1, K2, inci, content,
-                                                                                 nrows, bk ? 1 : 0);
+    const size_t smem = chain_smem_bytes(nrows, n, bk);
+    if (n <= 8 * kChainThreads) {
+      ATLG_CHECK(cudaFuncSetAttribute(laswp_chain_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kChainSmemMax));
+      laswp_chain_kernel<8><<<1, kChainThreads, smem, st>>>(ipiv, K1, K2, inci, content, nrows, bk ? 1 : 0);
+    } else {
+      ATLG_CHECK(cudaFuncSetAttribute(laswp_chain_kernel<kChainPer>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kChainSmemMax));
+      laswp_chain_kernel<kChainPer><<<1, kChainThreads, smem, st>>>(ipiv, K1, K2, inci, content, nrows,
+                                                                    bk ? 1 : 0);
+    }
   } else {
     const int mode = ((long)nrows + n <= kPermSmemRows) ? 2 : (nrows <= kPermSmemRows ? 1 : 0);
     const size_t smem = mode == 2 ? sizeof(int) * ((size_t)nrows + n) : mode == 1 ? sizeof(int) * (size_t)nrows : 0;

@@ -217,3 +217,31 @@ def test_strsv_chain_rejects_bad_arguments(gb):
     assert L.atlg_strsv_chain_prepare_dev(122, 132, -1, None, 1, None, None) == -1
     assert L.atlg_strsv_chain_prepare_dev(123, 132, 10, None, 10, None, None) == -1
     assert L.atlg_strsv_chain_dev(122, 10, None, 5, None, None, None) == -1
+
+
+@pytest.mark.parametrize("M,K,incx,beta", [(5000, 3000, 1, 0.5), (2048, 1024, 3, 0.0), (4097, 1500, 1, -1.0)])
+def test_dgemv_large_tiled_form(gb, M, K, incx, beta):
+    """NoTrans GEMV with M >= 2048 and K >= 1024 takes the tiled form (column
+    tiles summed in a fixed order by a second kernel): against torch FP64,
+    beta = 0 never reading y (NaN there stays out of the result), and the
+    same bits on a repeated call."""
+    torch = pytest.importorskip("torch")
+    L = gb.lib()
+    g = torch.Generator(device="cuda").manual_seed(M + K)
+    A = torch.randn(K, M, device="cuda", dtype=torch.float64, generator=g)     # column-major M x K
+    xs = torch.randn(K * incx, device="cuda", dtype=torch.float64, generator=g)
+    y0 = torch.randn(M, device="cuda", dtype=torch.float64, generator=g)
+    if beta == 0.0:
+        y0[::7] = float("nan")
+    outs = []
+    for _ in range(2):
+        y = y0.clone()
+        torch.cuda.synchronize()
+        assert L.atlg_dgemv_dev(111, M, K, 1.25, A.data_ptr(), M, xs.data_ptr(), incx, beta, y.data_ptr(), None) == 0
+        torch.cuda.synchronize()
+        outs.append(y)
+    ref = 1.25 * (A.T @ xs[::incx]) + (beta * y0 if beta != 0.0 else 0.0)
+    assert torch.isfinite(outs[0]).all()
+    err = float((outs[0] - ref).abs().max() / ref.abs().max())
+    assert err < 1e-13, err
+    assert torch.equal(outs[0], outs[1])
