@@ -1497,7 +1497,24 @@ static void getrs_impl(int order, int trans, int N, int NRHS, const T *A, int ld
     }
     return;
   }
-  if (order == kColMajor) {
+  if (order == kColMajor && NRHS >= 8 && N >= 256) {
+    // many right-hand sides: the solves apply 64 x 64 diagonal-block inverses
+    auto solve = [&](int uplo, int ta, int diag) {
+      if (sizeof(T) == 8)
+        dev_dtrsm_left_inv(uplo, ta, diag, N, NRHS, (const double *)A, lda, (double *)B, ldb, st);
+      else
+        dev_strsm_left_inv(uplo, ta, diag, N, NRHS, (const float *)A, lda, (float *)B, ldb, st);
+    };
+    if (trans == kNoTrans) {
+      laswp_impl<T>(NRHS, B, ldb, 0, N, ipiv, 1, N, st);
+      solve(kLower, kNoTrans, kUnit);
+      solve(kUpper, kNoTrans, kNonUnit);
+    } else {
+      solve(kUpper, kTrans, kNonUnit);
+      solve(kLower, kTrans, kUnit);
+      laswp_impl<T>(NRHS, B, ldb, 0, N, ipiv, -1, N, st);
+    }
+  } else if (order == kColMajor) {
     if (trans == kNoTrans) {
       laswp_impl<T>(NRHS, B, ldb, 0, N, ipiv, 1, N, st);
       trsm_any<T>(order, kLeft, kLower, kNoTrans, kUnit, N, NRHS, A, lda, B, ldb, st);

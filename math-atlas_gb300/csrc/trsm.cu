@@ -183,6 +183,110 @@ static void trsm_impl(int side, int uplo, int tA, int diag, int M, int N, T alph
   }
 }
 
+// ---------------------------------------------- left solves with block inverses
+// For many right-hand sides (getrs with NRHS >= 8, the adjoint's transposed
+// solves) the 64-step substitution of each diagonal block (one warp per
+// right-hand side, a dependent chain) dominates its step.  Here every
+// diagonal block of the stored triangle is inverted once (one CTA per block,
+// column by column: X(0:j, j) = -inv(T(0:j,0:j)) T(0:j, j) / T(j,j)) into a
+// workspace of 64 x 64 column-major blocks, and each step applies
+// op(inv(T_bb)) to its rows of B as a small dense product; the updates of the
+// other rows are the same GEMMs as trsm_impl's.  inv(op(T)) = op(inv(T)), so
+// one set of inverses serves both op(A) = A and A^T.  Rounding differs from
+// substitution.
+template <typename T>
+__global__ void __launch_bounds__(TB) trsm_inv_diag_kernel(int M, const T *__restrict__ A, int lda, int upper,
+                                                           int unit, T *__restrict__ W) {
+  __shared__ T a[TB][TB + 1];
+  const int o = blockIdx.x * TB;
+  const int nb = (M - o < TB) ? M - o : TB;
+  const int tid = threadIdx.x;
+  const T *Ab = A + o + (size_t)o * lda;
+  // a = the block as an upper triangle (a lower block is inverted through its transpose)
+  for (int e = tid; e < TB * TB; e += TB) {
+    const int i = e % TB, k = e / TB;
+    T v = T(0);
+    if (i < nb && k < nb && i <= k) v = upper ? Ab[i + (size_t)k * lda] : Ab[k + (size_t)i * lda];
+    a[i][k] = v;
+  }
+  __syncthreads();
+  if (unit && tid < nb) a[tid][tid] = T(1);
+  __syncthreads();
+  for (int j = 0; j < nb; ++j) {
+    const T dinv = unit ? T(1) : T(1) / a[j][j];
+    T t = T(0);
+    if (tid < j)
+      for (int k = tid; k < j; ++k) t = fma(a[tid][k], a[k][j], t);
+    __syncthreads();
+    if (tid < j) a[tid][j] = -dinv * t;
+    if (tid == j) a[j][j] = dinv;
+    __syncthreads();
+  }
+  T *Wb = W + (size_t)blockIdx.x * TB * TB;
+  for (int e = tid; e < TB * TB; e += TB) {
+    const int i = e % TB, k = e / TB;
+    T v = T(0);
+    if (i < nb && k < nb) v = upper ? (i <= k ? a[i][k] : T(0)) : (k <= i ? a[k][i] : T(0));
+    Wb[e] = v;                                   // W(i, k), column-major
+  }
+}
+
+// B(0:n, c) <- op(Wb) B(0:n, c) for 4 right-hand sides per CTA.
+template <typename T>
+__global__ void __launch_bounds__(256) trsm_inv_apply_kernel(const T *__restrict__ Wb, int ta, int n, int N, T *B,
+                                                             int ldb) {
+  __shared__ T w[TB][TB + 1];
+  __shared__ T bs[4][TB];
+  const int tid = threadIdx.x, i = tid & (TB - 1), cl = tid >> 6;
+  const int c = blockIdx.x * 4 + cl;
+  for (int e = tid; e < TB * TB; e += 256) w[e / TB][e % TB] = Wb[e];   // w[k][r] = W(r, k)
+  bs[cl][i] = (c < N && i < n) ? B[i + (size_t)c * ldb] : T(0);
+  __syncthreads();
+  T acc = T(0);
+  if (ta == kNoTrans) {
+    for (int k = 0; k < n; ++k) acc = fma(w[k][i], bs[cl][k], acc);     // W(i, k)
+  } else {
+    for (int k = 0; k < n; ++k) acc = fma(w[i][k], bs[cl][k], acc);     // W(k, i)
+  }
+  if (c < N && i < n) B[i + (size_t)c * ldb] = acc;
+}
+
+template <typename T>
+static void trsm_left_inv_impl(int uplo, int tA, int diag, int M, int N, const T *A, int lda, T *B, int ldb,
+                               cudaStream_t st) {
+  if (M <= 0 || N <= 0) return;
+  const int ta = (tA == kNoTrans) ? kNoTrans : kTrans;
+  const int unit = (diag == kUnit);
+  const bool lower = (uplo == kLower) != (ta != kNoTrans);   // of op(A)
+  const int nb = (M + TB - 1) / TB;
+  T *W = static_cast<T *>(ctx().buffer(kBufTrsmInv, sizeof(T) * (size_t)nb * TB * TB));
+  trsm_inv_diag_kernel<T><<<nb, TB, 0, st>>>(M, A, lda, uplo == kUpper ? 1 : 0, unit, W);
+  note_launch();
+  ATLG_CHECK(cudaGetLastError());
+  const int gridN = (N + 3) / 4;
+  for (int s = 0; s < nb; ++s) {
+    const int b = lower ? s : nb - 1 - s;
+    const int r0 = b * TB, n = (M - r0 < TB) ? M - r0 : TB;
+    trsm_inv_apply_kernel<T><<<gridN, 256, 0, st>>>(W + (size_t)b * TB * TB, ta, n, N, B + r0, ldb);
+    note_launch();
+    ATLG_CHECK(cudaGetLastError());
+    if (lower && r0 + n < M)
+      gemm_any<T>(ta, kNoTrans, M - r0 - n, N, n, T(-1), opblk(A, lda, ta, r0 + n, r0), lda, B + r0, ldb, T(1),
+                  B + r0 + n, ldb, st);
+    if (!lower && r0 > 0)
+      gemm_any<T>(ta, kNoTrans, r0, N, n, T(-1), opblk(A, lda, ta, 0, r0), lda, B + r0, ldb, T(1), B, ldb, st);
+  }
+}
+
+void dev_dtrsm_left_inv(int uplo, int ta, int diag, int M, int N, const double *A, int lda, double *B, int ldb,
+                        cudaStream_t st) {
+  trsm_left_inv_impl<double>(uplo, ta, diag, M, N, A, lda, B, ldb, st);
+}
+void dev_strsm_left_inv(int uplo, int ta, int diag, int M, int N, const float *A, int lda, float *B, int ldb,
+                        cudaStream_t st) {
+  trsm_left_inv_impl<float>(uplo, ta, diag, M, N, A, lda, B, ldb, st);
+}
+
 void dev_dtrsm(int side, int uplo, int ta, int diag, int M, int N, double alpha, const double *A, int lda,
                double *B, int ldb, cudaStream_t st) {
   trsm_impl<double>(side, uplo, ta, diag, M, N, alpha, A, lda, B, ldb, st);

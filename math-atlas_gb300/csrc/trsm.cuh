@@ -9,6 +9,13 @@ void dev_dtrsm(int side, int uplo, int ta, int diag, int M, int N, double alpha,
                double *B, int ldb, cudaStream_t st);
 void dev_strsm(int side, int uplo, int ta, int diag, int M, int N, float alpha, const float *A, int lda, float *B,
                int ldb, cudaStream_t st);
+// Left-side op(A) X = B (alpha 1, column-major) through 64 x 64 diagonal-block
+// inverses formed once per call: for many right-hand sides (rounding differs
+// from substitution).
+void dev_dtrsm_left_inv(int uplo, int ta, int diag, int M, int N, const double *A, int lda, double *B, int ldb,
+                        cudaStream_t st);
+void dev_strsm_left_inv(int uplo, int ta, int diag, int M, int N, const float *A, int lda, float *B, int ldb,
+                        cudaStream_t st);
 // L11 * X = B with L11 = unit lower A[k:k+n, k:k+n] (n <= 64): the LU's U12 solve.
 void dev_trsm_llnu_block(const double *A, int lda, int k, int n, double *B, int ldb, int ncols, cudaStream_t st);
 void dev_trsm_llnu_block(const float *A, int lda, int k, int n, float *B, int ldb, int ncols, cudaStream_t st);
