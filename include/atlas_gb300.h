@@ -263,6 +263,12 @@ int atlg_dlaswp_noalloc(int N, double *A, int lda, int K1, int K2, const int *ip
  * block cluster's shared memory with the cluster kernel, 0 always uses the
  * cooperative-grid kernel; both give bit-identical factors and pivots */
 void atlg_panel_cluster(int on);
+/* LU panels too tall for one cluster at their full width (no reference
+ * counterpart): 1 (default) factors them as two halves on the cluster (left
+ * half, its interchanges, triangular solve and update on the right half,
+ * right half), 0 on the cooperative-grid kernel; factors agree to rounding,
+ * pivots are the same partial-pivoting choices */
+void atlg_panel_split(int on);
 /* refinement solves of dgesv_mixed with one right-hand side (no reference
  * counterpart): 1 (default) the chained TRSV over 128-row blocks with block
  * inverses formed once per factorization, 0 the 64-row look-back TRSV; both

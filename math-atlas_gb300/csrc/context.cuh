@@ -37,7 +37,7 @@ struct Context {
   cudaEvent_t event();
   cudaStream_t side = nullptr;       // low-priority stream for overlapped updates
   cudaStream_t outer = nullptr;      // a second one, for a driver whose inner steps use `side`
-  cudaEvent_t sync_ev[4] = {};       // cross-stream ordering (no timing)
+  cudaEvent_t sync_ev[6] = {};       // cross-stream ordering (no timing)
   cudaStream_t side_stream();
   cudaStream_t outer_stream();
   cudaEvent_t sync_event(int i);

@@ -498,11 +498,20 @@ __global__ void __launch_bounds__(CT)
   const int nvj = (jb + VE - 1) / VE;            // vectors holding the jb columns
   T *sa = reinterpret_cast<T *>(panel_dyn);      // own rows, row-major, stride RS
 #define AT(i_, c_) sa[(size_t)((i_) - r0) * RS + (c_)]
-  if (nr > 0)
-    for (int e = tid; e < nr * jb; e += CT) {
-      const int i = e % nr, c = e / nr;
-      sa[(size_t)i * RS + c] = Ag[(r0 + i) + (size_t)c * lda];
+  // own rows into shared memory: a thread per row, each element an
+  // asynchronous copy (coalesced over the warp's consecutive rows), all of
+  // them in flight at once
+  for (int i = tid; i < nr; i += CT) {
+    const T *src = Ag + r0 + i;
+    T *dst = sa + (size_t)i * RS;
+    for (int c = 0; c < jb; ++c) {
+      if (sizeof(T) == 8) cp_async8(dst + c, src + (size_t)c * lda, true);
+      else cp_async4(dst + c, src + (size_t)c * lda, true);
     }
+  }
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
   cluster.sync();   // every CTA of the cluster is running before the first push
 
   // Reduce the per-thread candidates (rows ci already complete) to the CTA's
@@ -551,10 +560,9 @@ __global__ void __launch_bounds__(CT)
     warp_winner(v, b, idx);
     const bool zero = !(b < CN && v > K(0));
     const int p = zero ? j : idx;
-    if (me == 0 && tid == 0) {
-      ipiv[j] = koff + p;
+    if (tid == 0) {                // the pivots reach global memory after the loop
       piv_local[j] = p;
-      if (zero && *info == 0) *info = koff + j + 1;
+      if (zero && me == 0 && *info == 0) *info = koff + j + 1;
     }
     const bool last = (j + 1 >= jb);
     K best = K(-1);
@@ -585,28 +593,39 @@ __global__ void __launch_bounds__(CT)
       const bool use_rcp = s_use_rcp[par] != 0;
       const T rcp = s_rcp[par];
       const int lo = r0 > j ? r0 : j;
-      // phase 1: multipliers and column j+1 of every own row (rows j and p
-      // completely), with the first-max of column j+1
+      // phase 1: rows j and p completely, one 16-byte vector per lane of a
+      // warp each (nvj <= 32); every other own row its multiplier and
+      // column j+1, with the first-max of column j+1
+      if (w == NW - 1 && j >= r0 && j < r1 && lane < nvj)        // row j <- pivot row
+        reinterpret_cast<V *>(&AT(j, 0))[lane] = reinterpret_cast<const V *>(Ps)[lane];
+      if (w == NW - 2 && p != j && p >= r0 && p < r1 && lane < nvj) {   // row p <- old row j, eliminated
+        const T l = use_rcp ? Js[j] * rcp : Js[j] / pv;
+        V jv = reinterpret_cast<const V *>(Js)[lane];
+        const V pvec = reinterpret_cast<const V *>(Ps)[lane];
+        T *x = reinterpret_cast<T *>(&jv);
+        const T *y = reinterpret_cast<const T *>(&pvec);
+#pragma unroll
+        for (int e = 0; e < VE; ++e) {
+          const int c = lane * VE + e;
+          if (c == j) x[e] = l;
+          else if (c > j && c < jb) x[e] = x[e] - l * y[e];
+        }
+        reinterpret_cast<V *>(&AT(p, 0))[lane] = jv;
+        if (!last && lane == (j + 1) / VE) {   // the lane's own store: visible to it
+          const K a = PivKey<T>::key(AT(p, j + 1));
+          if (a > best || (a == best && p < bi)) { best = a; bi = p; }
+        }
+      }
       for (int i = lo + tid; i < r1; i += CT) {
+        if (i == j || i == p) continue;
         T *row = &AT(i, 0);
-        if (i == j) {                       // row j <- pivot row
-          for (int q = 0; q < nvj; ++q) reinterpret_cast<V *>(row)[q] = reinterpret_cast<const V *>(Ps)[q];
-          continue;
-        }
-        if (i == p) {                       // row p <- old row j, eliminated
-          const T l = use_rcp ? Js[j] * rcp : Js[j] / pv;
-          for (int c = 0; c < j; ++c) row[c] = Js[c];
-          row[j] = l;
-          for (int c = j + 1; c < jb; ++c) row[c] = Js[c] - l * Ps[c];
-        } else {
-          const T src = row[j];
-          const T l = use_rcp ? src * rcp : src / pv;
-          row[j] = l;
-          if (!last) row[j + 1] -= l * Ps[j + 1];
-        }
+        const T src = row[j];
+        const T l = use_rcp ? src * rcp : src / pv;
+        row[j] = l;
         if (!last) {
+          row[j + 1] -= l * Ps[j + 1];
           const K a = PivKey<T>::key(row[j + 1]);
-          if (a > best) { best = a; bi = i; }
+          if (a > best || (a == best && i < bi)) { best = a; bi = i; }
         }
       }
       if (!last) {
@@ -657,13 +676,39 @@ __global__ void __launch_bounds__(CT)
     if (last) break;
   }
   cluster.sync();   // no CTA leaves while another may still read or push to it
-  if (nr > 0)
-    for (int e = tid; e < nr * jb; e += CT) {
-      const int i = e % nr, c = e / nr;
-      Ag[(r0 + i) + (size_t)c * lda] = sa[(size_t)i * RS + c];
+  if (me == 0)
+    for (int t = tid; t < jb; t += CT) ipiv[t] = koff + piv_local[t];
+  // warp 0 of the last CTA reduces the interchanges while its other warps
+  // (and every other CTA) write the rows back: a thread per row, 16-byte
+  // shared-memory reads, stores coalesced over the warp's consecutive rows
+  const bool red = (me == CN - 1);
+  if (red && w == 0) {
+    reduce_interchanges(piv_local, jb, perm);
+  } else {
+    const int t0 = red ? tid - 32 : tid, nt = red ? CT - 32 : CT;
+    for (int i = t0; i < nr; i += nt) {
+      const V *srow = reinterpret_cast<const V *>(sa + (size_t)i * RS);
+      T *dst = Ag + r0 + i;
+      for (int q = 0; q < nvj; ++q) {
+        const V v = srow[q];
+        const T *x = reinterpret_cast<const T *>(&v);
+#pragma unroll
+        for (int e = 0; e < VE; ++e)
+          if (q * VE + e < jb) dst[(size_t)(q * VE + e) * lda] = x[e];
+      }
     }
+  }
 #undef AT
-  if (me == 0 && tid < 32) reduce_interchanges(piv_local, jb, perm);
+}
+
+// The permutation record of a panel factored in two halves: its jb pivots
+// (global rows, ipiv[t] for column koff + t) reduced as the panel kernels
+// reduce theirs.  One warp.
+__global__ void panel_perm_kernel(const int *ipiv, int jb, int koff, int *perm) {
+  __shared__ int pl[NB];
+  for (int t = threadIdx.x; t < jb; t += 32) pl[t] = ipiv[t] - koff;
+  __syncwarp();
+  reduce_interchanges(pl, jb, perm);
 }
 
 // Apply a row permutation (perm: count, dst[], src[] relative to row k) to
@@ -1303,6 +1348,12 @@ static int cluster_panel_size() {
 }
 
 void set_panel_cluster(bool on) { g_panel_cluster = on; }
+// A panel too tall for one cluster at its full width, but not at half of it,
+// is factored as two halves on the cluster (left half; its interchanges,
+// triangular solve and update on the right half; right half) instead of on
+// the cooperative grid: the cluster's per-column exchange is the faster one.
+static bool g_panel_split = true;
+void set_panel_split(bool on) { g_panel_split = on; }
 static int g_panel_grid = 0;   // CTAs of the grid panel; 0: the default below
 void set_panel_grid(int ctas) { g_panel_grid = ctas > 0 ? ctas : 0; }
 // Panel width of the FP64 LU (8..NB, a multiple of 8).  A panel's own
@@ -1335,20 +1386,25 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
   // at least a few rows per CTA for the tallest panel
   if (G > (M + 7) / 8) G = (M + 7) / 8;
   if (G < 1) G = 1;
-  // one scratch block: rec[2G][RS] T, jrow[2NB] T, bar[2], perm[1+4NB]
+  // one scratch block: rec[2G][RS] T, jrow[2NB] T, bar[2], perm[npan][1+4NB]
+  // (a permutation record per panel: the interchanges of the columns left of
+  // a panel run later, on the side stream)
+  const int npan = (MN + PW - 1) / PW;
+  constexpr int kPermInts = 1 + 4 * NB;
   const size_t tbytes = sizeof(T) * ((size_t)2 * G * rec_stride<T>() + 2 * NB);
-  const size_t ibytes = sizeof(int) * ((size_t)2 + 1 + 4 * NB);
+  const size_t ibytes = sizeof(int) * ((size_t)2 + (size_t)kPermInts * npan);
   unsigned char *scr = static_cast<unsigned char *>(c.buffer(kBufW0, tbytes + ibytes + 64));
   T *rec = reinterpret_cast<T *>(scr);
   T *jrow = rec + (size_t)2 * G * rec_stride<T>();
   unsigned *bar = reinterpret_cast<unsigned *>(scr + ((tbytes + 15) & ~size_t(15)));
-  int *perm = reinterpret_cast<int *>(bar + 2);
+  int *perm0 = reinterpret_cast<int *>(bar + 2);
   ATLG_CHECK(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st));
   ATLG_CHECK(cudaFuncSetAttribute(panel_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kPanelSmemMax));
   cudaStream_t side = c.side_stream();
-  cudaEvent_t ev_ready = c.sync_event(0), ev_side = c.sync_event(1);
+  cudaEvent_t ev_ready = c.sync_event(0), ev_side = c.sync_event(1), ev_left = c.sync_event(4);
   bool side_pending = false;
+  bool left_pending = false;   // interchanges of left columns queued on the side stream
   const int cn = g_panel_cluster ? cluster_panel_size<T>() : 0;
   bool used_cluster = false;
 
@@ -1358,6 +1414,7 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     int Mp = M - k;
     int *ipk = ipiv + k;
     int koff = k;
+    int *perm = perm0 + (size_t)(k / PW) * kPermInts;
     void *args[] = {&Ap, (void *)&lda, &Mp, (void *)&jb, &koff, &ipk, &info, &rec, &jrow, &bar, &perm};
     cudaEvent_t prof_b = nullptr;
     if (c.prof_panels) {
@@ -1366,13 +1423,15 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     }
     // one cluster when the panel fits its shared memory (panels only shrink,
     // so the grid path below is never needed after it)
-    const size_t ctile = cn ? sizeof(T) * (size_t)((Mp + cn - 1) / cn) * cl_rs<T>(jb) : 0;
-    if (cn && ctile <= kClusterSmemMax) {
+    auto cluster_tile = [&](int rows, int width) -> size_t {
+      return cn ? sizeof(T) * (size_t)((rows + cn - 1) / cn) * cl_rs<T>(width) : 0;
+    };
+    auto launch_cluster = [&](T *Apan, int rows, int width, int kof, int *ip, size_t tile) {
       cudaLaunchConfig_t cfg = {};
       cudaLaunchAttribute at[1];
       cfg.gridDim = dim3(cn);
       cfg.blockDim = dim3(CT);
-      cfg.dynamicSmemBytes = ctile;
+      cfg.dynamicSmemBytes = tile;
       cfg.stream = st;
       at[0].id = cudaLaunchAttributeClusterDimension;
       at[0].val.clusterDim.x = cn;
@@ -1380,7 +1439,25 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
       at[0].val.clusterDim.z = 1;
       cfg.attrs = at;
       cfg.numAttrs = 1;
-      ATLG_CHECK(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T>, Ap, lda, Mp, jb, koff, ipk, info, perm));
+      ATLG_CHECK(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T>, Apan, lda, rows, width, kof, ip, info, perm));
+    };
+    const size_t ctile = cluster_tile(Mp, jb);
+    const int h = jb / 2;
+    const size_t htile = cluster_tile(Mp, jb - h);   // the taller half is the left one
+    if (cn && ctile <= kClusterSmemMax) {
+      launch_cluster(Ap, Mp, jb, koff, ipk, ctile);
+      used_cluster = true;
+    } else if (cn && g_panel_split && h >= 8 && htile <= kClusterSmemMax) {
+      T *Ar = A + k + (size_t)(k + h) * lda;          // rows k.. of the right half
+      launch_cluster(Ap, Mp, h, koff, ipk, htile);
+      apply_perm_kernel<T><<<(jb - h + 31) / 32, 256, 0, st>>>(A, lda, k, perm, 0, k + h, k + jb);
+      dev_trsm_llnu_block(A, lda, k, h, Ar, lda, jb - h, st);
+      gemm_any<T>(Mp - h, jb - h, h, Ap + h, lda, Ar, lda, Ar + h, lda, st);
+      launch_cluster(Ar + h, Mp - h, jb - h, koff + h, ipk + h, cluster_tile(Mp - h, jb - h));
+      apply_perm_kernel<T><<<(h + 31) / 32, 256, 0, st>>>(A, lda, k + h, perm, 0, k, k + h);
+      panel_perm_kernel<<<1, 32, 0, st>>>(ipk, jb, koff, perm);
+      note_launch(4);   // with the one below: two panels, two interchanges, the record
+      ATLG_CHECK(cudaGetLastError());
       used_cluster = true;
     } else {
       if (used_cluster) {   // the grid barrier counts every earlier column
@@ -1409,9 +1486,22 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
       ATLG_CHECK(cudaStreamWaitEvent(st, ev_side, 0));
       side_pending = false;
     }
+    // the columns right of the panel now; those left of it (needed only by
+    // the finished factorization) on the side stream behind this step's side
+    // update, or here when this step has none
+    const bool side_step = lookahead && c_from < N && k + jb < M && nxt > 0 && c_from + nxt < N;
     const int nl = (k + 31) / 32, nr = (N - c_from + 31) / 32;
-    if (nl + nr > 0) {
-      apply_perm_kernel<T><<<nl + nr, 256, 0, st>>>(A, lda, k, perm, k, c_from, N);
+    if (nr > 0) {
+      apply_perm_kernel<T><<<nr, 256, 0, st>>>(A, lda, k, perm, 0, c_from, N);
+      note_launch();
+      ATLG_CHECK(cudaGetLastError());
+    }
+    if (nl > 0 && !side_step) {
+      if (left_pending) {
+        ATLG_CHECK(cudaStreamWaitEvent(st, ev_left, 0));
+        left_pending = false;
+      }
+      apply_perm_kernel<T><<<nl, 256, 0, st>>>(A, lda, k, perm, k, N, N);
       note_launch();
       ATLG_CHECK(cudaGetLastError());
     }
@@ -1430,13 +1520,20 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
           dev_sgemm_tf32x3_pack_a(m, jb, (const float *)L21, lda, Ap, st);
           dev_sgemm_tf32x3_pack_b(jb, ntot, (const float *)U12, lda, Bp, st);
         }
-        if (lookahead && nxt > 0 && c_from + nxt < N) {
+        if (side_step) {
           trailing_update<T>(use_tc, m, nxt, jb, L21, U12, C, lda, 0, ntot, Ap, Bp, st);
           ATLG_CHECK(cudaEventRecord(ev_ready, st));
           ATLG_CHECK(cudaStreamWaitEvent(side, ev_ready, 0));
           trailing_update<T>(use_tc, m, ntot - nxt, jb, L21, U12, C, lda, nxt, ntot, Ap, Bp, side);
           ATLG_CHECK(cudaEventRecord(ev_side, side));
           side_pending = true;
+          if (nl > 0) {
+            apply_perm_kernel<T><<<nl, 256, 0, side>>>(A, lda, k, perm, k, N, N);
+            note_launch();
+            ATLG_CHECK(cudaGetLastError());
+            ATLG_CHECK(cudaEventRecord(ev_left, side));
+            left_pending = true;
+          }
         } else {
           trailing_update<T>(use_tc, m, ntot, jb, L21, U12, C, lda, 0, ntot, Ap, Bp, st);
         }
@@ -1444,6 +1541,7 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     }
   }
   if (side_pending) ATLG_CHECK(cudaStreamWaitEvent(st, ev_side, 0));
+  if (left_pending) ATLG_CHECK(cudaStreamWaitEvent(st, ev_left, 0));
 }
 
 void dev_dgetrf(int M, int N, double *A, int lda, int *ipiv, int *info, cudaStream_t st) {

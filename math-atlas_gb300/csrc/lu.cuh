@@ -7,6 +7,7 @@ namespace atlg {
 // false forces the cooperative-grid panel (the cluster panel is the default
 // where the panel fits one cluster's shared memory); results are identical.
 void set_panel_cluster(bool on);
+void set_panel_split(bool on);
 // CTAs of the cooperative-grid panel (0: a quarter of the SMs with look-ahead,
 // more when the row slices would not fit shared memory).
 void set_panel_grid(int ctas);

@@ -14,9 +14,10 @@
 // (K-major 128-byte-swizzled tiles of A' and B', 32 FP32 per row, 2 x 48 KB
 // stages), warp 1 tensor-memory allocation (256 columns) and MMA issue
 // (K = 8 per instruction), warps 2-9 stream the accumulator out of tensor
-// memory and update C in place (each thread one row, 128 columns).  Two CTAs
-// fit per SM, so one CTA's epilogue (the C read-modify-write, which bounds
-// the LU update) overlaps the other's MMAs.  All waits are bounded.
+// memory and update C in place (each thread one row, 128 columns; the tile
+// of C is prefetched into L2 while the MMAs run).  Two CTAs fit per SM, so
+// one CTA's epilogue (the C read-modify-write, which bounds the LU update)
+// overlaps the other's MMAs.  All waits are bounded.
 #include "common.cuh"
 #include "context.cuh"
 #include "tc.cuh"
@@ -152,6 +153,14 @@ __global__ void __launch_bounds__(XT_THREADS, 2)
     // C is read in batches of 16 independent loads (the first batch before
     // the accumulator is ready), so the read-modify-write is bandwidth-
     // rather than latency-bound
+    // the tile's C lines into L2 while the MMAs run (a warp-wide prefetch
+    // covers one 128-byte line of a column): the epilogue's reads then come
+    // from L2 instead of waiting on HBM 16 loads at a time
+    if (rok)
+      for (int j = 0; j < 128; ++j) {
+        const int gn = n0 + h * 128 + j;
+        if (gn < p.N) prefetch_l2(crow + (size_t)gn * p.ldc);
+      }
     float cv[16];
     auto load_batch = [&](int cb) {
 #pragma unroll

@@ -13,6 +13,8 @@
 // broadcast with a shuffle, and the diagonal is applied as a precomputed
 // reciprocal as in the reference.  The off-diagonal update is one GEMM per
 // block step on the library's DFMA/FFMA GEMM.
+#include <mutex>
+
 #include "common.cuh"
 #include "context.cuh"
 #include "gemm.cuh"
@@ -307,12 +309,65 @@ void dev_trsm_llnu_block(const double *A, int lda, int k, int n, double *B, int 
       note_launch();
   ATLG_CHECK(cudaGetLastError());
 }
+// FP32 form: a thread per right-hand side, its column in registers, the
+// triangle's columns read as shared-memory broadcasts.  Each element gets
+// the same fused multiply-adds in the same order as in trsm_diag_left
+// (x_i -= L_ik x_k for k = 0, 1, ..., i-1; the unit diagonal's reciprocal
+// is 1), so the result is bit-identical; the latency chain is one thread's
+// FMAs instead of a shuffle per row, and the FP32 pipe is not the limit.
+constexpr int kColsPerCta = 128;
+constexpr size_t kColsSmem = sizeof(float) * ((size_t)TB * TB + (size_t)kColsPerCta * (TB + 1));
+
+__global__ void __launch_bounds__(kColsPerCta)
+    trsm_llnu_cols_kernel(const float *__restrict__ L, int lda, int n, int ncols, float *__restrict__ B, int ldb) {
+  extern __shared__ float cs_smem[];
+  float *tri = cs_smem;                      // column-major: tri[k * TB + i] = L(i, k), strictly lower, 0 elsewhere
+  float *xs = cs_smem + TB * TB;             // column c of the strip at xs[c * (TB + 1) + i]
+  const int t = threadIdx.x;
+  const int c0 = blockIdx.x * kColsPerCta;
+  for (int e = t; e < TB * TB; e += kColsPerCta) {
+    const int i = e & (TB - 1), k = e / TB;
+    tri[e] = (k < i && i < n) ? L[i + (size_t)k * lda] : 0.f;
+  }
+  for (int e = t; e < kColsPerCta * TB; e += kColsPerCta) {
+    const int i = e & (TB - 1), c = e / TB;
+    xs[c * (TB + 1) + i] = (i < n && c0 + c < ncols) ? B[i + (size_t)(c0 + c) * ldb] : 0.f;
+  }
+  __syncthreads();
+  float x[TB];
+#pragma unroll
+  for (int i = 0; i < TB; ++i) x[i] = xs[t * (TB + 1) + i];
+#pragma unroll
+  for (int k = 0; k < TB - 1; ++k) {
+    const float xk = x[k];
+#pragma unroll
+    for (int i = k + 1; i < TB; ++i) x[i] = fmaf(-tri[k * TB + i], xk, x[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < TB; ++i) xs[t * (TB + 1) + i] = x[i];
+  __syncthreads();
+  for (int e = t; e < kColsPerCta * TB; e += kColsPerCta) {
+    const int i = e & (TB - 1), c = e / TB;
+    if (i < n && c0 + c < ncols) B[i + (size_t)(c0 + c) * ldb] = xs[c * (TB + 1) + i];
+  }
+}
+
 void dev_trsm_llnu_block(const float *A, int lda, int k, int n, float *B, int ldb, int ncols, cudaStream_t st) {
   if (n <= 0 || ncols <= 0) return;
-  const dim3 grid(diag_grid(ncols));
-  trsm_diag_left<float><<<grid, WARPS * 32, 0, st>>>(A + k + (size_t)k * lda, lda, kNoTrans, 1, 1, 0, n, ncols, B,
-                                                      ldb);
-      note_launch();
+  if (n <= TB) {
+    static std::once_flag once;
+    std::call_once(once, [] {
+      ATLG_CHECK(cudaFuncSetAttribute(trsm_llnu_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kColsSmem));
+    });
+    trsm_llnu_cols_kernel<<<(ncols + kColsPerCta - 1) / kColsPerCta, kColsPerCta, kColsSmem, st>>>(
+        A + k + (size_t)k * lda, lda, n, ncols, B, ldb);
+  } else {
+    const dim3 grid(diag_grid(ncols));
+    trsm_diag_left<float><<<grid, WARPS * 32, 0, st>>>(A + k + (size_t)k * lda, lda, kNoTrans, 1, 1, 0, n, ncols,
+                                                        B, ldb);
+  }
+  note_launch();
   ATLG_CHECK(cudaGetLastError());
 }
 

@@ -248,9 +248,12 @@ def test_dgetrf_sizes_in_sequence(gb):
 def test_cluster_panel_matches_grid_panel(gb, ora, dtype):
     """The cluster panel (distributed shared memory, hardware cluster barrier)
     and the cooperative-grid panel do the same arithmetic: bit-identical
-    pivots and factors, for panels on both sides of the cluster's capacity."""
+    pivots and factors, for panels on both sides of the cluster's capacity
+    (panels too tall for the cluster stay on the grid: the two-half split is
+    switched off here)."""
     L = gb.lib()
     sizes = (700, 3000, 7100) if dtype == np.float64 else (700, 5000, 15000)
+    L.atlg_panel_split(0)
     try:
         for n in sizes:
             A0 = ora.gegen(n, n, n * n + n, dtype=dtype)
@@ -266,3 +269,69 @@ def test_cluster_panel_matches_grid_panel(gb, ora, dtype):
             assert np.array_equal(out[0][0], out[1][0]), n
     finally:
         L.atlg_panel_cluster(1)
+        L.atlg_panel_split(1)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_split_panel_matches_grid_panel(gb, ora, dtype):
+    """Panels too tall for one cluster at 64 columns but not at 32 (FP64 above
+    6816 rows, FP32 above 13248) run as two cluster halves: left half, its
+    interchanges, triangular solve and update of the right half, right half,
+    and one permutation record for the whole panel.  Against the grid panel
+    (one launch per panel): the same pivots in FP64 (in FP32 the rounding
+    differences of the two orders of operations flip near-ties in some
+    column, after which the pivot sequences part: there every multiplier
+    |l_ij| <= 1, the partial-pivoting property, is checked instead), and an
+    LU residual |A(perm) - L U|_1 / (|A|_1 n eps) below 1 for both."""
+    torch = pytest.importorskip("torch")
+    L = gb.lib()
+    n = 7100 if dtype == np.float64 else 14000
+    eps = float(np.finfo(dtype).eps)
+    A0 = ora.gegen(n, n, n * n + n, dtype=dtype)
+    f = gb.clapack_dgetrf if dtype == np.float64 else gb.clapack_sgetrf
+    out = []
+    try:
+        for on in (1, 0):
+            L.atlg_panel_split(on)
+            A = A0.copy(order="F")
+            piv = np.zeros(n, dtype=np.int32)
+            assert f(102, n, n, A, n, piv) == 0
+            out.append((A, piv))
+    finally:
+        L.atlg_panel_split(1)
+    if dtype == np.float64:
+        assert np.array_equal(out[0][1], out[1][1])
+    else:
+        for F_np, p in out:
+            assert (p >= np.arange(n)).all() and (p < n).all()
+            assert float(np.abs(np.tril(F_np, -1)).max()) <= 1.0
+    n1 = lambda Z: float(Z.abs().sum(dim=0).max())
+    Ad = torch.from_numpy(np.asfortranarray(A0).astype(np.float64).T.copy()).cuda().T
+    for F_np, p in out:
+        perm = np.arange(n)
+        for i in range(n):
+            perm[[i, p[i]]] = perm[[p[i], i]]
+        F = torch.from_numpy(F_np.astype(np.float64).T.copy()).cuda().T
+        Lm = torch.tril(F, -1) + torch.eye(n, device="cuda", dtype=torch.float64)
+        resid = n1(Ad[torch.from_numpy(perm).cuda()] - Lm @ torch.triu(F)) / (n1(Ad) * n * eps)
+        assert resid <= 1.0, resid
+        del F, Lm
+    torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("m,n", [(64, 2000), (40, 517)])
+def test_sgetrf_block_row_solve_matches_strsm(gb, ora, m, n):
+    """The LU's solve for its top block row, U12 = inv(L11) A12 (FP32: a
+    thread per column, the column in registers), gives the same bits as
+    cblas_strsm (a warp per column) on the same operands.  With M <= 64 the
+    factorization is one panel, its interchanges on A12 and this solve."""
+    A0 = ora.gegen(m, n, 77 + n, dtype=np.float32)
+    F = A0.copy(order="F")
+    piv = np.zeros(m, dtype=np.int32)
+    assert gb.clapack_sgetrf(102, m, n, F, m, piv) == 0
+    B = np.asfortranarray(A0[:, m:])
+    for i in range(m):
+        B[[i, piv[i]]] = B[[piv[i], i]]
+    L11 = np.asfortranarray(F[:, :m])
+    gb.cblas_strsm(102, 141, 122, 111, 132, m, n - m, 1.0, L11, m, B, m)
+    assert np.array_equal(B, F[:, m:])
