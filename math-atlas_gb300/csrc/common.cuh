@@ -77,6 +77,51 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
       : "memory");
   return ok != 0;
 }
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n"
+      " mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Spin (non-blocking tests, no suspension) bounded in time rather than in
+// polls, for waits that end within microseconds in a correct run: false
+// after `limit_ns` of global time.
+__device__ __forceinline__ bool mbar_wait_for(uint64_t *bar, unsigned parity, unsigned long long limit_ns) {
+  if (mbar_test_wait(bar, parity)) return true;
+  const unsigned long long t0 = globaltimer_ns();
+  for (;;) {
+    for (int i = 0; i < 64; ++i)
+      if (mbar_test_wait(bar, parity)) return true;
+    if (globaltimer_ns() - t0 > limit_ns) return false;
+  }
+}
+
+// Distributed shared memory: the address of the same variable in CTA `rank`
+// of the cluster, and a 16-byte store into it that completes 16 bytes of the
+// transaction count of an mbarrier in that CTA (the receiver waits on its
+// own mbarrier; no cluster barrier and no fence on the sender).
+__device__ __forceinline__ unsigned cluster_map(unsigned saddr, int rank) {
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_async16(unsigned raddr, uint4 v, unsigned rbar) {
+  asm volatile(
+      "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(raddr),
+      "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "r"(rbar)
+      : "memory");
+}
+
 // Bounded wait; returns false (and flags the status word) on timeout.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, unsigned *status) {
   for (unsigned i = 0; i < kMbarPollLimit; ++i)

@@ -365,24 +365,27 @@ __global__ void __launch_bounds__(PT)
 // Cluster panel: the same factorization as panel_kernel (identical arithmetic
 // per element, so identical pivots and factors) for panels whose rows fit the
 // shared memory of one thread-block cluster (up to 16 CTAs on one GPC).
-// Per column j: each CTA keeps its first-max candidate row (and the owner of
-// row j that row) in its own shared memory and pushes only the candidate's
-// |a| and row index into every CTA; one hardware cluster barrier; each warp
-// then picks the winner from its own CTA's copy of the candidates; the CTA
-// pulls the winner's row and row j with 16-byte distributed-shared-memory
-// loads and eliminates in its rows (batched loads ahead of the stores)
-// before it reduces its first-max of column j+1.  Two CTA barriers and one
-// cluster barrier per column.  Everything a CTA publishes is
-// double buffered by column parity: column j+1 is published only after the
-// barrier of column j, which every CTA reaches after reading column j.
+// Per column j every CTA sends to every CTA of the cluster (itself
+// included) its first-max candidate -- key of |a|, row index and the whole
+// row -- and the owner of row j sends row j, all as 16-byte st.async stores
+// that count down the receiver's mbarrier for that column.  A CTA waits only
+// on its own mbarrier (no cluster barrier, no remote load on the critical
+// path), picks the winner from its local copies (every warp the same), takes
+// the winner's row and row j from its own shared memory, eliminates in its
+// rows and reduces its first-max of column j+1, which it sends on before the
+// rest of its rank-1 update.  The receive areas and mbarriers are double
+// buffered by column parity: a CTA sends column j+2 only after it has
+// received column j+1 from every CTA, which each sent only after copying
+// what it needed of column j.  Every message of the fixed protocol is sent,
+// so every wait ends; the waits are bounded all the same.
 constexpr int kClusterMax = 16;
 
+// One column's receive area: every CTA's candidate record (the row's
+// 16-byte vectors, then {key low, key high, row index, 0}) and row j.
 template <typename T>
-struct ClusterSlots {
-  __align__(16) T crow[2][NB];   // own candidate row
-  __align__(16) T jrow[2][NB];   // row j, in the CTA that owns it
-  typename PivKey<T>::K cval[2][kClusterMax];   // pushed by every CTA: key of candidate |a| (< 0: none)
-  int cidx[2][kClusterMax];      //                      candidate row
+struct ClusterRecv {
+  uint4 row[kClusterMax][NB * sizeof(T) / 16 + 1];
+  uint4 jrow[NB * sizeof(T) / 16];
 };
 
 template <typename T> struct Vec16;
@@ -477,9 +480,10 @@ __global__ void __launch_bounds__(CT)
   const int RS = cl_rs<T>(jb);
   constexpr int NW = CT / 32;
   extern __shared__ __align__(16) unsigned char panel_dyn[];
-  __shared__ ClusterSlots<T> slot;
+  __shared__ __align__(16) ClusterRecv<T> recv[2];
+  __shared__ __align__(8) uint64_t rbar[2];
   // pivot row and row j, double buffered by column parity: a thread still in
-  // the previous column's phase 2 may read one while the next is pulled
+  // the previous column's phase 2 may read one while the next is copied
   __shared__ __align__(16) T Pb[2][NB];
   __shared__ __align__(16) T Jb[2][NB];
   __shared__ T s_rcp[2];
@@ -511,8 +515,18 @@ __global__ void __launch_bounds__(CT)
   }
   cp_async_commit();
   cp_async_wait<0>();
+  // bytes a CTA receives per column: CN candidate records and row j
+  const unsigned TX = (unsigned)(16 * (CN * (nvj + 1) + nvj));
+  if (tid == 0) {
+    mbar_init(&rbar[0], 1);
+    mbar_init(&rbar[1], 1);
+    fence_mbar_init();
+    mbar_arrive_expect_tx(&rbar[0], TX);               // columns 0 and 1
+    if (jb > 1) mbar_arrive_expect_tx(&rbar[1], TX);
+  }
   __syncthreads();
-  cluster.sync();   // every CTA of the cluster is running before the first push
+  cluster.sync();   // every CTA's mbarriers are armed before the first message
+  bool broken = false;   // a wait gave up: no further waits (the result is flagged)
 
   // Reduce the per-thread candidates (rows ci already complete) to the CTA's
   // first-max; keep its row and row jn locally, push |a| and row to all.
@@ -525,16 +539,28 @@ __global__ void __launch_bounds__(CT)
     warp_argmax(best, bi);
     return best >= K(0) ? bi : -1;
   };
+  // Send column jn's candidate record (row ci, then {key, ci}) to every CTA,
+  // and row jn if this CTA owns it: 16-byte st.async stores, a few per
+  // thread.  Called after a CTA barrier that follows every write to those
+  // rows.
   auto push = [&](K best, int ci, int jn) {
     const int par = jn & 1;
-    if (ci >= 0 && tid < nvj)
-      reinterpret_cast<V *>(slot.crow[par])[tid] = reinterpret_cast<const V *>(&AT(ci, 0))[tid];
-    if (jn >= r0 && jn < r1 && tid >= 64 && tid - 64 < nvj)
-      reinterpret_cast<V *>(slot.jrow[par])[tid - 64] = reinterpret_cast<const V *>(&AT(jn, 0))[tid - 64];
-    if (tid < CN) {
-      ClusterSlots<T> *rs = cluster.map_shared_rank(&slot, tid);
-      rs->cval[par][me] = best;
-      rs->cidx[par][me] = ci;
+    const unsigned lbar = smem_u32(&rbar[par]);
+    const bool own_j = (jn >= r0 && jn < r1);
+    const int per = nvj + 1;
+    for (int e = tid; e < CN * per; e += CT) {
+      const int d = e / per, q = e - d * per;
+      const unsigned db = cluster_map(lbar, d);
+      uint4 v;
+      if (q == nvj) {
+        const unsigned long long kb = (unsigned long long)(long long)best;
+        v = make_uint4((unsigned)kb, (unsigned)(kb >> 32), (unsigned)ci, 0u);
+      } else {
+        v = ci >= 0 ? reinterpret_cast<const uint4 *>(&AT(ci, 0))[q] : make_uint4(0u, 0u, 0u, 0u);
+        if (own_j)
+          st_async16(cluster_map(smem_u32(&recv[par].jrow[q]), d), reinterpret_cast<const uint4 *>(&AT(jn, 0))[q], db);
+      }
+      st_async16(cluster_map(smem_u32(&recv[par].row[me][q]), d), v, db);
     }
   };
 
@@ -551,12 +577,25 @@ __global__ void __launch_bounds__(CT)
 
   for (int j = 0; j < jb; ++j) {
     const int par = j & 1;
-    if (j == 0) cluster.sync();
-    else cluster.barrier_wait();
-    // ---- global winner, computed by every warp from its own CTA's slots ----
+    if (!broken) {                     // column j has arrived from every CTA
+      // a column's exchange takes microseconds: give up after 2 s
+      const bool ok = mbar_wait_for(&rbar[par], (unsigned)(j >> 1) & 1u, 2000000000ull);
+      if (!ok) {
+        broken = true;
+        atomicOr(&g_lu_status, kErrMbarTimeout);
+      } else if (tid == 0 && j + 2 < jb) {
+        mbar_arrive_expect_tx(&rbar[par], TX);           // armed for column j+2
+      }
+    }
+    // ---- global winner, computed by every warp from its own CTA's copies ----
     K v = K(-1);
     int b = 0x7fffffff, idx = -1;
-    if (lane < CN) { v = slot.cval[par][lane]; idx = slot.cidx[par][lane]; b = lane; }
+    if (lane < CN) {
+      const uint4 r = recv[par].row[lane][nvj];
+      v = (K)(long long)(((unsigned long long)r.y << 32) | r.x);
+      idx = (int)r.z;
+      b = lane;
+    }
     warp_winner(v, b, idx);
     const bool zero = !(b < CN && v > K(0));
     const int p = zero ? j : idx;
@@ -568,12 +607,14 @@ __global__ void __launch_bounds__(CT)
     K best = K(-1);
     int bi = 0x7fffffff;
     if (!zero) {
-      // the winner's row and row j, pulled once per CTA
+      // the winner's row and row j, copied from the receive area (which the
+      // senders reuse for column j+2 once this CTA has sent column j+1)
       T *Ps = Pb[par];
       T *Js = Jb[par];
       if (tid < 2 * NV) {
         if (tid < NV) {
-          const V pvec = reinterpret_cast<const V *>(cluster.map_shared_rank(slot.crow[par], b))[tid];
+          const uint4 pu = recv[par].row[b][tid < nvj ? tid : 0];
+          const V pvec = *reinterpret_cast<const V *>(&pu);
           reinterpret_cast<V *>(Ps)[tid] = pvec;
           if (tid == j / VE) {   // once per CTA: FP64 division is costly
             const T *pe = reinterpret_cast<const T *>(&pvec);
@@ -584,9 +625,10 @@ __global__ void __launch_bounds__(CT)
             s_rcp[par] = T(1) / pj;
             s_use_rcp[par] = (pj < T(0) ? -pj : pj) > Lim<T>::safmin();
           }
-        } else
-          reinterpret_cast<V *>(Js)[tid - NV] =
-              reinterpret_cast<const V *>(cluster.map_shared_rank(slot.jrow[par], j / chunk))[tid - NV];
+        } else {
+          const uint4 ju = recv[par].jrow[tid - NV < nvj ? tid - NV : 0];
+          reinterpret_cast<V *>(Js)[tid - NV] = *reinterpret_cast<const V *>(&ju);
+        }
       }
       __syncthreads();   // also: every thread is done with the previous column's phase 2
       const T pv = Ps[j];
@@ -652,8 +694,7 @@ __global__ void __launch_bounds__(CT)
         }
         __syncthreads();
         push(ci >= 0 ? PivKey<T>::key(AT(ci, j + 1)) : K(-1), ci, j + 1);
-        cluster.barrier_arrive();
-        // phase 2 (overlaps the barrier): columns j+2.. of the other rows
+        // phase 2 (overlaps the exchange): columns j+2.. of the other rows
         if (j + 2 < jb) {
           for (int i = lo + tid; i < r1; i += CT) {
             if (i == j || i == p || i == ci || i == j + 1) continue;
@@ -671,11 +712,12 @@ __global__ void __launch_bounds__(CT)
       const int ci = publish(best, bi, j + 1);
       __syncthreads();
       push(ci >= 0 ? PivKey<T>::key(AT(ci, j + 1)) : K(-1), ci, j + 1);
-      cluster.barrier_arrive();
     }
     if (last) break;
   }
-  cluster.sync();   // no CTA leaves while another may still read or push to it
+  // every message to this CTA has arrived (the last column's wait); the
+  // cluster barrier keeps all CTAs resident until that holds for each
+  cluster.sync();
   if (me == 0)
     for (int t = tid; t < jb; t += CT) ipiv[t] = koff + piv_local[t];
   // warp 0 of the last CTA reduces the interchanges while its other warps
@@ -1308,43 +1350,58 @@ static void trailing_update(bool tc, int m, int n, int jb, const T *L21, const T
 }
 
 // Largest cluster (16, else 8 CTAs) the panel kernel can be launched with at
-// the full shared-memory size; 0 when clusters are unavailable.
-constexpr size_t kClusterSmemMax = 220 * 1024;
+// its full shared-memory size (the device's opt-in maximum per block less the
+// kernel's static shared memory -- the receive areas of the exchange); size 0
+// when clusters are unavailable.
+struct ClusterCfg {
+  int size = 0;
+  size_t smem = 0;   // dynamic shared memory per CTA: the rows of the panel
+};
 static bool g_panel_cluster = true;
 
 template <typename T>
-static int cluster_panel_size() {
+static const ClusterCfg &cluster_cfg() {
   static std::once_flag once;
-  static int size = 0;
+  static ClusterCfg cfg;
   std::call_once(once, [] {
     auto k = panel_cluster_kernel<T>;
+    cudaFuncAttributes fa;
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, (const void *)k) != cudaSuccess || (size_t)optin <= fa.sharedSizeBytes + 1024) {
+      (void)cudaGetLastError();
+      return;
+    }
+    const size_t smax = ((size_t)optin - fa.sharedSizeBytes) & ~size_t(1023);
     if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kClusterSmemMax) != cudaSuccess) {
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax) != cudaSuccess) {
       (void)cudaGetLastError();
       return;
     }
     const int sizes[2] = {16, 8};
     for (int q = 0; q < 2; ++q) {
-      cudaLaunchConfig_t cfg = {};
+      cudaLaunchConfig_t lc = {};
       cudaLaunchAttribute at[1];
-      cfg.gridDim = dim3(sizes[q]);
-      cfg.blockDim = dim3(CT);
-      cfg.dynamicSmemBytes = kClusterSmemMax;
+      lc.gridDim = dim3(sizes[q]);
+      lc.blockDim = dim3(CT);
+      lc.dynamicSmemBytes = smax;
       at[0].id = cudaLaunchAttributeClusterDimension;
       at[0].val.clusterDim.x = sizes[q];
       at[0].val.clusterDim.y = 1;
       at[0].val.clusterDim.z = 1;
-      cfg.attrs = at;
-      cfg.numAttrs = 1;
+      lc.attrs = at;
+      lc.numAttrs = 1;
       int n = 0;
-      if (cudaOccupancyMaxActiveClusters(&n, (const void *)k, &cfg) == cudaSuccess && n > 0) {
-        size = sizes[q];
+      if (cudaOccupancyMaxActiveClusters(&n, (const void *)k, &lc) == cudaSuccess && n > 0) {
+        cfg.size = sizes[q];
+        cfg.smem = smax;
         break;
       }
       (void)cudaGetLastError();
     }
   });
-  return size;
+  return cfg;
 }
 
 void set_panel_cluster(bool on) { g_panel_cluster = on; }
@@ -1402,10 +1459,11 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
   ATLG_CHECK(cudaFuncSetAttribute(panel_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kPanelSmemMax));
   cudaStream_t side = c.side_stream();
-  cudaEvent_t ev_ready = c.sync_event(0), ev_side = c.sync_event(1), ev_left = c.sync_event(4);
-  bool side_pending = false;
-  bool left_pending = false;   // interchanges of left columns queued on the side stream
-  const int cn = g_panel_cluster ? cluster_panel_size<T>() : 0;
+  cudaEvent_t ev_ready = c.sync_event(0), ev_side = c.sync_event(1), ev_first = c.sync_event(4);
+  bool side_pending = false;    // side-stream work of the last side step not yet waited for
+  bool first_pending = false;   // its first part (the columns of the panel after next)
+  const int cn = g_panel_cluster ? cluster_cfg<T>().size : 0;
+  const size_t cmax = cluster_cfg<T>().smem;
   bool used_cluster = false;
 
   for (int k = 0; k < MN; k += PW) {
@@ -1444,10 +1502,10 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     const size_t ctile = cluster_tile(Mp, jb);
     const int h = jb / 2;
     const size_t htile = cluster_tile(Mp, jb - h);   // the taller half is the left one
-    if (cn && ctile <= kClusterSmemMax) {
+    if (cn && ctile <= cmax) {
       launch_cluster(Ap, Mp, jb, koff, ipk, ctile);
       used_cluster = true;
-    } else if (cn && g_panel_split && h >= 8 && htile <= kClusterSmemMax) {
+    } else if (cn && g_panel_split && h >= 8 && htile <= cmax) {
       T *Ar = A + k + (size_t)(k + h) * lda;          // rows k.. of the right half
       launch_cluster(Ap, Mp, h, koff, ipk, htile);
       apply_perm_kernel<T><<<(jb - h + 31) / 32, 256, 0, st>>>(A, lda, k, perm, 0, k + h, k + jb);
@@ -1481,27 +1539,74 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     }
     const int c_from = k + jb;
     const int nxt = (c_from < MN) ? ((MN - c_from < PW) ? MN - c_from : PW) : 0;
-    // the interchanges touch every other column: the side update must be done
+    const int far0 = c_from + nxt;                     // first column beyond the next panel
+    const int nl = (k + 31) / 32;
+    // A side step splits the work right of the panel: the next panel's
+    // columns (interchanges, block-row solve, update) on the caller's stream,
+    // so panel k+1 starts at once; everything beyond them on the side stream,
+    // which also does the panel after next's columns first and records that,
+    // so step k+1 waits only for those.  The left columns' interchanges (needed
+    // only by the finished factorization) run last on the side stream.
+    const bool side_step = lookahead && c_from < N && k + jb < M && nxt > 0 && far0 < N;
+    if (side_step) {
+      if (first_pending) {                             // the next panel's columns got step k-1's update
+        ATLG_CHECK(cudaStreamWaitEvent(st, ev_first, 0));
+        first_pending = false;
+      }
+      const int m = M - k - jb, ntot = N - c_from;
+      const T *L21 = A + (k + jb) + (size_t)k * lda;
+      const T *U12 = A + k + (size_t)c_from * lda;
+      T *C = A + (k + jb) + (size_t)c_from * lda;
+      const bool use_tc = tc && m >= 256 && ntot >= 128;
+      apply_perm_kernel<T><<<(nxt + 31) / 32, 256, 0, st>>>(A, lda, k, perm, 0, c_from, far0);
+      note_launch();
+      ATLG_CHECK(cudaGetLastError());
+      dev_trsm_llnu_block(A, lda, k, jb, A + k + (size_t)c_from * lda, lda, nxt, st);
+      float *Ap = nullptr, *Bp = nullptr;
+      if (use_tc) {   // two A packings in turn: the side stream may still read the last one
+        Ap = static_cast<float *>(c.buffer(((k / PW) & 1) ? kBufT2 : kBufT0,
+                                           sizeof(float) * tf32x3_packed_floats(m, jb, false)));
+        Bp = static_cast<float *>(c.buffer(kBufT1, sizeof(float) * tf32x3_packed_floats(ntot, jb, true)));
+        dev_sgemm_tf32x3_pack_a(m, jb, (const float *)L21, lda, Ap, st);
+        dev_sgemm_tf32x3_pack_b_rows(jb, nxt, (const float *)U12, lda, Bp, st);
+      }
+      trailing_update<T>(use_tc, m, nxt, jb, L21, U12, C, lda, 0, ntot, Ap, Bp, st);
+      ATLG_CHECK(cudaEventRecord(ev_ready, st));
+      ATLG_CHECK(cudaStreamWaitEvent(side, ev_ready, 0));
+      const int nfar = N - far0;
+      apply_perm_kernel<T><<<(nfar + 31) / 32, 256, 0, side>>>(A, lda, k, perm, 0, far0, N);
+      note_launch();
+      ATLG_CHECK(cudaGetLastError());
+      dev_trsm_llnu_block(A, lda, k, jb, A + k + (size_t)far0 * lda, lda, nfar, side);
+      if (use_tc) {
+        const size_t rstride = (size_t)3 * ((jb + 31) / 32 * 32);   // floats per packed row
+        dev_sgemm_tf32x3_pack_b_rows(jb, nfar, (const float *)U12 + (size_t)nxt * lda, lda,
+                                     Bp + (size_t)nxt * rstride, side);
+      }
+      const int nxt2 = (far0 < MN) ? ((MN - far0 < PW) ? MN - far0 : PW) : 0;
+      const int first = (nxt2 > 0 && nxt2 < nfar) ? nxt2 : nfar;
+      trailing_update<T>(use_tc, m, first, jb, L21, U12, C, lda, nxt, ntot, Ap, Bp, side);
+      ATLG_CHECK(cudaEventRecord(ev_first, side));
+      first_pending = true;
+      if (first < nfar) trailing_update<T>(use_tc, m, nfar - first, jb, L21, U12, C, lda, nxt + first, ntot, Ap, Bp, side);
+      if (nl > 0) {
+        apply_perm_kernel<T><<<nl, 256, 0, side>>>(A, lda, k, perm, k, N, N);
+        note_launch();
+        ATLG_CHECK(cudaGetLastError());
+      }
+      ATLG_CHECK(cudaEventRecord(ev_side, side));
+      side_pending = true;
+      continue;
+    }
+    // otherwise everything on the caller's stream, after all side work
     if (side_pending) {
       ATLG_CHECK(cudaStreamWaitEvent(st, ev_side, 0));
       side_pending = false;
+      first_pending = false;
     }
-    // the columns right of the panel now; those left of it (needed only by
-    // the finished factorization) on the side stream behind this step's side
-    // update, or here when this step has none
-    const bool side_step = lookahead && c_from < N && k + jb < M && nxt > 0 && c_from + nxt < N;
-    const int nl = (k + 31) / 32, nr = (N - c_from + 31) / 32;
-    if (nr > 0) {
-      apply_perm_kernel<T><<<nr, 256, 0, st>>>(A, lda, k, perm, 0, c_from, N);
-      note_launch();
-      ATLG_CHECK(cudaGetLastError());
-    }
-    if (nl > 0 && !side_step) {
-      if (left_pending) {
-        ATLG_CHECK(cudaStreamWaitEvent(st, ev_left, 0));
-        left_pending = false;
-      }
-      apply_perm_kernel<T><<<nl, 256, 0, st>>>(A, lda, k, perm, k, N, N);
+    const int nr = (N - c_from + 31) / 32;
+    if (nl + nr > 0) {
+      apply_perm_kernel<T><<<nl + nr, 256, 0, st>>>(A, lda, k, perm, k, c_from, N);
       note_launch();
       ATLG_CHECK(cudaGetLastError());
     }
@@ -1520,28 +1625,11 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
           dev_sgemm_tf32x3_pack_a(m, jb, (const float *)L21, lda, Ap, st);
           dev_sgemm_tf32x3_pack_b(jb, ntot, (const float *)U12, lda, Bp, st);
         }
-        if (side_step) {
-          trailing_update<T>(use_tc, m, nxt, jb, L21, U12, C, lda, 0, ntot, Ap, Bp, st);
-          ATLG_CHECK(cudaEventRecord(ev_ready, st));
-          ATLG_CHECK(cudaStreamWaitEvent(side, ev_ready, 0));
-          trailing_update<T>(use_tc, m, ntot - nxt, jb, L21, U12, C, lda, nxt, ntot, Ap, Bp, side);
-          ATLG_CHECK(cudaEventRecord(ev_side, side));
-          side_pending = true;
-          if (nl > 0) {
-            apply_perm_kernel<T><<<nl, 256, 0, side>>>(A, lda, k, perm, k, N, N);
-            note_launch();
-            ATLG_CHECK(cudaGetLastError());
-            ATLG_CHECK(cudaEventRecord(ev_left, side));
-            left_pending = true;
-          }
-        } else {
-          trailing_update<T>(use_tc, m, ntot, jb, L21, U12, C, lda, 0, ntot, Ap, Bp, st);
-        }
+        trailing_update<T>(use_tc, m, ntot, jb, L21, U12, C, lda, 0, ntot, Ap, Bp, st);
       }
     }
   }
   if (side_pending) ATLG_CHECK(cudaStreamWaitEvent(st, ev_side, 0));
-  if (left_pending) ATLG_CHECK(cudaStreamWaitEvent(st, ev_left, 0));
 }
 
 void dev_dgetrf(int M, int N, double *A, int lda, int *ipiv, int *info, cudaStream_t st) {

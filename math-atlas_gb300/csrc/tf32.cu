@@ -219,6 +219,14 @@ void dev_sgemm_tf32x3_pack_b(int K, int N, const float *B, int ldb, float *Bp, c
   pack3_kernel<<<grid_for((long)Np * Kp), 256, 0, st>>>(N, K, Np, Kp, B, ldb, 1, 1, Bp);
   note_launch();
 }
+// The same packing for exactly N rows (no padding rows written): a caller
+// that packs one operand in parts, each at its own row offset of Bp.
+void dev_sgemm_tf32x3_pack_b_rows(int K, int N, const float *B, int ldb, float *Bp, cudaStream_t st) {
+  if (N <= 0) return;
+  const int Kp = ceil_to(K, XT_KB);
+  pack3_kernel<<<grid_for((long)N * Kp), 256, 0, st>>>(N, K, N, Kp, B, ldb, 1, 1, Bp);
+  note_launch();
+}
 size_t tf32x3_packed_floats(int rows, int K, bool b_operand) {
   return (size_t)ceil_to(rows, b_operand ? XT_N : XT_M) * 3 * (size_t)ceil_to(K, XT_KB);
 }

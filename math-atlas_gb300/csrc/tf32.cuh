@@ -9,6 +9,7 @@ namespace atlg {
 // hi/lo-split layouts the tensor-core kernel reads.
 void dev_sgemm_tf32x3_pack_a(int M, int K, const float *A, int lda, float *Ap, cudaStream_t st);
 void dev_sgemm_tf32x3_pack_b(int K, int N, const float *B, int ldb, float *Bp, cudaStream_t st);
+void dev_sgemm_tf32x3_pack_b_rows(int K, int N, const float *B, int ldb, float *Bp, cudaStream_t st);
 size_t tf32x3_packed_floats(int rows, int K, bool b_operand);
 // C[M x N] += alpha * A * B from the packings (B columns boff .. boff+N-1 of
 // a packing made for b_rows_total columns).
