@@ -64,6 +64,7 @@ struct XtArgs {
   float alpha;
   float *C;
   int ldc;
+  int bulk_pf;   // C 16-byte aligned with ldc a multiple of 4: columns prefetched as bulk ranges
 };
 
 __device__ __forceinline__ bool xt_wait(uint64_t *bar, unsigned parity, volatile int *abort_flag) {
@@ -150,44 +151,70 @@ __global__ void __launch_bounds__(XT_THREADS, 2)
     const int gm = m0 + row;
     const bool rok = gm < p.M;
     float *crow = p.C + gm;
-    // C is read in batches of 16 independent loads (the first batch before
-    // the accumulator is ready), so the read-modify-write is bandwidth-
-    // rather than latency-bound
-    // the tile's C lines into L2 while the MMAs run (a warp-wide prefetch
-    // covers one 128-byte line of a column): the epilogue's reads then come
-    // from L2 instead of waiting on HBM 16 loads at a time
-    if (rok)
+    // the tile's C into L2 while the MMAs run: the epilogue's reads then
+    // come from L2 instead of waiting on HBM 16 loads at a time.  Aligned C:
+    // each thread one bulk prefetch of one column's rows of the tile; else a
+    // warp-wide prefetch per 128-byte line
+    if (p.bulk_pf) {
+      const int gn = n0 + (warp - 2) * 32 + lane;
+      const int rows = (p.M - m0 < XT_M ? p.M - m0 : XT_M) & ~3;
+      if (gn < p.N && rows > 0)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p.C + m0 + (size_t)gn * p.ldc),
+                     "r"(rows * 4)
+                     : "memory");
+    } else if (rok) {
       for (int j = 0; j < 128; ++j) {
         const int gn = n0 + h * 128 + j;
         if (gn < p.N) prefetch_l2(crow + (size_t)gn * p.ldc);
       }
-    float cv[16];
-    auto load_batch = [&](int cb) {
+    }
+    // a tile inside C on both sides needs no bounds tests
+    const bool inner = (m0 + XT_M <= p.M) && (n0 + XT_N <= p.N);
+    float *cbase = crow + (size_t)(n0 + h * 128) * p.ldc;
+    // C is read in batches of 16 columns, two batches ahead of the one being
+    // finished (the first two before the accumulator is ready), so the
+    // read-modify-write is bandwidth- rather than latency-bound
+    auto load_batch = [&](float (&cv)[16], int cb) {
+      if (inner) {
+        const float *cp = cbase + (size_t)(cb * 16) * p.ldc;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) cv[j] = __ldcs(cp + (size_t)j * p.ldc);
+        return;
+      }
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
         const int gn = n0 + h * 128 + cb * 16 + j;
         cv[j] = (rok && gn < p.N) ? __ldcs(crow + (size_t)gn * p.ldc) : 0.f;
       }
     };
-    load_batch(0);
+    float cv0[16], cv1[16];
+    load_batch(cv0, 0);
+    load_batch(cv1, 1);
     int okw = 1;
     if (lane == 0) okw = xt_wait(acc_full, 0, abort_flag) ? 1 : 0;
     okw = __shfl_sync(0xffffffffu, okw, 0);
     if (okw) {
       tc_fence_after();
-#pragma unroll 1
+#pragma unroll
       for (int cb = 0; cb < 8; ++cb) {
+        float (&cv)[16] = (cb & 1) ? cv1 : cv0;
         uint32_t r[16];
         tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * 128 + cb * 16), r);
         tmem_wait_ld();
         float out[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) out[j] = fmaf(p.alpha, __uint_as_float(r[j]), cv[j]);
-        if (cb + 1 < 8) load_batch(cb + 1);
+        if (cb + 2 < 8) load_batch(cv, cb + 2);
+        if (inner) {
+          float *cp = cbase + (size_t)(cb * 16) * p.ldc;
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int gn = n0 + h * 128 + cb * 16 + j;
-          if (rok && gn < p.N) __stcs(crow + (size_t)gn * p.ldc, out[j]);
+          for (int j = 0; j < 16; ++j) __stcs(cp + (size_t)j * p.ldc, out[j]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int gn = n0 + h * 128 + cb * 16 + j;
+            if (rok && gn < p.N) __stcs(crow + (size_t)gn * p.ldc, out[j]);
+          }
         }
       }
     }
@@ -250,6 +277,7 @@ void dev_sgemm_tf32x3_packed(int M, int N, int K, float alpha, const float *Ap, 
   }
   XtArgs a;
   a.M = M; a.N = N; a.K3 = K3; a.alpha = alpha; a.C = C; a.ldc = ldc;
+  a.bulk_pf = ((reinterpret_cast<uintptr_t>(C) & 15) == 0 && (ldc & 3) == 0) ? 1 : 0;
   ATLG_CHECK(cudaFuncSetAttribute(tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, XT_SMEM));
   tf32x3_kernel<<<dim3(Mp / XT_M, (N + XT_N - 1) / XT_N), XT_THREADS, XT_SMEM, st>>>(tA, tB, a);
   note_launch();

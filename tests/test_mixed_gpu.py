@@ -71,7 +71,8 @@ def test_tf32x3_update_is_fp32_accurate(gb):
     """The mixed solver's factor update (3xTF32 on tcgen05) against an FP64
     product: error at FP32 level, far below single-pass TF32 (~1e-3)."""
     torch = pytest.importorskip("torch")
-    for (M, N, K) in ((1000, 700, 64), (513, 300, 200), (256, 128, 64)):
+    # (384, 512, 96): every tile inside C (the epilogue without bounds tests)
+    for (M, N, K) in ((1000, 700, 64), (513, 300, 200), (256, 128, 64), (384, 512, 96)):
         g = torch.Generator(device="cuda").manual_seed(M + N)
         A = torch.randn(K, M, device="cuda", generator=g)     # column-major M x K storage
         B = torch.randn(N, K, device="cuda", generator=g)     # column-major K x N storage
