@@ -1544,8 +1544,8 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     // A side step splits the work right of the panel: the next panel's
     // columns (interchanges, block-row solve, update) on the caller's stream,
     // so panel k+1 starts at once; everything beyond them on the side stream,
-    // which also does the panel after next's columns first and records that,
-    // so step k+1 waits only for those.  The left columns' interchanges (needed
+    // which (tensor-core updates) does the panel after next's columns first
+    // and records that, so step k+1 waits only for those.  The left columns' interchanges (needed
     // only by the finished factorization) run last on the side stream.
     const bool side_step = lookahead && c_from < N && k + jb < M && nxt > 0 && far0 < N;
     if (side_step) {
@@ -1583,8 +1583,12 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
         dev_sgemm_tf32x3_pack_b_rows(jb, nfar, (const float *)U12 + (size_t)nxt * lda, lda,
                                      Bp + (size_t)nxt * rstride, side);
       }
+      // the panel after next's columns as their own launch only where the
+      // update is fast enough for the panel chain to be the critical path
+      // (tensor-core updates); the FFMA/DFMA update is the critical path
+      // itself, and a split would only add a small, inefficient launch
       const int nxt2 = (far0 < MN) ? ((MN - far0 < PW) ? MN - far0 : PW) : 0;
-      const int first = (nxt2 > 0 && nxt2 < nfar) ? nxt2 : nfar;
+      const int first = (use_tc && nxt2 > 0 && nxt2 < nfar) ? nxt2 : nfar;
       trailing_update<T>(use_tc, m, first, jb, L21, U12, C, lda, nxt, ntot, Ap, Bp, side);
       ATLG_CHECK(cudaEventRecord(ev_first, side));
       first_pending = true;
