@@ -376,18 +376,29 @@ int host_gesv(const char *rout, int Order, int N, int NRHS, T *A, int lda, int *
   if (lda < N || lda < 1) cblas_xerbla(5, rout, "lda must be >= MAX(N,1): lda=%d N=%d\n", lda, N);
   if (ldb < N || ldb < 1) cblas_xerbla(8, rout, "ldb must be >= MAX(N,1): ldb=%d N=%d\n", ldb, N);
   if (N == 0) return 0;
-  T *dA;
-  int ldd_a;
-  int *dpiv;
-  const int info = host_getrf_keep<T>(Order, N, N, A, lda, ipiv, &dA, &ldd_a, &dpiv);
-  if (info == 0 && NRHS > 0) {
-    cudaStream_t st = ctx().stream;
-    int ldd_b;
-    T *dB = to_dev<T>(kBufB, B, N, NRHS, ldb, &ldd_b, st);
-    dev_getrs_any<T>(Order, CblasNoTrans, N, NRHS, dA, ldd_a, dpiv, dB, ldd_b, st);
-    to_host<T>(B, ldb, dB, ldd_b, N, NRHS, st);
-    ATLG_CHECK(cudaStreamSynchronize(st));
-  }
+  // A and B up, the factorization, then at once the solve on the library
+  // stream while the factors, pivots and info go back on a second stream;
+  // the solution is copied back only when info is 0 (a singular A leaves B
+  // as it was, as in the reference; the solve that ran anyway is dropped).
+  Context &c = ctx();
+  cudaStream_t st = c.stream, cs = c.outer_stream();
+  int ldd_a, ldd_b = 0;
+  T *dA = to_dev<T>(kBufA, A, N, N, lda, &ldd_a, st);
+  T *dB = NRHS > 0 ? to_dev<T>(kBufB, B, N, NRHS, ldb, &ldd_b, st) : nullptr;
+  int *dpiv = static_cast<int *>(c.buffer(kBufPiv, sizeof(int) * (size_t)N));
+  int *dinfo = static_cast<int *>(c.buffer(kBufInfo, sizeof(int) * 4));
+  dev_getrf_any<T>(N, N, dA, ldd_a, dpiv, dinfo, st);
+  cudaEvent_t ev = c.sync_event(5);
+  ATLG_CHECK(cudaEventRecord(ev, st));
+  if (NRHS > 0) dev_getrs_any<T>(Order, CblasNoTrans, N, NRHS, dA, ldd_a, dpiv, dB, ldd_b, st);
+  ATLG_CHECK(cudaStreamWaitEvent(cs, ev, 0));
+  int info = 0;
+  ATLG_CHECK(cudaMemcpyAsync(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost, cs));
+  ATLG_CHECK(cudaMemcpyAsync(ipiv, dpiv, sizeof(int) * (size_t)N, cudaMemcpyDeviceToHost, cs));
+  to_host<T>(A, lda, dA, ldd_a, N, N, cs);
+  ATLG_CHECK(cudaStreamSynchronize(cs));
+  if (info == 0 && NRHS > 0) to_host<T>(B, ldb, dB, ldd_b, N, NRHS, st);
+  ATLG_CHECK(cudaStreamSynchronize(st));
   check_status(rout);
   return info;
 }
