@@ -10,12 +10,12 @@
 // mixed-precision solver (mixed.cu) -- the "TF32 via tcgen05" factor.  The
 // reference-semantics clapack_sgetrf keeps the FFMA GEMM of gemm.cu.
 //
-// Kernel: one 128 x 256 tile of C per CTA, 10 warps: warp 0 TMA producer
+// Kernel: one 256 x 128 tile of C per CTA, 10 warps: warp 0 TMA producer
 // (K-major 128-byte-swizzled tiles of A' and B', 32 FP32 per row, 2 x 48 KB
 // stages), warp 1 tensor-memory allocation (256 columns) and MMA issue
-// (K = 8 per instruction), warps 2-9 stream the accumulator out of tensor
-// memory and update C in place (each thread one row, 128 columns; the tile
-// of C is prefetched into L2 while the MMAs run).  Two CTAs fit per SM, so
+// (K = 8 per instruction, two 128-row accumulators), warps 2-9 stream the
+// accumulators out of tensor memory and update C in place (each thread one
+// row, 128 columns; the tile of C is prefetched into L2 while the MMAs run).  Two CTAs fit per SM, so
 // one CTA's epilogue (the C read-modify-write, which bounds the LU update)
 // overlaps the other's MMAs.  All waits are bounded.
 #include "common.cuh"
@@ -27,7 +27,12 @@ namespace atlg {
 
 __device__ unsigned g_tf32_status;
 
-constexpr int XT_M = 128, XT_N = 256, XT_KB = 32;       // 32 FP32 = one 128-byte swizzle row
+// A CTA's tile of C is 256 rows x 128 columns, two 128 x 128 accumulators in
+// tensor memory (rows 0-127 in columns 0-127, rows 128-255 in 128-255): each
+// column of the tile is 1 KB of contiguous C, the unit the read-modify-write
+// moves (a 128 x 256 tile gave 512-byte pieces).
+constexpr int XT_M = 256, XT_MM = 128, XT_N = 128, XT_KB = 32;   // 32 FP32 = one 128-byte swizzle row
+constexpr int XT_TMEM = 2 * XT_N;                                 // tensor-memory columns
 constexpr int XT_STAGES = 2;
 constexpr int XT_STAGE_BYTES = (XT_M + XT_N) * XT_KB * 4;   // 48 KB
 constexpr int XT_EPI_WARPS = 8;
@@ -98,7 +103,7 @@ __global__ void __launch_bounds__(XT_THREADS, 2)
     *abort_flag = 0;
     fence_mbar_init();
   }
-  if (warp == 1) tmem_alloc(tmem_slot, XT_N);
+  if (warp == 1) tmem_alloc(tmem_slot, XT_TMEM);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -124,30 +129,38 @@ __global__ void __launch_bounds__(XT_THREADS, 2)
     if (lane == 0) {
       // kind::tf32: D = F32 (bits 4-5 = 1), A = B = TF32 (2 at bits 7-9 and 10-12), K-major
       const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(XT_N >> 3) << 17) |
-                             ((uint32_t)(XT_M >> 4) << 24);
+                             ((uint32_t)(XT_MM >> 4) << 24);
       for (int kb = 0; kb < nkb; ++kb) {
         const int st = kb % XT_STAGES;
         if (!xt_wait(&full[st], (unsigned)((kb / XT_STAGES) & 1), abort_flag)) break;
         tc_fence_after();
         const uint32_t sa = smem_u32(base + st * XT_STAGE_BYTES);
-        const uint64_t da = sw128_kmajor_desc(sa);
+        const uint64_t da = sw128_kmajor_desc(sa);                             // rows 0-127
+        const uint64_t da1 = sw128_kmajor_desc(sa + XT_MM * XT_KB * 4);        // rows 128-255
         const uint64_t db = sw128_kmajor_desc(sa + XT_M * XT_KB * 4);
 #pragma unroll
-        for (int kk = 0; kk < XT_KB / 8; ++kk)   // K = 8 per MMA: 32 bytes along the swizzled row
+        for (int kk = 0; kk < XT_KB / 8; ++kk) {   // K = 8 per MMA: 32 bytes along the swizzled row
           asm volatile(
               "{\n .reg .pred q;\n setp.ne.b32 q, %4, 0;\n"
               " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, q;\n}\n" ::"r"(tmem),
               "l"(da + (uint64_t)(2 * kk)), "l"(db + (uint64_t)(2 * kk)), "r"(idesc),
               "r"((kb > 0 || kk > 0) ? 1u : 0u)
               : "memory");
+          asm volatile(
+              "{\n .reg .pred q;\n setp.ne.b32 q, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, q;\n}\n" ::"r"(tmem + (uint32_t)XT_N),
+              "l"(da1 + (uint64_t)(2 * kk)), "l"(db + (uint64_t)(2 * kk)), "r"(idesc),
+              "r"((kb > 0 || kk > 0) ? 1u : 0u)
+              : "memory");
+        }
         mma_commit(&empty[st]);
       }
       mma_commit(acc_full);   // arrives once every MMA issued above has completed
     }
   } else {
     const int q = warp & 3;
-    const int h = (warp - 2) >> 2;            // which 128-column half
-    const int row = q * 32 + lane;
+    const int h = (warp - 2) >> 2;            // which accumulator: rows h*128 .. h*128+127 of the tile
+    const int row = h * XT_MM + q * 32 + lane;
     const int gm = m0 + row;
     const bool rok = gm < p.M;
     float *crow = p.C + gm;
@@ -156,21 +169,22 @@ __global__ void __launch_bounds__(XT_THREADS, 2)
     // each thread one bulk prefetch of one column's rows of the tile; else a
     // warp-wide prefetch per 128-byte line
     if (p.bulk_pf) {
-      const int gn = n0 + (warp - 2) * 32 + lane;
+      const int t = (warp - 2) * 32 + lane;   // warps 2-5: one column each
+      const int gn = n0 + t;
       const int rows = (p.M - m0 < XT_M ? p.M - m0 : XT_M) & ~3;
-      if (gn < p.N && rows > 0)
+      if (t < XT_N && gn < p.N && rows > 0)
         asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p.C + m0 + (size_t)gn * p.ldc),
                      "r"(rows * 4)
                      : "memory");
     } else if (rok) {
-      for (int j = 0; j < 128; ++j) {
-        const int gn = n0 + h * 128 + j;
+      for (int j = 0; j < XT_N; ++j) {
+        const int gn = n0 + j;
         if (gn < p.N) prefetch_l2(crow + (size_t)gn * p.ldc);
       }
     }
     // a tile inside C on both sides needs no bounds tests
     const bool inner = (m0 + XT_M <= p.M) && (n0 + XT_N <= p.N);
-    float *cbase = crow + (size_t)(n0 + h * 128) * p.ldc;
+    float *cbase = crow + (size_t)n0 * p.ldc;
     // C is read in batches of 16 columns, two batches ahead of the one being
     // finished (the first two before the accumulator is ready), so the
     // read-modify-write is bandwidth- rather than latency-bound
@@ -183,7 +197,7 @@ __global__ void __launch_bounds__(XT_THREADS, 2)
       }
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
-        const int gn = n0 + h * 128 + cb * 16 + j;
+        const int gn = n0 + cb * 16 + j;
         cv[j] = (rok && gn < p.N) ? __ldcs(crow + (size_t)gn * p.ldc) : 0.f;
       }
     };
@@ -212,7 +226,7 @@ __global__ void __launch_bounds__(XT_THREADS, 2)
         } else {
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
-            const int gn = n0 + h * 128 + cb * 16 + j;
+            const int gn = n0 + cb * 16 + j;
             if (rok && gn < p.N) __stcs(crow + (size_t)gn * p.ldc, out[j]);
           }
         }
@@ -224,7 +238,7 @@ __global__ void __launch_bounds__(XT_THREADS, 2)
   if (warp == 1) {
     __syncwarp();
     tc_fence_after();
-    tmem_dealloc(tmem, XT_N);
+    tmem_dealloc(tmem, XT_TMEM);
   }
 }
 
