@@ -269,6 +269,13 @@ void atlg_panel_cluster(int on);
  * right half), 0 on the cooperative-grid kernel; factors agree to rounding,
  * pivots are the same partial-pivoting choices */
 void atlg_panel_split(int on);
+/* the mixed solver's FP32 factor (no reference counterpart): while at least
+ * `rows` rows lie at and below a step's panel, every other step's trailing
+ * update of the columns beyond the next panel is deferred into the next
+ * step's, which then updates them with rank 2 x 64 (one pass over the
+ * trailing matrix for two panels); default 12288, 0 never defers, negative
+ * restores the default.  Factors agree to rounding */
+void atlg_lu_defer_rows(int rows);
 /* refinement solves of dgesv_mixed with one right-hand side (no reference
  * counterpart): 1 (default) the chained TRSV over 128-row blocks with block
  * inverses formed once per factorization, 0 the 64-row look-back TRSV; both
@@ -284,6 +291,10 @@ void atlg_panel_width(int w);
 /* column-major LU; info written to device memory */
 int atlg_dgetrf_dev(int M, int N, double *A, int lda, int *ipiv, int *info, void *stream);
 int atlg_sgetrf_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void *stream);
+/* the mixed solver's FP32 factorization (no reference counterpart): the same
+ * LU with partial pivoting, trailing updates on the tensor cores in 3xTF32
+ * (FP32-level accuracy); pivots follow the FP32 values it computes */
+int atlg_sgetrf_tc_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void *stream);
 /* the split-DGEMM LU on device data (0-based device pivots), nslices 1..8,
  * outer block nb (rounded down to a multiple of 256; 1024 in dgesv_split);
  * returns info; synchronizes once per outer block */

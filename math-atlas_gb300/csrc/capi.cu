@@ -1198,6 +1198,7 @@ int atlg_isamax_dev(int N, const float *X, int incX, int *result, void *stream) 
 }
 void atlg_panel_cluster(int on) { set_panel_cluster(on != 0); }
 void atlg_panel_split(int on) { set_panel_split(on != 0); }
+void atlg_lu_defer_rows(int rows) { set_defer_rows(rows); }
 void atlg_refine_trsv(int chained) { set_refine_trsv_chained(chained != 0); }
 void atlg_panel_grid(int ctas) { set_panel_grid(ctas); }
 void atlg_split_lu_leaf(int nb) { set_split_lu_leaf(nb); }
@@ -1210,6 +1211,11 @@ int atlg_dgetrf_dev(int M, int N, double *A, int lda, int *ipiv, int *info, void
 int atlg_sgetrf_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void *stream) {
   if (M < 0 || N < 0 || lda < (M > 1 ? M : 1)) return -1;
   dev_sgetrf(M, N, A, lda, ipiv, info, stream_of(stream));
+  return 0;
+}
+int atlg_sgetrf_tc_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void *stream) {
+  if (M < 0 || N < 0 || lda < (M > 1 ? M : 1)) return -1;
+  dev_sgetrf_tc(M, N, A, lda, ipiv, info, stream_of(stream));
   return 0;
 }
 int atlg_dgesv_mixed_dev(int N, int NRHS, double *A, int lda, int *ipiv, const double *B, int ldb, double *X,

@@ -149,6 +149,13 @@ __device__ __forceinline__ void prefetch_l2(const void *p) {
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap *map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
+// x rounded to TF32 (10 mantissa bits), to nearest with ties away from zero:
+// the high part of the 3xTF32 split (the low part is x minus it, exact).
+__device__ __forceinline__ float tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
 // *p += v in L2 (round to nearest), no value returned: the issuing thread
 // does not wait for it.
 __device__ __forceinline__ void red_add_f64(double *p, double v) { (void)atomicAdd(p, v); }

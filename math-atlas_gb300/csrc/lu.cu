@@ -26,6 +26,7 @@
 // pivot search are within rounding of each other; the factors agree to
 // rounding (different but equally stable summation order).
 #include <float.h>
+#include <limits.h>
 
 #include <cooperative_groups.h>
 #include <mutex>
@@ -785,6 +786,170 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The block row of step k of the FP32 factorization for the columns
+// [c0, c0 + ncols), in one launch: the panel's interchanges (record perm,
+// rows relative to k), the solve with the panel's unit-lower jb x jb block
+// (A(k.., k..)), and, when Bp is given, the solved rows packed as the 3xTF32
+// B operand (row c of Bp is column c0 + c: TF32 high part, low part, high
+// part, each kp floats, zero beyond the rows).  It replaces an interchange
+// launch, a solve launch and a packing launch on the path between two panels.
+// With jp = NB the previous panel's trailing update of these columns is
+// still pending (the factorization pairs two steps into one update of rank
+// 2 NB): the block rows first take x_i -= sum_j Lp(i, j) * u_j, u = the
+// previous block row's solution (rows k-jp.. of the column), Lp = that
+// panel's L at the block rows (A(k.., k-jp..), already interchanged), and
+// the packing holds u then the solution (rank jp + jb).
+// The record lists the jb block rows first (dst[t] = t for t < jb, as
+// reduce_interchanges writes it), then the rows below that receive other
+// contents.  Each CTA owns whole columns and reads every source of a column
+// before it writes any destination.  A warp owns four columns; in the solve
+// lane l holds rows l and l + 32 of each, and row i takes
+// x_i -= L(i, j) * x_j for j = 0, 1, ... in turn (the order of the
+// one-thread-per-column solve, so the results are the same).
+constexpr int kBrCols = 32, kBrWarps = 8, kBrCpw = kBrCols / kBrWarps;
+
+__global__ void __launch_bounds__(kBrWarps * 32)
+    blockrow_kernel(float *__restrict__ A, int lda, int k, int jb, const int *__restrict__ perm, int c0, int ncols,
+                    float *__restrict__ Bp, int kp, int jp) {
+  extern __shared__ float br_dyn[];
+  float *tri = br_dyn;                            // tri[j * NB + i] = L(i, j) for j < i < jb
+  float *lp = br_dyn + NB * NB;                   // lp[j * NB + i] = Lp(i, j) (jp > 0 only)
+  __shared__ float xs[kBrCols][NB + 1];           // new rows k..k+jb-1, one column per row of xs
+  __shared__ float bl[NB][kBrCols + 1];           // record entries jb.. (rows below the block)
+  __shared__ int dst[2 * NB], src[2 * NB];
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int n = perm[0];
+  const int cb = c0 + blockIdx.x * kBrCols;
+  const int nc = (c0 + ncols - cb < kBrCols) ? c0 + ncols - cb : kBrCols;
+  for (int e = t; e < n; e += kBrWarps * 32) {
+    dst[e] = perm[1 + e];
+    src[e] = perm[1 + 2 * NB + e];
+  }
+  for (int e = t; e < NB * NB; e += kBrWarps * 32) {
+    const int i = e & (NB - 1), j = e / NB;
+    tri[e] = (j < i && i < jb) ? A[k + i + (size_t)(k + j) * lda] : 0.f;
+    if (jp) lp[e] = (i < jb) ? A[k + i + (size_t)(k - jp + j) * lda] : 0.f;
+  }
+  __syncthreads();
+  // gather: every load of the warp's columns issued before the first store
+  float v[kBrCpw][4];
+#pragma unroll
+  for (int cc = 0; cc < kBrCpw; ++cc) {
+    const int c = warp + kBrWarps * cc;
+    const float *col = A + k + (size_t)(cb + c) * lda;
+#pragma unroll
+    for (int qq = 0; qq < 4; ++qq) {
+      const int q = lane + 32 * qq;
+      v[cc][qq] = (c < nc && q < n) ? col[src[q]] : 0.f;
+    }
+  }
+#pragma unroll
+  for (int cc = 0; cc < kBrCpw; ++cc) {
+    const int c = warp + kBrWarps * cc;
+#pragma unroll
+    for (int qq = 0; qq < 4; ++qq) {
+      const int q = lane + 32 * qq;
+      if (q < jb) xs[c][dst[q]] = v[cc][qq];
+      else if (q < n) bl[q - jb][c] = v[cc][qq];
+    }
+  }
+  __syncthreads();
+  // rows below the block, then the solve of the warp's own columns
+#pragma unroll
+  for (int cc = 0; cc < kBrCpw; ++cc) {
+    const int c = warp + kBrWarps * cc;
+    if (c < nc) {
+      float *col = A + k + (size_t)(cb + c) * lda;
+#pragma unroll
+      for (int qq = 0; qq < 4; ++qq) {
+        const int q = jb + lane + 32 * qq;
+        if (q < n && dst[q] != src[q]) col[dst[q]] = bl[q - jb][c];
+      }
+    }
+  }
+  float x[kBrCpw][2], u[kBrCpw][2];
+#pragma unroll
+  for (int cc = 0; cc < kBrCpw; ++cc) {
+    const int c = warp + kBrWarps * cc;
+    x[cc][0] = (lane < jb) ? xs[c][lane] : 0.f;
+    x[cc][1] = (lane + 32 < jb) ? xs[c][lane + 32] : 0.f;
+    const float *col = A + k + (size_t)(cb + (c < nc ? c : 0)) * lda;
+    u[cc][0] = (jp && lane < jp) ? col[lane - jp] : 0.f;
+    u[cc][1] = (jp && lane + 32 < jp) ? col[lane + 32 - jp] : 0.f;
+  }
+  for (int j = 0; j < jp; ++j) {
+    const int hi = j >> 5;
+    float uj[kBrCpw];
+#pragma unroll
+    for (int cc = 0; cc < kBrCpw; ++cc) uj[cc] = __shfl_sync(0xffffffffu, hi ? u[cc][1] : u[cc][0], j & 31);
+#pragma unroll
+    for (int s2 = 0; s2 < 2; ++s2) {
+      const float l = lp[j * NB + lane + 32 * s2];
+#pragma unroll
+      for (int cc = 0; cc < kBrCpw; ++cc) x[cc][s2] = fmaf(-l, uj[cc], x[cc][s2]);
+    }
+  }
+  for (int j = 0; j < jb - 1; ++j) {
+    const int hi = j >> 5;
+    float xj[kBrCpw];
+#pragma unroll
+    for (int cc = 0; cc < kBrCpw; ++cc) xj[cc] = __shfl_sync(0xffffffffu, hi ? x[cc][1] : x[cc][0], j & 31);
+#pragma unroll
+    for (int s2 = 0; s2 < 2; ++s2) {
+      const int i = lane + 32 * s2;
+      if (i > j) {
+        const float l = tri[j * NB + i];
+#pragma unroll
+        for (int cc = 0; cc < kBrCpw; ++cc) x[cc][s2] = fmaf(-l, xj[cc], x[cc][s2]);
+      }
+    }
+  }
+#pragma unroll
+  for (int cc = 0; cc < kBrCpw; ++cc) {
+    const int c = warp + kBrWarps * cc;
+    if (c >= nc) continue;
+    float *col = A + k + (size_t)(cb + c) * lda;
+#pragma unroll
+    for (int s2 = 0; s2 < 2; ++s2) {
+      const int i = lane + 32 * s2;
+      if (i < jb) col[i] = x[cc][s2];
+    }
+    if (Bp) {
+      // packed row: u (jp values, 0 or NB), then the solution (jb values)
+      float *out = Bp + (size_t)(blockIdx.x * kBrCols + c) * 3 * kp;
+      float val[4] = {jp ? u[cc][0] : x[cc][0], jp ? u[cc][1] : x[cc][1], jp ? x[cc][0] : 0.f,
+                      jp ? x[cc][1] : 0.f};
+#pragma unroll
+      for (int sl = 0; sl < 4; ++sl) {
+        const int i = lane + 32 * sl;
+        if (i < kp) {
+          const float xv = i < jp + jb ? val[sl] : 0.f;
+          const float h = tf32_rna(xv);
+          out[i] = h;
+          out[kp + i] = xv - h;
+          out[2 * kp + i] = h;
+        }
+      }
+    }
+  }
+}
+
+static void blockrow_f32(float *A, int lda, int k, int jb, const int *perm, int c0, int ncols, float *Bp, int jp,
+                         cudaStream_t st) {
+  if (ncols <= 0) return;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    ATLG_CHECK(cudaFuncSetAttribute(blockrow_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(sizeof(float) * 2 * NB * NB)));
+  });
+  const int kp = (jp + jb + 31) / 32 * 32;
+  const size_t smem = sizeof(float) * (jp ? 2 : 1) * NB * NB;
+  blockrow_kernel<<<(ncols + kBrCols - 1) / kBrCols, kBrWarps * 32, smem, st>>>(A, lda, k, jb, perm, c0, ncols, Bp,
+                                                                               kp, jp);
+  note_launch();
+  ATLG_CHECK(cudaGetLastError());
+}
+
 // laswp as one permutation: laswp_perm_kernel runs the interchange sequence
 // K1..K2-1 (reversed when inci < 0) on a row-content table held in shared
 // memory (global memory above kPermSmemRows rows), then the rows are moved
@@ -1349,6 +1514,25 @@ static void trailing_update(bool tc, int m, int n, int jb, const T *L21, const T
   gemm_any<T>(m, n, jb, L21, lda, U12 + (size_t)boff * lda, lda, C + (size_t)boff * lda, lda, st);
 }
 
+// The block row of step k (rows k..k+jb-1) for columns [c0, c0+n): the
+// panel's interchanges and the unit-lower solve; FP32 in one launch that
+// also packs the 3xTF32 B operand when Bp is given.
+// jp = NB: the previous panel's update of these columns is pending (FP32
+// tensor-core factorization only; blockrow_kernel).
+template <typename T>
+static void block_row(T *A, int lda, int k, int jb, const int *perm, int c0, int n, float *Bp, int jp,
+                      cudaStream_t st) {
+  if (n <= 0) return;
+  if constexpr (sizeof(T) == 4) {
+    blockrow_f32(A, lda, k, jb, perm, c0, n, Bp, jp, st);
+  } else {
+    apply_perm_kernel<T><<<(n + 31) / 32, 256, 0, st>>>(A, lda, k, perm, 0, c0, c0 + n);
+    note_launch();
+    ATLG_CHECK(cudaGetLastError());
+    dev_trsm_llnu_block(A, lda, k, jb, A + k + (size_t)c0 * lda, lda, n, st);
+  }
+}
+
 // Largest cluster (16, else 8 CTAs) the panel kernel can be launched with at
 // its full shared-memory size (the device's opt-in maximum per block less the
 // kernel's static shared memory -- the receive areas of the exchange); size 0
@@ -1411,6 +1595,12 @@ void set_panel_cluster(bool on) { g_panel_cluster = on; }
 // the cooperative grid: the cluster's per-column exchange is the faster one.
 static bool g_panel_split = true;
 void set_panel_split(bool on) { g_panel_split = on; }
+// Below ~12k rows the panel chain, not the update, is the critical path, and
+// a paired step only lengthens it (n = 16384: 12288 measured best of 4096 to
+// 12288 in steps of 2048).
+constexpr int kDeferRowsDefault = 12288;
+static int g_defer_rows = kDeferRowsDefault;
+void set_defer_rows(int rows) { g_defer_rows = rows < 0 ? kDeferRowsDefault : rows > 0 ? rows : INT_MAX; }
 static int g_panel_grid = 0;   // CTAs of the grid panel; 0: the default below
 void set_panel_grid(int ctas) { g_panel_grid = ctas > 0 ? ctas : 0; }
 // Panel width of the FP64 LU (8..NB, a multiple of 8).  A panel's own
@@ -1465,6 +1655,27 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
   const int cn = g_panel_cluster ? cluster_cfg<T>().size : 0;
   const size_t cmax = cluster_cfg<T>().smem;
   bool used_cluster = false;
+  // A side step of the tensor-core factorization whose trailing matrix is
+  // tall defers its far update into the next step's: one update of rank 2 PW
+  // reads and writes C once for two panels (the C read-modify-write bounds
+  // that update).  The next panel's columns still get this step's update at
+  // once.  pend = the rank (0 or PW) owed by the previous step.
+  auto side_step_at = [&](int kk) {
+    const int jbk = (MN - kk < PW) ? MN - kk : PW;
+    const int cf = kk + jbk;
+    const int nx = (cf < MN) ? ((MN - cf < PW) ? MN - cf : PW) : 0;
+    return lookahead && cf < N && kk + jbk < M && nx > 0 && cf + nx < N;
+  };
+  auto tc_at = [&](int kk) {
+    const int jbk = (MN - kk < PW) ? MN - kk : PW;
+    return tc && M - kk - jbk >= 256 && N - kk - jbk >= 128;
+  };
+  int pend = 0;
+  if (tc && lookahead) {   // the packings at their largest (rank 2 PW) once, before any side-stream use
+    c.buffer(kBufT0, sizeof(float) * tf32x3_packed_floats(M, 2 * PW, false));
+    c.buffer(kBufT2, sizeof(float) * tf32x3_packed_floats(M, 2 * PW, false));
+    c.buffer(kBufT1, sizeof(float) * tf32x3_packed_floats(N, 2 * PW, true));
+  }
 
   for (int k = 0; k < MN; k += PW) {
     const int jb = (MN - k < PW) ? MN - k : PW;
@@ -1508,13 +1719,12 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     } else if (cn && g_panel_split && h >= 8 && htile <= cmax) {
       T *Ar = A + k + (size_t)(k + h) * lda;          // rows k.. of the right half
       launch_cluster(Ap, Mp, h, koff, ipk, htile);
-      apply_perm_kernel<T><<<(jb - h + 31) / 32, 256, 0, st>>>(A, lda, k, perm, 0, k + h, k + jb);
-      dev_trsm_llnu_block(A, lda, k, h, Ar, lda, jb - h, st);
+      block_row<T>(A, lda, k, h, perm, k + h, jb - h, nullptr, 0, st);
       gemm_any<T>(Mp - h, jb - h, h, Ap + h, lda, Ar, lda, Ar + h, lda, st);
       launch_cluster(Ar + h, Mp - h, jb - h, koff + h, ipk + h, cluster_tile(Mp - h, jb - h));
       apply_perm_kernel<T><<<(h + 31) / 32, 256, 0, st>>>(A, lda, k + h, perm, 0, k, k + h);
       panel_perm_kernel<<<1, 32, 0, st>>>(ipk, jb, koff, perm);
-      note_launch(4);   // with the one below: two panels, two interchanges, the record
+      note_launch(3);   // with the one below: two panels, the left half's interchanges, the record
       ATLG_CHECK(cudaGetLastError());
       used_cluster = true;
     } else {
@@ -1554,52 +1764,58 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
         first_pending = false;
       }
       const int m = M - k - jb, ntot = N - c_from;
-      const T *L21 = A + (k + jb) + (size_t)k * lda;
-      const T *U12 = A + k + (size_t)c_from * lda;
-      T *C = A + (k + jb) + (size_t)c_from * lda;
       const bool use_tc = tc && m >= 256 && ntot >= 128;
-      apply_perm_kernel<T><<<(nxt + 31) / 32, 256, 0, st>>>(A, lda, k, perm, 0, c_from, far0);
-      note_launch();
-      ATLG_CHECK(cudaGetLastError());
-      dev_trsm_llnu_block(A, lda, k, jb, A + k + (size_t)c_from * lda, lda, nxt, st);
+      const bool defer = pend == 0 && use_tc && jb == PW && M - k >= g_defer_rows && side_step_at(k + PW) &&
+                         tc_at(k + PW);
+      const int kq = k - pend;                          // this step's update: L columns kq..k+jb-1
+      const int rk = pend + jb;                         // its rank
+      const T *L21 = A + (k + jb) + (size_t)kq * lda;
+      const T *U12 = A + kq + (size_t)c_from * lda;
+      T *C = A + (k + jb) + (size_t)c_from * lda;
+      if (pend) {   // the deferred panel's L rows take this step's interchanges before they are used
+        apply_perm_kernel<T><<<(pend + 31) / 32, 256, 0, st>>>(A, lda, k, perm, 0, kq, k);
+        note_launch();
+        ATLG_CHECK(cudaGetLastError());
+      }
       float *Ap = nullptr, *Bp = nullptr;
       if (use_tc) {   // two A packings in turn: the side stream may still read the last one
         Ap = static_cast<float *>(c.buffer(((k / PW) & 1) ? kBufT2 : kBufT0,
-                                           sizeof(float) * tf32x3_packed_floats(m, jb, false)));
-        Bp = static_cast<float *>(c.buffer(kBufT1, sizeof(float) * tf32x3_packed_floats(ntot, jb, true)));
-        dev_sgemm_tf32x3_pack_a(m, jb, (const float *)L21, lda, Ap, st);
-        dev_sgemm_tf32x3_pack_b_rows(jb, nxt, (const float *)U12, lda, Bp, st);
+                                           sizeof(float) * tf32x3_packed_floats(m, rk, false)));
+        Bp = static_cast<float *>(c.buffer(kBufT1, sizeof(float) * tf32x3_packed_floats(ntot, rk, true)));
       }
-      trailing_update<T>(use_tc, m, nxt, jb, L21, U12, C, lda, 0, ntot, Ap, Bp, st);
+      block_row<T>(A, lda, k, jb, perm, c_from, nxt, Bp, pend, st);
+      if (use_tc) dev_sgemm_tf32x3_pack_a(m, rk, (const float *)L21, lda, Ap, st);
+      trailing_update<T>(use_tc, m, nxt, rk, L21, U12, C, lda, 0, ntot, Ap, Bp, st);
       ATLG_CHECK(cudaEventRecord(ev_ready, st));
       ATLG_CHECK(cudaStreamWaitEvent(side, ev_ready, 0));
       const int nfar = N - far0;
-      apply_perm_kernel<T><<<(nfar + 31) / 32, 256, 0, side>>>(A, lda, k, perm, 0, far0, N);
-      note_launch();
-      ATLG_CHECK(cudaGetLastError());
-      dev_trsm_llnu_block(A, lda, k, jb, A + k + (size_t)far0 * lda, lda, nfar, side);
-      if (use_tc) {
-        const size_t rstride = (size_t)3 * ((jb + 31) / 32 * 32);   // floats per packed row
-        dev_sgemm_tf32x3_pack_b_rows(jb, nfar, (const float *)U12 + (size_t)nxt * lda, lda,
-                                     Bp + (size_t)nxt * rstride, side);
+      const size_t rstride = (size_t)3 * ((rk + 31) / 32 * 32);   // floats per packed row of B
+      block_row<T>(A, lda, k, jb, perm, far0, nfar, (use_tc && !defer) ? Bp + (size_t)nxt * rstride : nullptr, pend,
+                   side);
+      if (defer) {
+        ATLG_CHECK(cudaEventRecord(ev_first, side));
+      } else {
+        // the panel after next's columns as their own launch only where the
+        // update is fast enough for the panel chain to be the critical path
+        // (tensor-core updates); the FFMA/DFMA update is the critical path
+        // itself, and a split would only add a small, inefficient launch
+        const int nxt2 = (far0 < MN) ? ((MN - far0 < PW) ? MN - far0 : PW) : 0;
+        const int first = (use_tc && nxt2 > 0 && nxt2 < nfar) ? nxt2 : nfar;
+        trailing_update<T>(use_tc, m, first, rk, L21, U12, C, lda, nxt, ntot, Ap, Bp, side);
+        ATLG_CHECK(cudaEventRecord(ev_first, side));
+        if (first < nfar)
+          trailing_update<T>(use_tc, m, nfar - first, rk, L21, U12, C, lda, nxt + first, ntot, Ap, Bp, side);
       }
-      // the panel after next's columns as their own launch only where the
-      // update is fast enough for the panel chain to be the critical path
-      // (tensor-core updates); the FFMA/DFMA update is the critical path
-      // itself, and a split would only add a small, inefficient launch
-      const int nxt2 = (far0 < MN) ? ((MN - far0 < PW) ? MN - far0 : PW) : 0;
-      const int first = (use_tc && nxt2 > 0 && nxt2 < nfar) ? nxt2 : nfar;
-      trailing_update<T>(use_tc, m, first, jb, L21, U12, C, lda, nxt, ntot, Ap, Bp, side);
-      ATLG_CHECK(cudaEventRecord(ev_first, side));
       first_pending = true;
-      if (first < nfar) trailing_update<T>(use_tc, m, nfar - first, jb, L21, U12, C, lda, nxt + first, ntot, Ap, Bp, side);
-      if (nl > 0) {
-        apply_perm_kernel<T><<<nl, 256, 0, side>>>(A, lda, k, perm, k, N, N);
+      const int nlq = (kq + 31) / 32;                   // left columns (the deferred panel's are done)
+      if (nlq > 0) {
+        apply_perm_kernel<T><<<nlq, 256, 0, side>>>(A, lda, k, perm, kq, N, N);
         note_launch();
         ATLG_CHECK(cudaGetLastError());
       }
       ATLG_CHECK(cudaEventRecord(ev_side, side));
       side_pending = true;
+      pend = defer ? jb : 0;
       continue;
     }
     // otherwise everything on the caller's stream, after all side work

@@ -8,6 +8,9 @@ namespace atlg {
 // where the panel fits one cluster's shared memory); results are identical.
 void set_panel_cluster(bool on);
 void set_panel_split(bool on);
+// Rows at and below a panel above which the FP32 tensor-core factorization
+// pairs side steps into rank-2*NB far updates (0: never, negative: default).
+void set_defer_rows(int rows);
 // CTAs of the cooperative-grid panel (0: a quarter of the SMs with look-ahead,
 // more when the row slices would not fit shared memory).
 void set_panel_grid(int ctas);

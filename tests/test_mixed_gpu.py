@@ -143,3 +143,70 @@ def test_dgesv_mixed_n16384_kappa1e6(gb):
     fe = float((X - xp).abs().max() / xp.abs().max())
     assert fe <= 1e3 * kappa * np.finfo(float).eps, fe
     assert L.atlg_status() == 0
+
+
+def _sgetrf_tc(gb, A0, defer_rows):
+    """FP32 tensor-core factorization of A0 (float32, column-major) on the
+    GPU with the given deferral threshold (restored to the default after)."""
+    torch = pytest.importorskip("torch")
+    m, n = A0.shape
+    L = gb.lib()
+    A = torch.from_numpy(np.ascontiguousarray(A0.T)).cuda()      # column-major storage
+    piv = torch.zeros(min(m, n), dtype=torch.int32, device="cuda")
+    info = torch.zeros(4, dtype=torch.int32, device="cuda")
+    L.atlg_lu_defer_rows(defer_rows)
+    try:
+        torch.cuda.synchronize()
+        assert L.atlg_sgetrf_tc_dev(m, n, A.data_ptr(), m, piv.data_ptr(), info.data_ptr(), None) == 0
+        torch.cuda.synchronize()
+    finally:
+        L.atlg_lu_defer_rows(-1)
+    assert L.atlg_status() == 0
+    return A.cpu().numpy().T, piv.cpu().numpy(), int(info[0])
+
+
+@pytest.mark.parametrize("m,n,defer_rows", [(2048, 2048, 256), (1500, 1700, 320), (1700, 1500, 256),
+                                            (2048, 2048, 0)])
+def test_sgetrf_tc_paired_updates(gb, ora, m, n, defer_rows):
+    """The mixed solver's FP32 factorization with every other far update
+    deferred into the next step's rank-128 update (threshold lowered so that
+    small matrices pair steps; 0 = never): partial pivoting holds
+    (|l_ij| <= 1 below the diagonal) and the scaled residual
+    ||P A - L U||_1 / (k ||A||_1 eps32) stays within the LU tester's 100."""
+    A0 = ora.gegen(m, n, 4242 + m + n, dtype=np.float32)
+    F, piv, info = _sgetrf_tc(gb, A0, defer_rows)
+    assert info == 0
+    k = min(m, n)
+    assert np.all(piv >= np.arange(k)) and np.all(piv < m)
+    Lf = np.tril(F[:, :k].astype(np.float64), -1) + np.eye(m, k)
+    Uf = np.triu(F[:k, :].astype(np.float64))
+    assert np.abs(Lf).max() <= 1.0
+    PA = A0.astype(np.float64)
+    for i in range(k):
+        if piv[i] != i:
+            PA[[i, piv[i]]] = PA[[piv[i], i]]
+    R = PA - Lf @ Uf
+    resid = np.abs(R).sum(axis=0).max() / (k * np.abs(A0.astype(np.float64)).sum(axis=0).max() *
+                                           np.finfo(np.float32).eps)
+    assert resid <= 100.0, resid
+
+
+def test_dgesv_mixed_paired_updates_converge(gb, ora):
+    """The mixed solve with the factorization's steps paired down to 256 rows:
+    refinement converges to the FP64 backward error as with unpaired steps."""
+    n = 2049
+    L = gb.lib()
+    out = {}
+    for rows in (256, 0):
+        A, b = make_system(n, 1e4, 77)
+        A0 = A.copy(order="F")
+        X = np.zeros((n, 1), order="F")
+        L.atlg_lu_defer_rows(rows)
+        try:
+            info, berr, ferr, iters, status = gb.dgesv_mixed(A, np.zeros(n, dtype=np.int32), b.copy(order="F"), X)
+        finally:
+            L.atlg_lu_defer_rows(-1)
+        assert info == 0 and status == 0, (rows, status, iters)
+        assert ora.backward_error(A0, X[:, 0], b[:, 0]) <= n * np.finfo(float).eps
+        out[rows] = iters
+    assert out[256] <= out[0] + 2, out
