@@ -295,6 +295,11 @@ int atlg_sgetrf_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void 
  * LU with partial pivoting, trailing updates on the tensor cores in 3xTF32
  * (FP32-level accuracy); pivots follow the FP32 values it computes */
 int atlg_sgetrf_tc_dev(int M, int N, float *A, int lda, int *ipiv, int *info, void *stream);
+/* SA = A rounded to FP32 (to nearest even), the conversion the mixed solver
+ * factors (LAPACK dlag2s; no ATLAS counterpart); device arrays; returns 1
+ * when some |a| exceeds FLT_MAX (that entry becomes an infinity), 0
+ * otherwise, -1 for a bad argument; synchronizes the stream */
+int atlg_dlag2s_dev(int M, int N, const double *A, int lda, float *SA, int ldsa, void *stream);
 /* the split-DGEMM LU on device data (0-based device pivots), nslices 1..8,
  * outer block nb (rounded down to a multiple of 256; 1024 in dgesv_split);
  * returns info; synchronizes once per outer block */

@@ -26,7 +26,7 @@ EXPORTS = [
     "clapack_dgetrf", "clapack_sgetrf", "clapack_dgetrs", "clapack_sgetrs", "clapack_dgesv",
     "clapack_sgesv", "atlg_num_sms", "atlg_stream", "atlg_status", "atlg_dgemm_dev",
     "atlg_dgemm_dev_opts", "atlg_sgemm_dev", "atlg_dtrsm_dev", "atlg_dlaswp_dev", "atlg_dgetrf_dev",
-    "atlg_sgetrf_dev", "atlg_sgetrf_tc_dev", "atlg_dgetrs_dev", "atlg_launch_count", "atlg_prof_enable", "atlg_prof_collect",
+    "atlg_sgetrf_dev", "atlg_sgetrf_tc_dev", "atlg_dlag2s_dev", "atlg_dgetrs_dev", "atlg_launch_count", "atlg_prof_enable", "atlg_prof_collect",
     "atlg_probe_peaks", "atlg_probe_fp64_mma", "atlg_prof_panels", "atlg_prof_panels_collect", "dgesv_mixed", "dgesv_adjoint", "atlg_dgesv_mixed_dev", "atlg_dgesv_adjoint_dev",
     "atlg_dlaswp_noalloc", "dgemm_split", "atlg_dgemm_split_dev", "atlg_sgemm_tf32x3_dev",
     "cblas_dsyrk", "cblas_ssyrk", "clapack_dpotrf", "clapack_spotrf", "clapack_dpotrs", "clapack_spotrs",
@@ -130,6 +130,7 @@ def _declare(L):
         "atlg_dgetrf_dev": (_i, [_i, _i, _v, _i, _v, _v, _v]),
         "atlg_sgetrf_dev": (_i, [_i, _i, _v, _i, _v, _v, _v]),
         "atlg_sgetrf_tc_dev": (_i, [_i, _i, _v, _i, _v, _v, _v]),
+        "atlg_dlag2s_dev": (_i, [_i, _i, _v, _i, _v, _i, _v]),
         "atlg_dgetrs_dev": (_i, [_i, _i, _i, _i, _v, _i, _v, _v, _i, _v]),
         "dgesv_mixed": (_i, [_i, _i, _dp, _i, _ip, _dp, _i, _dp, _i, np.ctypeslib.ndpointer(np.float64),
                              np.ctypeslib.ndpointer(np.float64), C.POINTER(_i), C.POINTER(_i)]),

@@ -1218,6 +1218,10 @@ int atlg_sgetrf_tc_dev(int M, int N, float *A, int lda, int *ipiv, int *info, vo
   dev_sgetrf_tc(M, N, A, lda, ipiv, info, stream_of(stream));
   return 0;
 }
+int atlg_dlag2s_dev(int M, int N, const double *A, int lda, float *SA, int ldsa, void *stream) {
+  if (M < 0 || N < 0 || lda < (M > 1 ? M : 1) || ldsa < (M > 1 ? M : 1)) return -1;
+  return dev_dlag2s(M, N, A, lda, SA, ldsa, stream_of(stream));
+}
 int atlg_dgesv_mixed_dev(int N, int NRHS, double *A, int lda, int *ipiv, const double *B, int ldb, double *X,
                          int ldx, double *berr, double *ferr, int *iters, int *status, void *stream) {
   if (N < 0 || NRHS < 0) return -1;

@@ -8,7 +8,7 @@ namespace atlg {
 
 // Device buffer slots reused across calls (grown on demand, never shrunk).
 enum BufSlot {
-  kBufA = 0, kBufB, kBufC, kBufPiv, kBufInfo, kBufW0, kBufW1, kBufW2, kBufW3, kBufW4, kBufW5, kBufW6, kBufW7, kBufS0, kBufS1, kBufS2, kBufT0, kBufT1, kBufV0, kBufV1, kBufChol, kBufTrmm, kBufX0, kBufX1, kBufX2, kBufS3, kBufS4, kBufS5, kBufTri, kBufV2, kBufIamax, kBufTrsvL, kBufTrsvU, kBufGemv, kBufTrsmInv, kBufT2,
+  kBufA = 0, kBufB, kBufC, kBufPiv, kBufInfo, kBufW0, kBufW1, kBufW2, kBufW3, kBufW4, kBufW5, kBufW6, kBufW7, kBufS0, kBufS1, kBufS2, kBufT0, kBufT1, kBufV0, kBufV1, kBufChol, kBufTrmm, kBufX0, kBufX1, kBufX2, kBufS3, kBufS4, kBufS5, kBufTri, kBufV2, kBufIamax, kBufTrsvL, kBufTrsvU, kBufGemv, kBufTrsmInv, kBufT2, kBufRowPart, kBufFlag,
   kNumSlots
 };
 

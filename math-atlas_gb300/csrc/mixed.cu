@@ -19,6 +19,7 @@
 // the update x += d and the norms; the O(n^3) work is FP32.
 #include <float.h>
 #include <math.h>
+#include <string.h>
 #include <vector>
 
 #include "common.cuh"
@@ -82,22 +83,88 @@ __global__ void __launch_bounds__(256) colmax_kernel(int M, const T *__restrict_
   }
 }
 
-// row sums of |A| (n x n, column-major): a CTA owns 32 rows, warps stride columns
-__global__ void __launch_bounds__(256) rowabs_kernel(int M, int N, const double *__restrict__ A, int lda,
-                                                     double *rows) {
-  __shared__ double part[8][32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int i = blockIdx.x * 32 + lane;
-  double acc = 0.0;
-  if (i < M)
-    for (int k = w; k < N; k += 8) acc += fabs(A[i + (size_t)k * lda]);
-  part[w][lane] = acc;
-  __syncthreads();
-  if (w == 0 && i < M) {
-    double s = 0.0;
-    for (int q = 0; q < 8; ++q) s += part[q][lane];
-    rows[i] = s;
+// FP64 -> FP32 with IEEE round to nearest even, on the integer pipes: GB300
+// retires about two FP64 operations (conversions and compares included) per
+// SM per cycle, which would bound a 16384^2 copy at 0.43 ms per operation
+// per element.  NaN gives a quiet NaN, magnitudes beyond the float range
+// infinity, results below half the smallest float subnormal zero (with the
+// sign kept).  value = 1.M * 2^e; for a float subnormal result it is
+// F * 2^(e + 97) units of 2^-149, F = 2^52 + M.
+__device__ __forceinline__ uint32_t d2f_bits(uint64_t x) {
+  const uint32_t sign = (uint32_t)(x >> 32) & 0x80000000u;
+  const int E = (int)((x >> 52) & 0x7FF);
+  const uint64_t M = x & 0xFFFFFFFFFFFFFull;
+  if (E == 0x7FF) return sign | 0x7F800000u | (M ? 0x400000u | (uint32_t)(M >> 29) : 0u);
+  const int e = E - 1023;
+  if (e > 127) return sign | 0x7F800000u;
+  if (e >= -126) {
+    uint32_t b = ((uint32_t)(e + 127) << 23) | (uint32_t)(M >> 29);
+    const uint32_t rem = (uint32_t)(M & 0x1FFFFFFFu);
+    if (rem > 0x10000000u || (rem == 0x10000000u && (b & 1u))) b += 1u;   // a carry may reach infinity
+    return sign | b;
   }
+  const int sh = -(e + 97);   // 30 .. 53 for the float subnormal range
+  if (E == 0 || sh >= 54) return sign;
+  const uint64_t F = M | (1ull << 52);
+  uint32_t q = (uint32_t)(F >> sh);
+  const uint64_t rem = F & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+  if (rem > half || (rem == half && (q & 1u))) q += 1u;
+  return sign | q;
+}
+
+// The FP32 copy of A and the row sums of |A| (for ||A||_inf) in one pass over
+// A: a CTA converts a 256-row x 128-column tile (a thread per row, 16
+// columns' loads in flight at a time) and writes its rows' partial sums,
+// part[tile column][row]; rowsum_kernel adds the partials in a fixed order.
+// The sum of a group of 16 |a| is taken in FP32 from the converted values
+// (relative error below 2^-19, enough for a norm used in a stopping test and
+// an error estimate) and added in FP64; a group whose FP32 sum could
+// overflow (or holds a NaN) is summed again in FP64 from the FP64 values.
+// *overflow is set when some |a| exceeds FLT_MAX.
+constexpr int kCvRows = 256, kCvCols = 128;
+
+__global__ void __launch_bounds__(kCvRows)
+    d2s_rowabs_kernel(int M, int N, const double *__restrict__ A, int lda, float *__restrict__ S, int lds,
+                      double *__restrict__ part, int *overflow) {
+  const int i = blockIdx.x * kCvRows + threadIdx.x;
+  const int j0 = blockIdx.y * kCvCols;
+  const int jn = (N - j0 < kCvCols) ? N - j0 : kCvCols;
+  if (i >= M) return;
+  const unsigned long long *a = reinterpret_cast<const unsigned long long *>(A) + i + (size_t)j0 * lda;
+  float *s = S + i + (size_t)j0 * lds;
+  double acc = 0.0;
+  bool ovf = false;
+  for (int g = 0; g < jn; g += 16) {
+    unsigned long long v[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = (g + q < jn) ? a[(size_t)(g + q) * lda] : 0ull;
+    float sum = 0.f;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const uint32_t fb = d2f_bits(v[q]);
+      const unsigned long long ax = v[q] & 0x7FFFFFFFFFFFFFFFull;
+      ovf |= ax > 0x47EFFFFFE0000000ull && ax <= 0x7FF0000000000000ull;   // FLT_MAX < |a| <= inf
+      sum += __uint_as_float(fb & 0x7FFFFFFFu);
+      if (g + q < jn) s[(size_t)(g + q) * lds] = __uint_as_float(fb);
+    }
+    if (sum < 1e37f) {
+      acc += (double)sum;
+    } else {
+      double d = 0.0;
+      for (int q = 0; q < 16; ++q) d += fabs(__longlong_as_double((long long)v[q]));
+      acc += d;
+    }
+  }
+  if (part) part[(size_t)blockIdx.y * M + i] = acc;
+  if (ovf) *overflow = 1;
+}
+
+__global__ void rowsum_kernel(int M, int T, const double *__restrict__ part, double *__restrict__ rows) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M) return;
+  double s = 0.0;
+  for (int t = 0; t < T; ++t) s += part[(size_t)t * M + i];
+  rows[i] = s;
 }
 
 static int grid_for(long work) {
@@ -150,24 +217,33 @@ int dev_dgesv_mixed(int n, int nrhs, double *A, int lda, int *ipiv, const double
   int *dinfo = reinterpret_cast<int *>(small);
   int *dovf = dinfo + 1;
   double *dtmp = small + 2;
-  double *drows = dtmp + nrhs;
+  double *drows = dtmp + nrhs + 1;
 
-  // ||A||_inf and ||b_j||_inf in FP64
-  rowabs_kernel<<<(n + 31) / 32, 256, 0, st>>>(n, n, A, lda, drows);
-  note_launch();
-  const double anrm = colmax_host(n, 1, drows, n, dtmp, st)[0];
-  std::vector<double> bnrm = colmax_host(n, nrhs, B, ldb, dtmp, st);
+  // The FP32 copy of A with the row sums of |A| in the same pass, ||A||_inf
+  // and ||b_j||_inf, then the FP32 factorization; info, the overflow flag and
+  // the norms come back with one host synchronisation after it.
+  ATLG_CHECK(cudaMemsetAsync(dinfo, 0, 2 * sizeof(int), st));
+  {
+    const int tiles = (n + kCvCols - 1) / kCvCols;
+    double *part = static_cast<double *>(c.buffer(kBufRowPart, sizeof(double) * (size_t)tiles * n));
+    d2s_rowabs_kernel<<<dim3((n + kCvRows - 1) / kCvRows, tiles), kCvRows, 0, st>>>(n, n, A, lda, S, lds, part,
+                                                                                   dovf);
+    rowsum_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, tiles, part, drows);
+    colmax_kernel<double><<<1, 256, 0, st>>>(n, drows, n, dtmp);
+    colmax_kernel<double><<<nrhs, 256, 0, st>>>(n, B, ldb, dtmp + 1);
+    note_launch(4);
+    ATLG_CHECK(cudaGetLastError());
+  }
+  dev_sgetrf_tc(n, n, S, lds, ipiv, dinfo, st);
+  std::vector<double> head(3 + (size_t)nrhs);
+  ATLG_CHECK(cudaMemcpyAsync(head.data(), small, sizeof(double) * head.size(), cudaMemcpyDeviceToHost, st));
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  int hinfo[2];
+  memcpy(hinfo, head.data(), sizeof(hinfo));
+  const double anrm = head[2];
+  std::vector<double> bnrm(head.begin() + 3, head.end());
   const double eps = ldexp(1.0, -53);
   const double cte = anrm * eps * sqrt((double)n);
-
-  // FP32 factorization
-  ATLG_CHECK(cudaMemsetAsync(dinfo, 0, 2 * sizeof(int), st));
-  d2s_kernel<<<grid_for((long)n * n), 256, 0, st>>>(n, n, A, lda, S, lds, dovf);
-  note_launch();
-  dev_sgetrf_tc(n, n, S, lds, ipiv, dinfo, st);
-  int hinfo[2] = {0, 0};
-  ATLG_CHECK(cudaMemcpyAsync(hinfo, dinfo, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
-  ATLG_CHECK(cudaStreamSynchronize(st));
   bool fallback = hinfo[0] != 0 || hinfo[1] != 0;
 
   int iter = 0;
@@ -282,6 +358,23 @@ int dev_dgesv_mixed(int n, int nrhs, double *A, int lda, int *ipiv, const double
     ATLG_CHECK(cudaStreamSynchronize(st));
   }
   return 0;
+}
+
+// SA = A in FP32 (LAPACK dlag2s, the conversion dsgesv makes): returns 1
+// when some |a| exceeds FLT_MAX (those entries become infinities), else 0.
+int dev_dlag2s(int M, int N, const double *A, int lda, float *SA, int ldsa, cudaStream_t st) {
+  if (M <= 0 || N <= 0) return 0;
+  Context &c = ctx();
+  int *flag = static_cast<int *>(c.buffer(kBufFlag, sizeof(int)));
+  ATLG_CHECK(cudaMemsetAsync(flag, 0, sizeof(int), st));
+  d2s_rowabs_kernel<<<dim3((M + kCvRows - 1) / kCvRows, (N + kCvCols - 1) / kCvCols), kCvRows, 0, st>>>(
+      M, N, A, lda, SA, ldsa, nullptr, flag);
+  note_launch();
+  ATLG_CHECK(cudaGetLastError());
+  int h = 0;
+  ATLG_CHECK(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ATLG_CHECK(cudaStreamSynchronize(st));
+  return h;
 }
 
 }  // namespace atlg

@@ -19,5 +19,8 @@ int dev_dgesv_mixed(int n, int nrhs, double *A, int lda, int *ipiv, const double
 // Single right-hand side refinement solves: the chained 128-row TRSV (true)
 // or the tagged 64-row look-back TRSV (false).
 void set_refine_trsv_chained(bool on);
+// SA = A in FP32, round to nearest even (LAPACK dlag2s); returns 1 when some
+// |a| exceeds FLT_MAX, else 0.  Synchronizes the stream.
+int dev_dlag2s(int M, int N, const double *A, int lda, float *SA, int ldsa, cudaStream_t st);
 
 }  // namespace atlg

@@ -210,3 +210,61 @@ def test_dgesv_mixed_paired_updates_converge(gb, ora):
         assert ora.backward_error(A0, X[:, 0], b[:, 0]) <= n * np.finfo(float).eps
         out[rows] = iters
     assert out[256] <= out[0] + 2, out
+
+
+def _dlag2s_cases():
+    rng = np.random.default_rng(5)
+    parts = [rng.integers(0, 2**64, size=60000, dtype=np.uint64)]          # the whole double range, NaNs included
+    # exponents around the float range, random mantissas, and exact ties
+    # (the 29 bits dropped equal half a float ulp) with odd and even kept bits
+    e = rng.integers(1023 - 160, 1023 + 130, size=60000).astype(np.uint64)
+    m = rng.integers(0, 2**52, size=60000, dtype=np.uint64)
+    s = rng.integers(0, 2, size=60000).astype(np.uint64) << np.uint64(63)
+    parts.append(s | (e << np.uint64(52)) | m)
+    mt = (m & ~np.uint64(0x1FFFFFFF)) | np.uint64(0x10000000)
+    parts.append(s | (e << np.uint64(52)) | mt)
+    f32max = float(np.finfo(np.float32).max)
+    sub = 2.0 ** -149
+    special = [0.0, -0.0, 5e-324, 2.0 ** -1022, sub, sub / 2, sub * 1.5, sub * 2.5, sub * 0.75, sub * 0.5000001,
+               2.0 ** -126, 2.0 ** -126 - sub / 2, 2.0 ** -126 - sub, 1.0 + 2.0 ** -24, 1.0 + 3 * 2.0 ** -24,
+               1.0 + 2.0 ** -24 + 2.0 ** -52, f32max, f32max + 2.0 ** 103, f32max + 2.0 ** 103 - 2.0 ** 75,
+               2.0 ** 128, 1e300, np.inf, -np.inf, -f32max, np.nan, -1.0 / 3.0, np.pi]
+    parts.append(np.array(special, dtype=np.float64).view(np.uint64))
+    return np.concatenate(parts).view(np.float64)
+
+
+def test_dlag2s_rounds_to_nearest_even(gb):
+    """atlg_dlag2s_dev, the mixed solver's FP64 -> FP32 copy (IEEE round to
+    nearest even in integer arithmetic), against the host's conversion bit
+    for bit: random bit patterns over the whole double range, random values
+    and exact ties around the float range, the float subnormal range, the
+    FLT_MAX rounding boundary, zeros and infinities; NaN stays NaN.  Returns 1
+    when some |a| exceeds FLT_MAX, 0 otherwise; padding rows untouched."""
+    torch = pytest.importorskip("torch")
+    L = gb.lib()
+    x = _dlag2s_cases()
+    M, lda, ldsa = 997, 1000, 1003
+    N = (x.size + M - 1) // M
+    A = np.zeros((lda, N))
+    flat = np.zeros(M * N)
+    flat[:x.size] = x
+    A[:M, :] = flat.reshape(N, M).T
+    Ad = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()
+    Sd = torch.full((N, ldsa), 7.0, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    assert L.atlg_dlag2s_dev(M, N, Ad.data_ptr(), lda, Sd.data_ptr(), ldsa, None) == 1
+    S = Sd.cpu().numpy().T
+    with np.errstate(over="ignore", invalid="ignore"):
+        want = A[:M, :].astype(np.float32)
+    got = S[:M, :]
+    nan = np.isnan(want)
+    assert np.array_equal(np.isnan(got), nan)
+    assert np.array_equal(got[~nan].view(np.uint32), want[~nan].view(np.uint32))
+    assert np.all(S[M:, :] == 7.0)
+    # in range: no overflow reported
+    B = np.asfortranarray(np.random.default_rng(1).standard_normal((300, 200)))
+    Bd = torch.from_numpy(np.ascontiguousarray(B.T)).cuda()
+    Td = torch.zeros((200, 300), dtype=torch.float32, device="cuda")
+    assert L.atlg_dlag2s_dev(300, 200, Bd.data_ptr(), 300, Td.data_ptr(), 300, None) == 0
+    assert np.array_equal(Td.cpu().numpy().T, B.astype(np.float32))
+    assert L.atlg_dlag2s_dev(-1, 2, Bd.data_ptr(), 300, Td.data_ptr(), 300, None) == -1
