@@ -49,8 +49,13 @@ __device__ __forceinline__ int b_idx(int k, int n) {
   return TB == kNoTrans ? n * BK + k : k * BN + n;
 }
 
+// SUB: C -= op(A)*op(B) (alpha = -1, beta = 1, the LU's trailing update):
+// the accumulators start from C and take fma(-a, b, acc), so the epilogue is
+// a store -- no FP64 instruction besides the K DFMAs per element, where the
+// general epilogue spends two (alpha*acc, then beta*c + v) per K = 64 tile:
+// 3% of an FP64 pipe that bounds the kernel.
 template <typename T, int BM, int BN, int BK, int TM, int TN, int NT, int STAGES, int TA, int TB,
-          bool USE_TMA>
+          bool USE_TMA, bool SUB = false>
 __global__ void __launch_bounds__(NT)
     gemm_kernel(int M, int N, int K, T alpha, const T *__restrict__ A, int lda,
                 const T *__restrict__ B, int ldb, T beta, T *__restrict__ C, int ldc, int uplo, int tri,
@@ -87,10 +92,22 @@ __global__ void __launch_bounds__(NT)
   const int tx = tid % KC::GX, ty = tid / KC::GX;
 
   T acc[TM][TN];
+  if (SUB) {
 #pragma unroll
-  for (int i = 0; i < TM; ++i)
+    for (int j = 0; j < TN; ++j) {
+      const int n = n0 + ty + j * KC::GY;
 #pragma unroll
-    for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
+      for (int i = 0; i < TM; ++i) {
+        const int m = m0 + tx + i * KC::GX;
+        acc[i][j] = (m < M && n < N) ? C[m + (size_t)n * ldc] : T(0);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+      for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
+  }
 
   auto stageA = [&](int s) { return smem + s * KC::STAGE_ELEMS; };
   auto stageB = [&](int s) { return smem + s * KC::STAGE_ELEMS + KC::A_ELEMS; };
@@ -201,7 +218,7 @@ __global__ void __launch_bounds__(NT)
 #pragma unroll
       for (int i = 0; i < TM; ++i)
 #pragma unroll
-        for (int j = 0; j < TN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        for (int j = 0; j < TN; ++j) acc[i][j] = fma(SUB ? -a[i] : a[i], b[j], acc[i][j]);
     }
     if (USE_TMA) {
       __syncthreads();                       // every thread is done with stage s
@@ -224,8 +241,12 @@ __global__ void __launch_bounds__(NT)
     for (int i = 0; i < TM; ++i) {
       const int m = m0 + tx + i * KC::GX;
       if (m >= M || (uplo == kLower && m < n) || (uplo == kUpper && m > n)) continue;
-      const T v = alpha * acc[i][j];
-      c[m] = (beta == T(0)) ? v : fma(beta, c[m], v);
+      if (SUB) {
+        c[m] = acc[i][j];
+      } else {
+        const T v = alpha * acc[i][j];
+        c[m] = (beta == T(0)) ? v : fma(beta, c[m], v);
+      }
     }
   }
 }
@@ -254,7 +275,12 @@ static void launch_cfg(int M, int N, int K, T alpha, const T *A, int lda, const 
   }
   if (tma) {
     using KC = GemmKernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, true>;
-    auto k = gemm_kernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, true>;
+    // C -= op(A) op(B) in FP64 without epilogue arithmetic (the LU, TRSM and
+    // getrs updates); FP32 keeps the general form, whose rounding the
+    // reference-semantics sgetrf's pivots were checked with
+    const bool sub = sizeof(T) == 8 && alpha == T(-1) && beta == T(1) && uplo == 0 && tri == 0;
+    auto k = sub ? gemm_kernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, true, true>
+                 : gemm_kernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, true, false>;
     ATLG_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, KC::SMEM_BYTES));
     k<<<grid, NT, KC::SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, uplo, tri, tmA, tmB, 0L, 0L,
                                         0L);
