@@ -275,10 +275,11 @@ static void launch_cfg(int M, int N, int K, T alpha, const T *A, int lda, const 
   }
   if (tma) {
     using KC = GemmKernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, true>;
-    // C -= op(A) op(B) in FP64 without epilogue arithmetic (the LU, TRSM and
-    // getrs updates); FP32 keeps the general form, whose rounding the
+    // C -= op(A) op(B) in FP64 without epilogue arithmetic (the LU, TRSM,
+    // getrs and Cholesky updates; a SYRK's triangle mask still applies at the
+    // store); FP32 keeps the general form, whose rounding the
     // reference-semantics sgetrf's pivots were checked with
-    const bool sub = sizeof(T) == 8 && alpha == T(-1) && beta == T(1) && uplo == 0 && tri == 0;
+    const bool sub = sizeof(T) == 8 && alpha == T(-1) && beta == T(1) && tri == 0;
     auto k = sub ? gemm_kernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, true, true>
                  : gemm_kernel<T, BM, BN, BK, TM, TN, NT, STAGES, TA, TB, true, false>;
     ATLG_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, KC::SMEM_BYTES));
