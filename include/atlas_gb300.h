@@ -276,6 +276,12 @@ void atlg_panel_split(int on);
  * trailing matrix for two panels); default 12288, 0 never defers, negative
  * restores the default.  Factors agree to rounding */
 void atlg_lu_defer_rows(int rows);
+/* the mixed solver's FP32 factor (no reference counterpart): 1 (default) a
+ * full-width cluster panel applies the previous step's interchanges,
+ * block-row solve and FP32 update of its own columns as it loads them, 0
+ * leaves them to separate launches (3xTF32 update); factors agree to
+ * rounding */
+void atlg_panel_fuse(int on);
 /* refinement solves of dgesv_mixed with one right-hand side (no reference
  * counterpart): 1 (default) the chained TRSV over 128-row blocks with block
  * inverses formed once per factorization, 0 the 64-row look-back TRSV; both

@@ -35,7 +35,7 @@ EXPORTS = [
     "atlg_dtrmm_dev", "atlg_dgemv_dev", "atlg_dtrsv_dev", "atlg_strsv_chain_ws", "atlg_strsv_chain_prepare_dev",
     "atlg_strsv_chain_dev",
     "clapack_dtrtri", "clapack_strtri", "clapack_dgetri", "clapack_sgetri", "atlg_dtrtri_dev", "atlg_dgetri_dev",
-    "atlg_panel_cluster", "atlg_panel_split", "atlg_lu_defer_rows", "atlg_refine_trsv", "dgesv_split", "atlg_dgetrf_split_dev", "atlg_panel_grid", "atlg_split_lu_leaf", "atlg_panel_width",
+    "atlg_panel_cluster", "atlg_panel_split", "atlg_lu_defer_rows", "atlg_panel_fuse", "atlg_refine_trsv", "dgesv_split", "atlg_dgetrf_split_dev", "atlg_panel_grid", "atlg_split_lu_leaf", "atlg_panel_width",
     "cblas_idamax", "cblas_isamax", "atlg_idamax_dev", "atlg_isamax_dev",
 ]
 
@@ -108,6 +108,7 @@ def _declare(L):
         "atlg_panel_cluster": (None, [_i]),
         "atlg_panel_split": (None, [_i]),
         "atlg_lu_defer_rows": (None, [_i]),
+        "atlg_panel_fuse": (None, [_i]),
         "atlg_refine_trsv": (None, [_i]),
         "atlg_panel_grid": (None, [_i]),
         "atlg_split_lu_leaf": (None, [_i]),

@@ -1199,6 +1199,7 @@ int atlg_isamax_dev(int N, const float *X, int incX, int *result, void *stream) 
 void atlg_panel_cluster(int on) { set_panel_cluster(on != 0); }
 void atlg_panel_split(int on) { set_panel_split(on != 0); }
 void atlg_lu_defer_rows(int rows) { set_defer_rows(rows); }
+void atlg_panel_fuse(int on) { set_panel_fuse(on != 0); }
 void atlg_refine_trsv(int chained) { set_refine_trsv_chained(chained != 0); }
 void atlg_panel_grid(int ctas) { set_panel_grid(ctas); }
 void atlg_split_lu_leaf(int nb) { set_split_lu_leaf(nb); }

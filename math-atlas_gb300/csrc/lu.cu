@@ -471,9 +471,31 @@ __device__ __forceinline__ void row_axpy(T *row, const T *P, T l, int cb, int jb
   }
 }
 
+// The previous step's update of this panel's columns, applied by the panel
+// kernel itself as it loads them (FP32 factorization, full-width panels):
+// L = the previous panel (A(kp.., kp..), kp = koff - NB), perm its
+// interchange record (rows relative to kp); pw = NB, or 0 for none.  Each CTA
+// applies the interchanges to its rows, solves the previous block row
+// U12 = inv(L11) P A12 itself (a warp per four columns, from the unmodified
+// values in global memory) and takes rows -= L21 U12 in FP32; CTA 0 writes
+// U12 back after the cluster's last barrier, when every CTA has read what it
+// needed.  The interchanges, the block-row solve and the update of the next
+// panel's columns leave the path between two panels.
+struct PanelPend {
+  const float *L;
+  const int *perm;
+  int pw;
+};
+// U12 staged behind the panel's rows: 64 rows of four 16-column quarters at a
+// stride of 20 floats (16-byte loads of the four quarters hit distinct banks)
+constexpr int kPendUS = 80;
+constexpr size_t kPendSmem = sizeof(float) * (size_t)NB * kPendUS;   // also holds L11 during the solve
+
+// One CTA per SM (the panel's rows fill its shared memory): the whole
+// register file is the CTA's.
 template <typename T>
-__global__ void __launch_bounds__(CT)
-    panel_cluster_kernel(T *Ag, int lda, int M, int jb, int koff, int *ipiv, int *info, int *perm) {
+__global__ void __launch_bounds__(CT, 1)
+    panel_cluster_kernel(T *Ag, int lda, int M, int jb, int koff, int *ipiv, int *info, int *perm, PanelPend pd) {
   using V = typename Vec16<T>::type;
   using K = typename PivKey<T>::K;
   constexpr int VE = 16 / (int)sizeof(T);        // elements per 16-byte vector
@@ -516,6 +538,113 @@ __global__ void __launch_bounds__(CT)
   }
   cp_async_commit();
   cp_async_wait<0>();
+  float *us = nullptr;   // U12 of the pending update (CTA 0 writes it back at the end)
+  if constexpr (sizeof(T) == 4) {
+    if (pd.pw == NB && jb == NB) {
+      __shared__ int p_dst[2 * NB], p_src[2 * NB];
+      us = reinterpret_cast<float *>(panel_dyn + (size_t)chunk * RS * sizeof(T));
+      float *tri = us;                                   // L11 of the previous panel, then U12
+      const int pn = pd.perm[0];
+      for (int e = tid; e < pn; e += CT) {
+        p_dst[e] = pd.perm[1 + e];
+        p_src[e] = pd.perm[1 + 2 * NB + e];
+      }
+      for (int e = tid; e < NB * NB; e += CT) {
+        const int i = e & (NB - 1), jj = e / NB;
+        tri[e] = jj < i ? pd.L[i + (size_t)jj * lda] : 0.f;
+      }
+      __syncthreads();
+      // own rows that the previous interchanges fill with block-row contents
+      // (record entries NB.., whose sources are block rows: rows Ag - NB ..)
+      for (int e = tid; e < (pn - NB) * NB; e += CT) {
+        const int q = NB + e / NB, c = e % NB;
+        const int r = p_dst[q] - NB;                     // this panel's row
+        if (r >= r0 && r < r1 && p_dst[q] != p_src[q]) AT(r, c) = Ag[(p_src[q] - NB) + (size_t)c * lda];
+      }
+      // the previous block row's new rows (record entries 0..NB-1), solved:
+      // warp w owns columns w, w+16, w+32, w+48; lane l rows l and l+32
+      float x[4][2];
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) {
+        const float *col = Ag + (size_t)(w + 16 * cc) * lda - NB;
+        x[cc][0] = col[p_src[lane]];
+        x[cc][1] = col[p_src[lane + 32]];
+      }
+      for (int jj = 0; jj < NB - 1; ++jj) {
+        const int hi = jj >> 5;
+        float xj[4];
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) xj[cc] = __shfl_sync(0xffffffffu, hi ? x[cc][1] : x[cc][0], jj & 31);
+#pragma unroll
+        for (int s2 = 0; s2 < 2; ++s2) {
+          const int i = lane + 32 * s2;
+          if (i > jj) {
+            const float l = tri[jj * NB + i];
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) x[cc][s2] = fmaf(-l, xj[cc], x[cc][s2]);
+          }
+        }
+      }
+      __syncthreads();                                   // every warp is done with L11
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) {
+        const int c = w + 16 * cc;
+        us[lane * kPendUS + (c >> 4) * 20 + (c & 15)] = x[cc][0];
+        us[(lane + 32) * kPendUS + (c >> 4) * 20 + (c & 15)] = x[cc][1];
+      }
+      __syncthreads();
+      // rows -= L21 U12: thread (row pair p, quarter q) takes rows p and p+128
+      // of each 256-row pass, 16 columns, FMAs onto the row values
+      const int q4 = tid & 3, pr = tid >> 2;
+      const float *L21 = pd.L + NB;                      // row koff + i of the previous panel: L21[i]
+      for (int base = r0; base < r1; base += 256) {
+        const int ia = base + pr, ib = ia + 128;
+        const bool va = ia < r1, vb = ib < r1;
+        float ca[16], cb[16];
+        float4 *ra = reinterpret_cast<float4 *>(&AT(va ? ia : r0, q4 * 16));
+        float4 *rb = reinterpret_cast<float4 *>(&AT(vb ? ib : r0, q4 * 16));
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const float4 a4 = ra[v], b4 = rb[v];
+          ca[4 * v] = a4.x; ca[4 * v + 1] = a4.y; ca[4 * v + 2] = a4.z; ca[4 * v + 3] = a4.w;
+          cb[4 * v] = b4.x; cb[4 * v + 1] = b4.y; cb[4 * v + 2] = b4.z; cb[4 * v + 3] = b4.w;
+        }
+        for (int j0 = 0; j0 < NB; j0 += 16) {
+          // the 32 L values of this chunk in flight together (L2 latency, not
+          // the FMAs, bounds this loop otherwise)
+          float la[16], lb[16];
+#pragma unroll
+          for (int t = 0; t < 16; ++t) {
+            la[t] = va ? L21[ia + (size_t)(j0 + t) * lda] : 0.f;
+            lb[t] = vb ? L21[ib + (size_t)(j0 + t) * lda] : 0.f;
+          }
+#pragma unroll
+          for (int t = 0; t < 16; ++t) {
+            const float4 *u4 = reinterpret_cast<const float4 *>(us + (j0 + t) * kPendUS + q4 * 20);
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+              const float4 u = u4[v];
+              ca[4 * v] = fmaf(-la[t], u.x, ca[4 * v]);
+              ca[4 * v + 1] = fmaf(-la[t], u.y, ca[4 * v + 1]);
+              ca[4 * v + 2] = fmaf(-la[t], u.z, ca[4 * v + 2]);
+              ca[4 * v + 3] = fmaf(-la[t], u.w, ca[4 * v + 3]);
+              cb[4 * v] = fmaf(-lb[t], u.x, cb[4 * v]);
+              cb[4 * v + 1] = fmaf(-lb[t], u.y, cb[4 * v + 1]);
+              cb[4 * v + 2] = fmaf(-lb[t], u.z, cb[4 * v + 2]);
+              cb[4 * v + 3] = fmaf(-lb[t], u.w, cb[4 * v + 3]);
+            }
+          }
+        }
+        if (va)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) ra[v] = make_float4(ca[4 * v], ca[4 * v + 1], ca[4 * v + 2], ca[4 * v + 3]);
+        if (vb)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) rb[v] = make_float4(cb[4 * v], cb[4 * v + 1], cb[4 * v + 2], cb[4 * v + 3]);
+      }
+      __syncthreads();
+    }
+  }
   // bytes a CTA receives per column: CN candidate records and row j
   const unsigned TX = (unsigned)(16 * (CN * (nvj + 1) + nvj));
   if (tid == 0) {
@@ -721,6 +850,11 @@ __global__ void __launch_bounds__(CT)
   cluster.sync();
   if (me == 0)
     for (int t = tid; t < jb; t += CT) ipiv[t] = koff + piv_local[t];
+  if (sizeof(T) == 4 && us != nullptr && me == 0)   // the pending update's U12, rows Ag - NB ..
+    for (int e = tid; e < NB * NB; e += CT) {
+      const int i = e & (NB - 1), c = e / NB;
+      reinterpret_cast<float *>(Ag)[(i - NB) + (size_t)c * lda] = us[i * kPendUS + (c >> 4) * 20 + (c & 15)];
+    }
   // warp 0 of the last CTA reduces the interchanges while its other warps
   // (and every other CTA) write the rows back: a thread per row, 16-byte
   // shared-memory reads, stores coalesced over the warp's consecutive rows
@@ -1600,6 +1734,10 @@ void set_panel_split(bool on) { g_panel_split = on; }
 // 12288 in steps of 2048).
 constexpr int kDeferRowsDefault = 12288;
 static int g_defer_rows = kDeferRowsDefault;
+// FP32 tensor-core factorization: the next panel applies a step's update of
+// its columns itself (PanelPend) where it can
+static bool g_panel_fuse = true;
+void set_panel_fuse(bool on) { g_panel_fuse = on; }
 void set_defer_rows(int rows) { g_defer_rows = rows < 0 ? kDeferRowsDefault : rows > 0 ? rows : INT_MAX; }
 static int g_panel_grid = 0;   // CTAs of the grid panel; 0: the default below
 void set_panel_grid(int ctas) { g_panel_grid = ctas > 0 ? ctas : 0; }
@@ -1671,6 +1809,9 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     return tc && M - kk - jbk >= 256 && N - kk - jbk >= 128;
   };
   int pend = 0;
+  // the next-panel update a step hands to the next panel's kernel (FP32
+  // tensor-core factorization; PanelPend)
+  PanelPend next_pend = {nullptr, nullptr, 0};
   if (tc && lookahead) {   // the packings at their largest (rank 2 PW) once, before any side-stream use
     c.buffer(kBufT0, sizeof(float) * tf32x3_packed_floats(M, 2 * PW, false));
     c.buffer(kBufT2, sizeof(float) * tf32x3_packed_floats(M, 2 * PW, false));
@@ -1695,7 +1836,7 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
     auto cluster_tile = [&](int rows, int width) -> size_t {
       return cn ? sizeof(T) * (size_t)((rows + cn - 1) / cn) * cl_rs<T>(width) : 0;
     };
-    auto launch_cluster = [&](T *Apan, int rows, int width, int kof, int *ip, size_t tile) {
+    auto launch_cluster = [&](T *Apan, int rows, int width, int kof, int *ip, size_t tile, PanelPend pd) {
       cudaLaunchConfig_t cfg = {};
       cudaLaunchAttribute at[1];
       cfg.gridDim = dim3(cn);
@@ -1708,20 +1849,26 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
       at[0].val.clusterDim.z = 1;
       cfg.attrs = at;
       cfg.numAttrs = 1;
-      ATLG_CHECK(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T>, Apan, lda, rows, width, kof, ip, info, perm));
+      ATLG_CHECK(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T>, Apan, lda, rows, width, kof, ip, info, perm, pd));
     };
+    const PanelPend none = {nullptr, nullptr, 0};
     const size_t ctile = cluster_tile(Mp, jb);
     const int h = jb / 2;
     const size_t htile = cluster_tile(Mp, jb - h);   // the taller half is the left one
+    if (next_pend.pw && !(cn && jb == NB && ctile + kPendSmem <= cmax)) {
+      fprintf(stderr, "atlas_gb300: getrf: a pending panel update without room for it\n");
+      abort();
+    }
     if (cn && ctile <= cmax) {
-      launch_cluster(Ap, Mp, jb, koff, ipk, ctile);
+      launch_cluster(Ap, Mp, jb, koff, ipk, ctile + (next_pend.pw ? kPendSmem : 0), next_pend);
+      next_pend = none;
       used_cluster = true;
     } else if (cn && g_panel_split && h >= 8 && htile <= cmax) {
       T *Ar = A + k + (size_t)(k + h) * lda;          // rows k.. of the right half
-      launch_cluster(Ap, Mp, h, koff, ipk, htile);
+      launch_cluster(Ap, Mp, h, koff, ipk, htile, none);
       block_row<T>(A, lda, k, h, perm, k + h, jb - h, nullptr, 0, st);
       gemm_any<T>(Mp - h, jb - h, h, Ap + h, lda, Ar, lda, Ar + h, lda, st);
-      launch_cluster(Ar + h, Mp - h, jb - h, koff + h, ipk + h, cluster_tile(Mp - h, jb - h));
+      launch_cluster(Ar + h, Mp - h, jb - h, koff + h, ipk + h, cluster_tile(Mp - h, jb - h), none);
       apply_perm_kernel<T><<<(h + 31) / 32, 256, 0, st>>>(A, lda, k + h, perm, 0, k, k + h);
       panel_perm_kernel<<<1, 32, 0, st>>>(ipk, jb, koff, perm);
       note_launch(3);   // with the one below: two panels, the left half's interchanges, the record
@@ -1767,6 +1914,10 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
       const bool use_tc = tc && m >= 256 && ntot >= 128;
       const bool defer = pend == 0 && use_tc && jb == PW && M - k >= g_defer_rows && side_step_at(k + PW) &&
                          tc_at(k + PW);
+      // the next panel applies this step's update of its columns itself when
+      // it is one full-width cluster panel with room for the staged block row
+      const bool fuse = sizeof(T) == 4 && g_panel_fuse && use_tc && !defer && pend == 0 && jb == NB &&
+                        nxt == NB && cn && cluster_tile(M - c_from, NB) + kPendSmem <= cmax;
       const int kq = k - pend;                          // this step's update: L columns kq..k+jb-1
       const int rk = pend + jb;                         // its rank
       const T *L21 = A + (k + jb) + (size_t)kq * lda;
@@ -1783,11 +1934,16 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
                                            sizeof(float) * tf32x3_packed_floats(m, rk, false)));
         Bp = static_cast<float *>(c.buffer(kBufT1, sizeof(float) * tf32x3_packed_floats(ntot, rk, true)));
       }
-      block_row<T>(A, lda, k, jb, perm, c_from, nxt, Bp, pend, st);
-      if (use_tc) dev_sgemm_tf32x3_pack_a(m, rk, (const float *)L21, lda, Ap, st);
-      trailing_update<T>(use_tc, m, nxt, rk, L21, U12, C, lda, 0, ntot, Ap, Bp, st);
+      if (fuse) {
+        next_pend = {reinterpret_cast<const float *>(A + k + (size_t)k * lda), perm, NB};
+      } else {
+        block_row<T>(A, lda, k, jb, perm, c_from, nxt, Bp, pend, st);
+        if (use_tc) dev_sgemm_tf32x3_pack_a(m, rk, (const float *)L21, lda, Ap, st);
+        trailing_update<T>(use_tc, m, nxt, rk, L21, U12, C, lda, 0, ntot, Ap, Bp, st);
+      }
       ATLG_CHECK(cudaEventRecord(ev_ready, st));
       ATLG_CHECK(cudaStreamWaitEvent(side, ev_ready, 0));
+      if (fuse) dev_sgemm_tf32x3_pack_a(m, rk, (const float *)L21, lda, Ap, side);
       const int nfar = N - far0;
       const size_t rstride = (size_t)3 * ((rk + 31) / 32 * 32);   // floats per packed row of B
       block_row<T>(A, lda, k, jb, perm, far0, nfar, (use_tc && !defer) ? Bp + (size_t)nxt * rstride : nullptr, pend,

@@ -11,6 +11,9 @@ void set_panel_split(bool on);
 // Rows at and below a panel above which the FP32 tensor-core factorization
 // pairs side steps into rank-2*NB far updates (0: never, negative: default).
 void set_defer_rows(int rows);
+// true (default): in the FP32 tensor-core factorization a full-width cluster
+// panel applies the previous step's update of its columns itself
+void set_panel_fuse(bool on);
 // CTAs of the cooperative-grid panel (0: a quarter of the SMs with look-ahead,
 // more when the row slices would not fit shared memory).
 void set_panel_grid(int ctas);

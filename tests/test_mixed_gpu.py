@@ -145,9 +145,10 @@ def test_dgesv_mixed_n16384_kappa1e6(gb):
     assert L.atlg_status() == 0
 
 
-def _sgetrf_tc(gb, A0, defer_rows):
+def _sgetrf_tc(gb, A0, defer_rows, fuse=1):
     """FP32 tensor-core factorization of A0 (float32, column-major) on the
-    GPU with the given deferral threshold (restored to the default after)."""
+    GPU with the given deferral threshold and panel fusion (both restored to
+    their defaults after)."""
     torch = pytest.importorskip("torch")
     m, n = A0.shape
     L = gb.lib()
@@ -155,26 +156,30 @@ def _sgetrf_tc(gb, A0, defer_rows):
     piv = torch.zeros(min(m, n), dtype=torch.int32, device="cuda")
     info = torch.zeros(4, dtype=torch.int32, device="cuda")
     L.atlg_lu_defer_rows(defer_rows)
+    L.atlg_panel_fuse(fuse)
     try:
         torch.cuda.synchronize()
         assert L.atlg_sgetrf_tc_dev(m, n, A.data_ptr(), m, piv.data_ptr(), info.data_ptr(), None) == 0
         torch.cuda.synchronize()
     finally:
         L.atlg_lu_defer_rows(-1)
+        L.atlg_panel_fuse(1)
     assert L.atlg_status() == 0
     return A.cpu().numpy().T, piv.cpu().numpy(), int(info[0])
 
 
-@pytest.mark.parametrize("m,n,defer_rows", [(2048, 2048, 256), (1500, 1700, 320), (1700, 1500, 256),
-                                            (2048, 2048, 0)])
-def test_sgetrf_tc_paired_updates(gb, ora, m, n, defer_rows):
+@pytest.mark.parametrize("m,n,defer_rows,fuse", [(2048, 2048, 256, 1), (1500, 1700, 320, 1), (1700, 1500, 256, 1),
+                                                 (2048, 2048, 0, 1), (2048, 2048, 0, 0), (1700, 1500, 0, 1),
+                                                 (1500, 1700, 0, 0), (3000, 3000, 1024, 1)])
+def test_sgetrf_tc_paired_updates(gb, ora, m, n, defer_rows, fuse):
     """The mixed solver's FP32 factorization with every other far update
     deferred into the next step's rank-128 update (threshold lowered so that
-    small matrices pair steps; 0 = never): partial pivoting holds
-    (|l_ij| <= 1 below the diagonal) and the scaled residual
+    small matrices pair steps; 0 = never), and with the next panel applying a
+    step's update of its columns itself (fuse 1) or not: partial pivoting
+    holds (|l_ij| <= 1 below the diagonal) and the scaled residual
     ||P A - L U||_1 / (k ||A||_1 eps32) stays within the LU tester's 100."""
     A0 = ora.gegen(m, n, 4242 + m + n, dtype=np.float32)
-    F, piv, info = _sgetrf_tc(gb, A0, defer_rows)
+    F, piv, info = _sgetrf_tc(gb, A0, defer_rows, fuse)
     assert info == 0
     k = min(m, n)
     assert np.all(piv >= np.arange(k)) and np.all(piv < m)
@@ -192,24 +197,27 @@ def test_sgetrf_tc_paired_updates(gb, ora, m, n, defer_rows):
 
 
 def test_dgesv_mixed_paired_updates_converge(gb, ora):
-    """The mixed solve with the factorization's steps paired down to 256 rows:
-    refinement converges to the FP64 backward error as with unpaired steps."""
+    """The mixed solve with the factorization's steps paired down to 256 rows,
+    and with the next-panel updates in the panel kernel or not: refinement
+    converges to the FP64 backward error as with unpaired, separate steps."""
     n = 2049
     L = gb.lib()
     out = {}
-    for rows in (256, 0):
+    for rows, fuse in ((256, 1), (0, 1), (0, 0)):
         A, b = make_system(n, 1e4, 77)
         A0 = A.copy(order="F")
         X = np.zeros((n, 1), order="F")
         L.atlg_lu_defer_rows(rows)
+        L.atlg_panel_fuse(fuse)
         try:
             info, berr, ferr, iters, status = gb.dgesv_mixed(A, np.zeros(n, dtype=np.int32), b.copy(order="F"), X)
         finally:
             L.atlg_lu_defer_rows(-1)
-        assert info == 0 and status == 0, (rows, status, iters)
+            L.atlg_panel_fuse(1)
+        assert info == 0 and status == 0, (rows, fuse, status, iters)
         assert ora.backward_error(A0, X[:, 0], b[:, 0]) <= n * np.finfo(float).eps
-        out[rows] = iters
-    assert out[256] <= out[0] + 2, out
+        out[(rows, fuse)] = iters
+    assert max(out.values()) <= min(out.values()) + 2, out
 
 
 def _dlag2s_cases():
