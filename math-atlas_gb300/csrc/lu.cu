@@ -920,6 +920,46 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The interchanges of several steps on the columns left of their panels, in
+// step order, in one launch: record r (perm0 + off[r], rows relative to k[r])
+// applies to columns [0, kq[r]).  Only the finished factorization reads
+// those columns, so a step's interchanges can wait for the batch.
+constexpr int kPermBatch = 8;
+struct PermBatch {
+  int n;
+  int k[kPermBatch], kq[kPermBatch], off[kPermBatch];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) apply_perm_batch_kernel(T *A, int lda, const int *perm0, PermBatch b) {
+  constexpr int CB = 32;
+  __shared__ T v[2 * NB][CB];
+  __shared__ int dst[2 * NB], src[2 * NB];
+  const int c0 = blockIdx.x * CB;
+  for (int r = 0; r < b.n; ++r) {
+    if (c0 >= b.kq[r]) continue;                     // the same for the whole CTA
+    const int *perm = perm0 + b.off[r];
+    const int k = b.k[r];
+    const int n = perm[0];
+    __syncthreads();                                 // the previous record's stores are done
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+      dst[t] = perm[1 + t];
+      src[t] = perm[1 + 2 * NB + t];
+    }
+    __syncthreads();
+    const int ncols = (b.kq[r] - c0 < CB) ? b.kq[r] - c0 : CB;
+    for (int e = threadIdx.x; e < n * ncols; e += blockDim.x) {
+      const int t = e % n, c = e / n;
+      v[t][c] = A[k + src[t] + (size_t)(c0 + c) * lda];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * ncols; e += blockDim.x) {
+      const int t = e % n, c = e / n;
+      if (dst[t] != src[t]) A[k + dst[t] + (size_t)(c0 + c) * lda] = v[t][c];
+    }
+  }
+}
+
 // The block row of step k of the FP32 factorization for the columns
 // [c0, c0 + ncols), in one launch: the panel's interchanges (record perm,
 // rows relative to k), the solve with the panel's unit-lower jb x jb block
@@ -1812,6 +1852,18 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
   // the next-panel update a step hands to the next panel's kernel (FP32
   // tensor-core factorization; PanelPend)
   PanelPend next_pend = {nullptr, nullptr, 0};
+  // interchanges of the columns left of the panels, batched on the side stream
+  PermBatch lbatch;
+  lbatch.n = 0;
+  auto flush_left = [&](cudaStream_t s) {
+    if (lbatch.n == 0) return;
+    int maxq = 0;
+    for (int r = 0; r < lbatch.n; ++r) maxq = lbatch.kq[r] > maxq ? lbatch.kq[r] : maxq;
+    apply_perm_batch_kernel<T><<<(maxq + 31) / 32, 256, 0, s>>>(A, lda, perm0, lbatch);
+    note_launch();
+    ATLG_CHECK(cudaGetLastError());
+    lbatch.n = 0;
+  };
   if (tc && lookahead) {   // the packings at their largest (rank 2 PW) once, before any side-stream use
     c.buffer(kBufT0, sizeof(float) * tf32x3_packed_floats(M, 2 * PW, false));
     c.buffer(kBufT2, sizeof(float) * tf32x3_packed_floats(M, 2 * PW, false));
@@ -1963,11 +2015,11 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
           trailing_update<T>(use_tc, m, nfar - first, rk, L21, U12, C, lda, nxt + first, ntot, Ap, Bp, side);
       }
       first_pending = true;
-      const int nlq = (kq + 31) / 32;                   // left columns (the deferred panel's are done)
-      if (nlq > 0) {
-        apply_perm_kernel<T><<<nlq, 256, 0, side>>>(A, lda, k, perm, kq, N, N);
-        note_launch();
-        ATLG_CHECK(cudaGetLastError());
+      if (kq > 0) {                                     // left columns (the deferred panel's are done)
+        lbatch.k[lbatch.n] = k;
+        lbatch.kq[lbatch.n] = kq;
+        lbatch.off[lbatch.n] = (k / PW) * kPermInts;
+        if (++lbatch.n == kPermBatch) flush_left(side);
       }
       ATLG_CHECK(cudaEventRecord(ev_side, side));
       side_pending = true;
@@ -1975,6 +2027,11 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
       continue;
     }
     // otherwise everything on the caller's stream, after all side work
+    if (lbatch.n) {
+      flush_left(side);
+      ATLG_CHECK(cudaEventRecord(ev_side, side));
+      side_pending = true;
+    }
     if (side_pending) {
       ATLG_CHECK(cudaStreamWaitEvent(st, ev_side, 0));
       side_pending = false;
@@ -2004,6 +2061,11 @@ static void getrf_impl(int M, int N, T *A, int lda, int *ipiv, int *info, cudaSt
         trailing_update<T>(use_tc, m, ntot, jb, L21, U12, C, lda, 0, ntot, Ap, Bp, st);
       }
     }
+  }
+  if (lbatch.n) {
+    flush_left(side);
+    ATLG_CHECK(cudaEventRecord(ev_side, side));
+    side_pending = true;
   }
   if (side_pending) ATLG_CHECK(cudaStreamWaitEvent(st, ev_side, 0));
 }
