@@ -549,10 +549,12 @@ __global__ void __launch_bounds__(CT, 1)
         p_dst[e] = pd.perm[1 + e];
         p_src[e] = pd.perm[1 + 2 * NB + e];
       }
-      for (int e = tid; e < NB * NB; e += CT) {
+      for (int e = tid; e < NB * NB; e += CT) {   // asynchronous copies, all in flight
         const int i = e & (NB - 1), jj = e / NB;
-        tri[e] = jj < i ? pd.L[i + (size_t)jj * lda] : 0.f;
+        cp_async4(&tri[e], jj < i ? pd.L + i + (size_t)jj * lda : pd.L, jj < i);
       }
+      cp_async_commit();
+      cp_async_wait<0>();
       __syncthreads();
       // own rows that the previous interchanges fill with block-row contents
       // (record entries NB.., whose sources are block rows: rows Ag - NB ..)
@@ -999,11 +1001,20 @@ __global__ void __launch_bounds__(kBrWarps * 32)
     dst[e] = perm[1 + e];
     src[e] = perm[1 + 2 * NB + e];
   }
+  // L11 (and Lp) as asynchronous copies, zero fill outside the triangle: all
+  // of a thread's loads in flight at once (a load-then-store loop waited for
+  // each in turn and dominated the kernel's latency)
   for (int e = t; e < NB * NB; e += kBrWarps * 32) {
     const int i = e & (NB - 1), j = e / NB;
-    tri[e] = (j < i && i < jb) ? A[k + i + (size_t)(k + j) * lda] : 0.f;
-    if (jp) lp[e] = (i < jb) ? A[k + i + (size_t)(k - jp + j) * lda] : 0.f;
+    const bool ok = j < i && i < jb;
+    cp_async4(&tri[e], ok ? A + k + i + (size_t)(k + j) * lda : A, ok);
+    if (jp) {
+      const bool okp = i < jb;
+      cp_async4(&lp[e], okp ? A + k + i + (size_t)(k - jp + j) * lda : A, okp);
+    }
   }
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
   // gather: every load of the warp's columns issued before the first store
   float v[kBrCpw][4];
